@@ -1,0 +1,251 @@
+/*
+ * microlc_gb300.h -- C ABI of the GB300-native microLC light-curve hot path.
+ *
+ * The reference (gvernard/microSN, package microLC) exposes this path as C++ free
+ * functions over host structs that own device buffers
+ * (simulating_lcurves/include/gpu_functions.hpp:11-18, cpu_functions.hpp:12-15,
+ * chi2/chi2_functions.cuh:93).  This header replaces them with plain-pointer C entry
+ * points that a cgo / ctypes / C++ caller can bind; the C++ shim in
+ * microsn_gb300/csrc/microlc_compat.hpp rebuilds the reference's own signatures on top.
+ *
+ * Conventions
+ *  - Every entry returns an int status: MLC_OK (0) or one of MLC_ERR_*; the text of
+ *    the last failure is available from mlc_ctx_last_error().
+ *  - Array arguments are DEVICE pointers unless their name ends in _host.  Device
+ *    pointers are borrowed: the library never frees them.
+ *  - Work is queued on the context's stream; entries that return host results
+ *    synchronise that stream before returning.
+ *  - A context is used by one host thread at a time.
+ *  - The library is built for sm_103a only and fails with MLC_ERR_CUDA elsewhere.
+ */
+#ifndef MICROLC_GB300_H
+#define MICROLC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define MLC_OK 0
+#define MLC_ERR_ARG 1         /* bad argument (null, size, unsupported length) */
+#define MLC_ERR_OOM 2         /* device or host allocation failed */
+#define MLC_ERR_CUDA 3        /* CUDA runtime / launch failure */
+#define MLC_ERR_TIMEOUT 4     /* a bounded device-side wait gave up */
+#define MLC_ERR_UNSUPPORTED 5 /* valid request the library does not implement */
+#define MLC_ERR_LIMIT 6       /* size beyond a documented limit */
+
+/* ---- precisions ---- */
+#define MLC_F64 0
+#define MLC_F32 1
+
+/* ---- profile shapes (profile.hpp:112-170 factory keys, plus limb_darkened) ---- */
+#define MLC_SHAPE_UNIFORM 0       /* "uniform"       profile.cpp:185-222 */
+#define MLC_SHAPE_GAUSSIAN 1      /* "gaussian"      profile.cpp:228-263 */
+#define MLC_SHAPE_GAUSSIAN_HOLE 2 /* "gaussian_hole" profile.cpp:269-311 */
+#define MLC_SHAPE_THERMAL_HOLE 3  /* "thermal_hole"  profile.cpp:315-354 */
+#define MLC_SHAPE_WAVY 4          /* "wavy"          profile.cpp:358-398 */
+#define MLC_SHAPE_EXPONENTIAL 5   /* "exponential" (thin disc) profile.cpp:402-446 */
+#define MLC_SHAPE_LIMB_DARKENED 6 /* linear limb-darkened disc (no reference counterpart) */
+
+/* ---- convolution modes ---- */
+#define MLC_CONV_FUSED 0 /* profile spectrum generated from the small raster, multiply fused */
+#define MLC_CONV_PLAIN 1 /* full-size wrapped kernel, forward FFT, multiply, inverse: one launch per stage */
+
+typedef struct mlc_ctx mlc_ctx;
+typedef struct mlc_map mlc_map;
+
+/* Source profile description.  Physical units are those of pix (the reference uses
+ * 10^14 cm; any consistent unit works).  ref_compat = 1 passes rhalf, pix, incl, orient,
+ * Rin and a through the reference's std::to_string / std::stof round trip
+ * (gpu_functions.cu:108,184) and keeps its exponential-core overwrite
+ * (profile.cpp:435-441), so rasters are bit-identical to the reference's. */
+typedef struct {
+  int shape;
+  int ref_compat;
+  double rhalf;  /* half-light radius */
+  double pix;    /* pixel size */
+  double incl;   /* degrees */
+  double orient; /* degrees */
+  double Rin;    /* gaussian_hole inner radius */
+  double a;      /* wavy amplitude */
+  double u;      /* limb-darkening coefficient */
+} mlc_profile;
+
+/* ======================================================================= context */
+
+/* New context on `device`, queueing work on `stream` (a cudaStream_t; NULL = the
+ * legacy default stream).  No reference counterpart: the reference uses the default
+ * stream and global __constant__ state (gpu_functions.cu:25-33). */
+int mlc_ctx_create(int device, void* stream, mlc_ctx** out);
+int mlc_ctx_destroy(mlc_ctx* ctx);
+int mlc_ctx_set_stream(mlc_ctx* ctx, void* stream);
+int mlc_ctx_synchronize(mlc_ctx* ctx);
+const char* mlc_ctx_last_error(const mlc_ctx* ctx);
+/* Bytes of device workspace the context currently holds (grow-only pool). */
+size_t mlc_ctx_workspace_bytes(const mlc_ctx* ctx);
+/* Library version (major*10000 + minor*100 + patch). */
+int mlc_version(void);
+
+/* ======================================================================= profiles (host) */
+
+/* Side length N of the N x N raster (profile.cpp:197, 241, 285, 329, 373, 415). */
+int mlc_profile_dims(const mlc_profile* p, int* N);
+/* Normalised N x N raster into out_host (capacity cap doubles), FP64 on the host,
+ * replacing FactoryProfile::createProfileFromHalfRadius (profile.hpp:142-166). */
+int mlc_profile_raster(const mlc_profile* p, double* out_host, long cap, int* N);
+
+/* ======================================================================= maps */
+
+/* A map resident on the device in `precision` (MLC_F64 / MLC_F32), Ny rows of Nx
+ * pixels, row-major (the layout of MagnificationMap::data, magnification_map.cpp:33-38).
+ * `data` is FP64 (data_dtype MLC_F64) or FP32 (MLC_F32), on the device if data_is_device
+ * else on the host.  Nx and Ny must be even and factor into 2, 3 and 5. */
+int mlc_map_create(mlc_ctx* ctx, const void* data, int data_is_device, int data_dtype, int Nx, int Ny,
+                   int precision, mlc_map** out);
+int mlc_map_destroy(mlc_map* map);
+/* Device pointer to the map's pixels (precision of the map). */
+int mlc_map_data(mlc_map* map, void** dev_ptr);
+/* Forward spectrum of the map (computed once and cached), replacing the
+ * cufftExecD2Z of the map (gpu_functions.cu:171-176). */
+int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map);
+
+/* ======================================================================= convolution */
+
+/* Convolve the map with one profile into out (Ny x Nx, the map's precision), the
+ * per-profile body of expanding_source (gpu_functions.cu:183-201): kernel wrap
+ * (magnification_map.cpp:172-193), forward transform, multiply / (Nx Ny)
+ * (kernel_multiplyFFTs :571-577) and inverse transform, with hand-written FFTs. */
+int mlc_convolve(mlc_ctx* ctx, mlc_map* map, const mlc_profile* prof, int mode, void* out);
+
+/* Replaces expanding_source (gpu_functions.cu:82-225) for an FP64 map: LC (Nloc x Nprof)
+ * and DLC (Nloc x (Nprof-1)), location-major like SimLC (data_structs.hpp:50-63).
+ * sizes_host[k] are half-light radii in Einstein radii (sizes_host[0] must be 0, the
+ * point source); the profile for k >= 1 has rhalf = sizes_host[k] * base->pix * Nx / width
+ * and base's other fields.  loc_x, loc_y: Nloc int pixel indices.  mode: MLC_CONV_*. */
+int mlc_expanding_source(mlc_ctx* ctx, mlc_map* map, const double* sizes_host, int Nprof,
+                         const mlc_profile* base, double width, int Nloc, const int* loc_x,
+                         const int* loc_y, int mode, double* LC, double* DLC);
+
+/* ======================================================================= sampling */
+
+/* kernel_sample (gpu_functions.cu:604-620): LC[id*Nprof+k] = map[loc_y*Nx+loc_x] and,
+ * for k > 0, DLC[id*(Nprof-1)+k-1] = LC[id*Nprof+k] - LC[id*Nprof+k-1]. FP64 map of
+ * Ny x Nx; a location outside the map yields NaN instead of an out-of-range read. */
+int mlc_sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int Nprof, int Nloc,
+                       const int* loc_x, const int* loc_y, double* LC, double* DLC);
+
+/* Straight source tracks (no reference counterpart; bilinear formula of
+ * RectGrid::interp2d_bilinear, rectGrid.cpp:349-378, pixel centres at j + 1/2).
+ * Track k is at (x0 + v t cos phi, y0 + v t sin phi) pixels at each of its epoch times
+ * t[off[k] .. off[k+1]).  `maps` holds nmaps device pointers to Ny x Nx maps of
+ * `precision`; x0, y0, phi, v, t are in that precision; off is int64 (ntracks+1).
+ * out[m * E + e] (E = off[ntracks]) is -2.5 log10(mu) when mag != 0, else mu.
+ * A position outside the hull of pixel centres samples 0 (magnitude +inf). */
+int mlc_sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny, int precision,
+                      int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
+                      const int64_t* off, const void* t, int mag, void* out);
+
+/* ======================================================================= chi2 vs one observed curve */
+
+/* Offset-minimised chi2 of ncurves magnitude curves of T epochs (m, row-major, the
+ * given precision) against one observed curve obs_host / weights w_host (FP64, T):
+ * dm = sum w (o - m) / sum w (FP64), chi2 = sum w (o - m - dm)^2.  No reference
+ * counterpart (the reference has no offset solve).  chi2, dm: FP64 device arrays. */
+int mlc_chi2_offset(mlc_ctx* ctx, int precision, int ncurves, int T, const void* m,
+                    const double* obs_host, const double* w_host, double* chi2, double* dm);
+
+/* ======================================================================= pair stage (reference ratio form) */
+
+/* setup_integral_GPU (gpu_functions.cu:351-401): z = LCA[a*Nprof]/LCB[b*Nprof] for all
+ * Nloc^2 pairs; rank[a*Nloc+b] = position of that pair in the stable ascending order of
+ * z (d_sorted_ind); lower_host / nper_host per right edge (edges_host, ascending) from
+ * upper_bound, as Chi2SortBins::lower_ind / n_per_bin.  rank may be NULL (bins only). */
+int mlc_pair_setup(mlc_ctx* ctx, int Nloc, int Nprof, const double* LCA, const double* LCB, int Nbins,
+                   const double* edges_host, uint32_t* rank, uint32_t* lower_host, uint32_t* nper_host);
+
+/* calculate_chi2_GPU (gpu_functions.cu:428-456, kernel_chi2 :700-750):
+ * chi2 = sum_i ((d_i - mA_i/mB_i)/s_i)^2 with mA, mB interpolated on the profile axis
+ * (index -1 gives 1), FP64, written to chi2[rank[a*Nloc+b]] (or chi2[a*Nloc+b] when rank
+ * is NULL).  indA/indB/facA/facB/d/s are the Chi2Vars arrays (data_structs.hpp:4-18) on
+ * the host, Njp entries (no limit of 50). */
+int mlc_pair_chi2_ratio(mlc_ctx* ctx, int Njp, const int* indA_host, const int* indB_host,
+                        const double* facA_host, const double* facB_host, const double* d_host,
+                        const double* s_host, int Nloc, int Nprof, const double* LCA, const double* DLCA,
+                        const double* LCB, const double* DLCB, const uint32_t* rank, double* chi2);
+
+/* bin_chi2_GPU (gpu_functions.cu:483-503, kernel_bin_chi2 :772-795): per bin, mean of
+ * chi2 and of exp(-chi2/2) over chi2_sorted[lower .. lower+n); empty bins give 2000 and
+ * exp(-1000).  Results to the host arrays. */
+int mlc_bin_chi2(mlc_ctx* ctx, int Nbins, const uint32_t* lower_host, const uint32_t* nper_host,
+                 const double* chi2_sorted, double* binned_chi2_host, double* binned_exp_host);
+
+/* The three calls above fused without the Nloc^2 arrays: each pair's z bin is found
+ * from edges_host directly (bin i holds edge[i-1] < z <= edge[i], bin 0 everything
+ * <= edge[0], z above the last edge is dropped) and its chi2 and exp(-chi2/2) are summed
+ * per bin.  Same outputs as mlc_bin_chi2 plus the counts. */
+int mlc_pair_bin_fused(mlc_ctx* ctx, int Njp, const int* indA_host, const int* indB_host,
+                       const double* facA_host, const double* facB_host, const double* d_host,
+                       const double* s_host, int Nloc, int Nprof, const double* LCA, const double* DLCA,
+                       const double* LCB, const double* DLCB, int Nbins, const double* edges_host,
+                       double* binned_chi2_host, double* binned_exp_host, uint32_t* nper_host);
+
+/* ======================================================================= sort / histogram */
+
+/* Stable ascending sort of n FP64 keys (in place) carrying uint32 values (in place);
+ * hand-written LSD radix sort.  keys and vals are device arrays of n. */
+int mlc_sort_f64_u32(mlc_ctx* ctx, long n, double* keys, uint32_t* vals);
+
+/* Histogram of n FP64 values (device) into nbins equal bins on [lo, hi) of the value,
+ * or of log10(value) when logscale != 0; values outside are not counted.  counts_host
+ * receives nbins uint64 counts. */
+int mlc_histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, double hi, int logscale,
+                      uint64_t* counts_host);
+
+/* ======================================================================= host-side stages (C++, FP64) */
+
+/* setup_chi2_calculation (cpu_functions.cpp:80-144) with find_indices (:28-45), M = {MA, MB},
+ * V = {V0}: maps the Nd data times to profile-size indices and interpolation factors for
+ * images A and B, cuts at Njp (the first epoch outside the size range in both images) and
+ * returns the constant chi2 term of the dropped epochs.  Output arrays hold Nd entries;
+ * Njp_out receives their used length.  ref_compat = 1 keeps the reference's constant-term
+ * range i = Nd-Njp .. Nd-1; 0 sums the dropped epochs Njp .. Nd-1. */
+int mlc_setup_chi2(double MA, double MB, double V0, double Dfac, int Nd, const double* d_host,
+                   const double* t_host, const double* s_host, int Nprof, const double* x_host, int ref_compat,
+                   int* Njp_out, int* indA, int* indB, double* facA, double* facB, double* d_out, double* s_out,
+                   double* const_term);
+
+/* locations_on_grid / locations_random (locations.cpp:6-25); host arrays of Nside^2 / Nloc. */
+int mlc_locations_grid(int Nside, int Nmap, int Noff, int* x_host, int* y_host);
+int mlc_locations_random(int Nloc, int Nmap, int Noff, int seed, int* x_host, int* y_host);
+
+/* Right bin edges of Mpd(Nbins, min, max, "log"|linear) (mpd.cpp:4-21). */
+int mlc_bin_edges(int Nbins, double mn, double mx, int logscale, double* out_host);
+
+/* trapezium (integration.cpp:3-9): sum (f1 f2 [i-1] + f1 f2 [i]) (x[i] - x[i-1]) / 2.
+ * Returns the integral (not a status). */
+double mlc_trapezium(int N, const double* f1, const double* f2, const double* x);
+
+/* gerlumph map reader (magnification_map.cpp:7-40) from the directory dir (mapmeta.dat,
+ * map.bin).  meta6 (nullable) receives avgmu, avgN, width, k, g, s.  out_host NULL reads
+ * the size only; otherwise it receives the Nx*Nx FP64 magnifications. */
+int mlc_read_gerlumph(const char* dir, int* Nx, double* width, double* meta6, double* out_host, long cap);
+
+/* ======================================================================= synthetic maps */
+
+/* Inverse ray shooting (no reference counterpart; produces the gerlumph ray counts the
+ * reference reads, magnification_map.cpp:27-31): nrx x nry rays on the image-plane grid
+ * (x0 + i dx, y0 + j dx) are deflected by nl unit-mass point lenses (lenses_xy: device
+ * float pairs, Einstein-radius units), smooth convergence kappa_c and shear gamma, and
+ * counted into the N x N source-plane pixels of a square of side `width` centred on 0.
+ * counts: device int32 N*N (zeroed here).  ctx is an mlc_ctx*. */
+int mlc_rayshoot(void* ctx, const float* lenses_xy, int nl, double kappa_c, double gamma, double x0, double y0,
+                 double dx, long nrx, long nry, double width, int N, int* counts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MICROLC_GB300_H */

@@ -1,0 +1,91 @@
+"""ctypes binding of the C ABI declared in include/microlc_gb300.h.
+
+The library is built in-tree (microsn_gb300/libmicrolc_gb300.so); loading fails
+loudly when it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmicrolc_gb300.so")
+
+MLC_OK, MLC_ERR_ARG, MLC_ERR_OOM, MLC_ERR_CUDA, MLC_ERR_TIMEOUT, MLC_ERR_UNSUPPORTED, MLC_ERR_LIMIT = range(7)
+MLC_F64, MLC_F32 = 0, 1
+MLC_CONV_FUSED, MLC_CONV_PLAIN = 0, 1
+SHAPES = {"uniform": 0, "gaussian": 1, "gaussian_hole": 2, "thermal_hole": 3, "wavy": 4, "exponential": 5,
+          "limb_darkened": 6}
+
+
+class MlcProfile(C.Structure):
+    _fields_ = [("shape", C.c_int), ("ref_compat", C.c_int), ("rhalf", C.c_double), ("pix", C.c_double),
+                ("incl", C.c_double), ("orient", C.c_double), ("Rin", C.c_double), ("a", C.c_double),
+                ("u", C.c_double)]
+
+
+class MlcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"mlc error {code}: {msg}")
+        self.code = code
+
+
+vp = C.c_void_p
+i32, i64, f64 = C.c_int, C.c_int64, C.c_double
+P_i32 = C.POINTER(C.c_int)
+P_f64 = C.POINTER(C.c_double)
+P_u32 = C.POINTER(C.c_uint32)
+P_u64 = C.POINTER(C.c_uint64)
+
+# name -> (restype, argtypes); every entry returns int status unless noted
+SIGNATURES = {
+    "mlc_version": (i32, []),
+    "mlc_ctx_create": (i32, [i32, vp, C.POINTER(vp)]),
+    "mlc_ctx_destroy": (i32, [vp]),
+    "mlc_ctx_set_stream": (i32, [vp, vp]),
+    "mlc_ctx_synchronize": (i32, [vp]),
+    "mlc_ctx_last_error": (C.c_char_p, [vp]),
+    "mlc_ctx_workspace_bytes": (C.c_size_t, [vp]),
+    "mlc_profile_dims": (i32, [C.POINTER(MlcProfile), P_i32]),
+    "mlc_profile_raster": (i32, [C.POINTER(MlcProfile), vp, C.c_long, P_i32]),
+    "mlc_map_create": (i32, [vp, vp, i32, i32, i32, i32, i32, C.POINTER(vp)]),
+    "mlc_map_destroy": (i32, [vp]),
+    "mlc_map_data": (i32, [vp, C.POINTER(vp)]),
+    "mlc_map_prepare": (i32, [vp, vp]),
+    "mlc_convolve": (i32, [vp, vp, C.POINTER(MlcProfile), i32, vp]),
+    "mlc_expanding_source": (i32, [vp, vp, vp, i32, C.POINTER(MlcProfile), f64, i32, vp, vp, i32, vp, vp]),
+    "mlc_sample_nearest": (i32, [vp, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
+    "mlc_sample_tracks": (i32, [vp, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
+    "mlc_chi2_offset": (i32, [vp, i32, i32, i32, vp, vp, vp, vp, vp]),
+    "mlc_pair_setup": (i32, [vp, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
+    "mlc_pair_chi2_ratio": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]),
+    "mlc_bin_chi2": (i32, [vp, i32, vp, vp, vp, vp, vp]),
+    "mlc_pair_bin_fused": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, vp, vp, vp, vp, i32, vp, vp, vp,
+                                 vp]),
+    "mlc_sort_f64_u32": (i32, [vp, C.c_long, vp, vp]),
+    "mlc_histogram_f64": (i32, [vp, C.c_long, vp, i32, f64, f64, i32, vp]),
+    "mlc_setup_chi2": (i32, [f64, f64, f64, f64, i32, vp, vp, vp, i32, vp, i32, P_i32, vp, vp, vp, vp, vp, vp,
+                             P_f64]),
+    "mlc_locations_grid": (i32, [i32, i32, i32, vp, vp]),
+    "mlc_locations_random": (i32, [i32, i32, i32, i32, vp, vp]),
+    "mlc_bin_edges": (i32, [i32, f64, f64, i32, vp]),
+    "mlc_trapezium": (f64, [i32, vp, vp, vp]),
+    "mlc_read_gerlumph": (i32, [C.c_char_p, P_i32, P_f64, vp, vp, C.c_long]),
+    "mlc_rayshoot": (i32, [vp, vp, i32, f64, f64, f64, f64, f64, C.c_long, C.c_long, f64, i32, vp]),
+}
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run microsn_gb300.build.build() (no CPU fallback exists)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib

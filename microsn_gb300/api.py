@@ -1,0 +1,323 @@
+"""Python host mirror of the reference's hot-path interface, over the C ABI.
+
+Names follow the reference (simulating_lcurves/include/gpu_functions.hpp:11-18,
+cpu_functions.hpp:12-15): ``expanding_source``, ``setup_integral``, ``calculate_chi2``,
+``bin_chi2``, ``setup_chi2_calculation``, plus the new track / offset-chi2 stages.
+Device buffers are torch CUDA tensors (plumbing only); all compute runs in
+libmicrolc_gb300.so.  Errors raise :class:`MlcError` with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import MLC_CONV_FUSED, MLC_CONV_PLAIN, MLC_F32, MLC_F64, MlcError, MlcProfile, SHAPES
+
+_MODES = {"fused": MLC_CONV_FUSED, "plain": MLC_CONV_PLAIN}
+_PREC = {"f64": MLC_F64, "f32": MLC_F32, torch.float64: MLC_F64, torch.float32: MLC_F32}
+
+
+def _ptr(t) -> C.c_void_p:
+    if t is None:
+        return None
+    if isinstance(t, torch.Tensor):
+        return C.c_void_p(t.data_ptr())
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data_as(C.c_void_p)
+    raise TypeError(type(t))
+
+
+def _np(a, dtype):
+    return np.ascontiguousarray(np.asarray(a), dtype=dtype)
+
+
+class Context:
+    """A library context bound to one CUDA device and stream (torch's current stream by default)."""
+
+    def __init__(self, device: int = 0, stream: torch.cuda.Stream | None = None):
+        self.L = _lib.load()
+        self.device = device
+        s = stream if stream is not None else torch.cuda.current_stream(device)
+        self.stream = s
+        h = C.c_void_p()
+        st = self.L.mlc_ctx_create(device, C.c_void_p(s.cuda_stream), C.byref(h))
+        if st != 0:
+            raise MlcError(st, "mlc_ctx_create failed (is this an sm_103 GPU?)")
+        self.h = h
+
+    def check(self, st: int):
+        if st != 0:
+            raise MlcError(st, self.L.mlc_ctx_last_error(self.h).decode())
+
+    def set_stream(self, stream: torch.cuda.Stream):
+        self.stream = stream
+        self.check(self.L.mlc_ctx_set_stream(self.h, C.c_void_p(stream.cuda_stream)))
+
+    def synchronize(self):
+        self.check(self.L.mlc_ctx_synchronize(self.h))
+
+    def workspace_bytes(self) -> int:
+        return int(self.L.mlc_ctx_workspace_bytes(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mlc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def profile(shape: str, rhalf: float, pix: float, incl=0.0, orient=0.0, Rin=0.0, a=1.0, u=0.0,
+            ref_compat=True) -> MlcProfile:
+    return MlcProfile(SHAPES[shape], int(ref_compat), rhalf, pix, incl, orient, Rin, a, u)
+
+
+def profile_raster(p: MlcProfile) -> np.ndarray:
+    L = _lib.load()
+    n = C.c_int()
+    st = L.mlc_profile_dims(C.byref(p), C.byref(n))
+    if st:
+        raise MlcError(st, "invalid profile")
+    out = np.zeros(n.value * n.value)
+    st = L.mlc_profile_raster(C.byref(p), out.ctypes.data_as(C.c_void_p), out.size, C.byref(n))
+    if st:
+        raise MlcError(st, "profile raster failed")
+    return out.reshape(n.value, n.value)
+
+
+class Map:
+    """A magnification map resident on the device (MagnificationMap::data)."""
+
+    def __init__(self, ctx: Context, data, precision: str = "f64"):
+        self.ctx = ctx
+        if isinstance(data, torch.Tensor):
+            src = data.contiguous()
+            on_dev = int(src.is_cuda)
+            dt = MLC_F64 if src.dtype == torch.float64 else MLC_F32
+            ptr = C.c_void_p(src.data_ptr())
+            keep = src
+        else:
+            keep = np.ascontiguousarray(data)
+            if keep.dtype not in (np.float64, np.float32):
+                keep = keep.astype(np.float64)
+            on_dev = 0
+            dt = MLC_F64 if keep.dtype == np.float64 else MLC_F32
+            ptr = keep.ctypes.data_as(C.c_void_p)
+        self.Ny, self.Nx = keep.shape
+        self.prec = _PREC[precision]
+        h = C.c_void_p()
+        ctx.check(ctx.L.mlc_map_create(ctx.h, ptr, on_dev, dt, self.Nx, self.Ny, self.prec, C.byref(h)))
+        self.h = h
+        ctx.synchronize()
+
+    @property
+    def dtype(self):
+        return torch.float64 if self.prec == MLC_F64 else torch.float32
+
+    def data_ptr(self) -> int:
+        p = C.c_void_p()
+        self.ctx.check(self.ctx.L.mlc_map_data(self.h, C.byref(p)))
+        return p.value
+
+    def prepare(self):
+        self.ctx.check(self.ctx.L.mlc_map_prepare(self.ctx.h, self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.mlc_map_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def convolve(ctx: Context, m: Map, prof: MlcProfile, mode: str = "fused", out: torch.Tensor | None = None):
+    if out is None:
+        out = torch.empty((m.Ny, m.Nx), dtype=m.dtype, device=f"cuda:{ctx.device}")
+    ctx.check(ctx.L.mlc_convolve(ctx.h, m.h, C.byref(prof), _MODES[mode], _ptr(out)))
+    return out
+
+
+def expanding_source(ctx: Context, m: Map, sizes, base: MlcProfile, width: float, loc_x, loc_y,
+                     mode: str = "fused"):
+    """expanding_source (gpu_functions.cu:82): returns LC (Nloc x Nprof) and DLC
+    (Nloc x (Nprof-1)) as FP64 device tensors."""
+    dev = f"cuda:{ctx.device}"
+    sizes = _np(sizes, np.float64)
+    lx = torch.as_tensor(np.asarray(loc_x, np.int32), device=dev)
+    ly = torch.as_tensor(np.asarray(loc_y, np.int32), device=dev)
+    Nloc, Nprof = lx.numel(), sizes.size
+    LC = torch.empty((Nloc, Nprof), dtype=torch.float64, device=dev)
+    DLC = torch.empty((Nloc, max(Nprof - 1, 1)), dtype=torch.float64, device=dev)
+    ctx.check(ctx.L.mlc_expanding_source(ctx.h, m.h, _ptr(sizes), Nprof, C.byref(base), width, Nloc, _ptr(lx),
+                                         _ptr(ly), _MODES[mode], _ptr(LC), _ptr(DLC)))
+    return LC, DLC[:, : Nprof - 1]
+
+
+def sample_tracks(ctx: Context, maps, Nx: int, Ny: int, x0, y0, phi, v, off, t, mag: bool = True,
+                  out: torch.Tensor | None = None):
+    """Bilinear samples of the maps along straight tracks; returns (len(maps), E)."""
+    dt = x0.dtype
+    prec = _PREC[dt]
+    arr = (C.c_void_p * len(maps))(*[C.c_void_p(mm.data_ptr()) for mm in maps])
+    E = int(off[-1].item())
+    if out is None:
+        out = torch.empty((len(maps), E), dtype=dt, device=x0.device)
+    ctx.check(ctx.L.mlc_sample_tracks(ctx.h, arr, len(maps), Nx, Ny, prec, x0.numel(), _ptr(x0), _ptr(y0),
+                                      _ptr(phi), _ptr(v), _ptr(off), _ptr(t), int(mag), _ptr(out)))
+    return out
+
+
+def chi2_offset(ctx: Context, m: torch.Tensor, obs, w):
+    """Offset-minimised chi2 of each row of m against obs with weights w."""
+    n, T = m.shape
+    obs = _np(obs, np.float64)
+    w = _np(w, np.float64)
+    chi2 = torch.empty(n, dtype=torch.float64, device=m.device)
+    dm = torch.empty(n, dtype=torch.float64, device=m.device)
+    ctx.check(ctx.L.mlc_chi2_offset(ctx.h, _PREC[m.dtype], n, T, _ptr(m), _ptr(obs), _ptr(w), _ptr(chi2), _ptr(dm)))
+    return chi2, dm
+
+
+@dataclass
+class Chi2Vars:
+    """Chi2Vars (data_structs.hpp:4-18)."""
+    Njp: int
+    indA: np.ndarray
+    indB: np.ndarray
+    facA: np.ndarray
+    facB: np.ndarray
+    d: np.ndarray
+    s: np.ndarray
+    const_term: float
+
+
+def setup_chi2_calculation(M, V, Dfac, d, t, s, x, ref_compat=True) -> Chi2Vars:
+    L = _lib.load()
+    d = _np(d, np.float64); t = _np(t, np.float64); s = _np(s, np.float64); x = _np(x, np.float64)
+    Nd = d.size
+    indA = np.zeros(Nd, np.int32); indB = np.zeros(Nd, np.int32)
+    facA = np.zeros(Nd); facB = np.zeros(Nd); nd = np.zeros(Nd); ns = np.zeros(Nd)
+    Njp = C.c_int(); ct = C.c_double()
+    st = L.mlc_setup_chi2(M[0], M[1], V[0], Dfac, Nd, _ptr(d), _ptr(t), _ptr(s), x.size, _ptr(x), int(ref_compat),
+                          C.byref(Njp), _ptr(indA), _ptr(indB), _ptr(facA), _ptr(facB), _ptr(nd), _ptr(ns),
+                          C.byref(ct))
+    if st:
+        raise MlcError(st, "mlc_setup_chi2 failed")
+    n = Njp.value
+    return Chi2Vars(n, indA[:n].copy(), indB[:n].copy(), facA[:n].copy(), facB[:n].copy(), nd[:n].copy(),
+                    ns[:n].copy(), ct.value)
+
+
+def _vars_args(v: Chi2Vars):
+    arrs = [_np(v.indA, np.int32), _np(v.indB, np.int32), _np(v.facA, np.float64), _np(v.facB, np.float64),
+            _np(v.d, np.float64), _np(v.s, np.float64)]
+    return arrs, [_ptr(a) for a in arrs]
+
+
+def setup_integral(ctx: Context, LCA: torch.Tensor, LCB: torch.Tensor, edges, want_rank: bool = True):
+    """setup_integral_GPU: returns (rank as int32 device tensor holding uint32, lower, nper)."""
+    Nloc, Nprof = LCA.shape
+    edges = _np(edges, np.float64)
+    nb = edges.size
+    rank = torch.empty(Nloc * Nloc, dtype=torch.int32, device=LCA.device) if want_rank else None
+    lower = np.zeros(max(nb, 1), np.uint32); nper = np.zeros(max(nb, 1), np.uint32)
+    ctx.check(ctx.L.mlc_pair_setup(ctx.h, Nloc, Nprof, _ptr(LCA), _ptr(LCB), nb, _ptr(edges), _ptr(rank),
+                                   _ptr(lower), _ptr(nper)))
+    return rank, lower[:nb], nper[:nb]
+
+
+def calculate_chi2(ctx: Context, v: Chi2Vars, LCA, DLCA, LCB, DLCB, rank=None):
+    """calculate_chi2_GPU: FP64 chi2 of all Nloc^2 pairs, at rank order if rank is given."""
+    Nloc, Nprof = LCA.shape
+    keep, p = _vars_args(v)
+    out = torch.empty(Nloc * Nloc, dtype=torch.float64, device=LCA.device)
+    ctx.check(ctx.L.mlc_pair_chi2_ratio(ctx.h, v.Njp, *p, Nloc, Nprof, _ptr(LCA.contiguous()),
+                                        _ptr(DLCA.contiguous()), _ptr(LCB.contiguous()), _ptr(DLCB.contiguous()),
+                                        _ptr(rank), _ptr(out)))
+    return out
+
+
+def bin_chi2(ctx: Context, lower, nper, chi2_sorted: torch.Tensor):
+    """bin_chi2_GPU: (binned_chi2, binned_exp) host arrays."""
+    lower = _np(lower, np.uint32); nper = _np(nper, np.uint32)
+    nb = lower.size
+    bc = np.zeros(nb); be = np.zeros(nb)
+    ctx.check(ctx.L.mlc_bin_chi2(ctx.h, nb, _ptr(lower), _ptr(nper), _ptr(chi2_sorted), _ptr(bc), _ptr(be)))
+    return bc, be
+
+
+def pair_bin_fused(ctx: Context, v: Chi2Vars, LCA, DLCA, LCB, DLCB, edges):
+    Nloc, Nprof = LCA.shape
+    keep, p = _vars_args(v)
+    edges = _np(edges, np.float64)
+    nb = edges.size
+    bc = np.zeros(nb); be = np.zeros(nb); nper = np.zeros(nb, np.uint32)
+    ctx.check(ctx.L.mlc_pair_bin_fused(ctx.h, v.Njp, *p, Nloc, Nprof, _ptr(LCA.contiguous()),
+                                       _ptr(DLCA.contiguous()), _ptr(LCB.contiguous()), _ptr(DLCB.contiguous()), nb,
+                                       _ptr(edges), _ptr(bc), _ptr(be), _ptr(nper)))
+    return bc, be, nper
+
+
+def sort_f64_u32(ctx: Context, keys: torch.Tensor, vals: torch.Tensor):
+    """Stable in-place radix sort of FP64 keys with 32-bit values (int32 tensor)."""
+    ctx.check(ctx.L.mlc_sort_f64_u32(ctx.h, keys.numel(), _ptr(keys), _ptr(vals)))
+
+
+def histogram_f64(ctx: Context, v: torch.Tensor, nbins: int, lo: float, hi: float, log: bool = False):
+    out = np.zeros(nbins, np.uint64)
+    ctx.check(ctx.L.mlc_histogram_f64(ctx.h, v.numel(), _ptr(v), nbins, lo, hi, int(log), _ptr(out)))
+    return out
+
+
+def bin_edges(Nbins: int, mn: float, mx: float, log: bool = True) -> np.ndarray:
+    out = np.zeros(Nbins)
+    st = _lib.load().mlc_bin_edges(Nbins, mn, mx, int(log), _ptr(out))
+    if st:
+        raise MlcError(st, "bad bin spec")
+    return out
+
+
+def trapezium(f1, f2, x) -> float:
+    f1 = _np(f1, np.float64); f2 = _np(f2, np.float64); x = _np(x, np.float64)
+    return _lib.load().mlc_trapezium(x.size, _ptr(f1), _ptr(f2), _ptr(x))
+
+
+def locations_grid(Nside, Nmap, Noff):
+    x = np.zeros(Nside * Nside, np.int32); y = np.zeros(Nside * Nside, np.int32)
+    st = _lib.load().mlc_locations_grid(Nside, Nmap, Noff, _ptr(x), _ptr(y))
+    if st:
+        raise MlcError(st, "bad grid")
+    return x, y
+
+
+def locations_random(Nloc, Nmap, Noff, seed):
+    x = np.zeros(Nloc, np.int32); y = np.zeros(Nloc, np.int32)
+    st = _lib.load().mlc_locations_random(Nloc, Nmap, Noff, seed, _ptr(x), _ptr(y))
+    if st:
+        raise MlcError(st, "bad random locations")
+    return x, y
+
+
+def read_gerlumph(directory: str):
+    L = _lib.load()
+    n = C.c_int(); w = C.c_double(); meta = np.zeros(6)
+    st = L.mlc_read_gerlumph(directory.encode(), C.byref(n), C.byref(w), _ptr(meta), None, 0)
+    if st:
+        raise MlcError(st, f"cannot read {directory}")
+    out = np.zeros(n.value * n.value)
+    st = L.mlc_read_gerlumph(directory.encode(), C.byref(n), C.byref(w), _ptr(meta), _ptr(out), out.size)
+    if st:
+        raise MlcError(st, f"cannot read {directory}")
+    return out.reshape(n.value, n.value), w.value, meta

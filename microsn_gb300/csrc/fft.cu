@@ -1,0 +1,471 @@
+// 2-D real FFTs and FFT convolution of a magnification map with a source profile.
+//
+// Replaces the reference's cuFFT D2Z/Z2D plans and kernel_multiplyFFTs
+// (simulating_lcurves/src/gpu_functions.cu:150-200, 522-577) with hand-written passes:
+//
+//   forward(map):  R  rows, real FFT of length Nx (complex FFT of Nx/2 + split)
+//                  A  columns, sub-pass over row sets {n1*N2 + n2}: length-N1 DFT, twiddle
+//                  B  columns, sub-pass over row blocks {k1*N2 + n2}: length-N2 DFT
+//     The spectrum is left in "digit-transposed" row order (row k1*N2 + k2 holds
+//     frequency k1 + N1*k2); every consumer below works in that order, so no
+//     reordering pass is ever made.
+//
+//   fused convolution per profile (MLC_CONV_FUSED):
+//     P0  real FFT of the 2h non-zero rows of the wrapped profile only
+//     P1  per (k1, strip): the profile's column spectrum for all k2 built in shared
+//         memory (sub-pass A of the profile reduces to <= 2*ceil(h/N2) terms because
+//         only rows [0,h) and [Ny-h,Ny) are non-zero), multiplied by the map spectrum
+//         and by 1/(Nx Ny), then the inverse length-N2 sub-pass and its twiddle
+//     P2  inverse sub-pass over row sets (length N1)
+//     P3  inverse real FFT of each row (c2r)
+//   plain convolution (MLC_CONV_PLAIN): full-size wrapped kernel, full forward,
+//     pointwise multiply, full inverse -- one launch per stage, like the reference.
+#include <cmath>
+#include <mutex>
+#include <unordered_map>
+
+#include "mlc_internal.h"
+
+namespace mlc {
+
+RadixList factor_radices(int L) {
+  RadixList rl{};
+  rl.n = 0;
+  if (L < 1) {
+    rl.n = -1;
+    return rl;
+  }
+  int n = L;
+  while (n % 5 == 0) { rl.r[rl.n++] = 5; n /= 5; }
+  while (n % 3 == 0) { rl.r[rl.n++] = 3; n /= 3; }
+  int e2 = 0;
+  while (n % 2 == 0) { e2++; n /= 2; }
+  if (n != 1) {
+    rl.n = -1;
+    return rl;
+  }
+  int n8 = e2 / 3, rem = e2 % 3;
+  if (rem == 1 && n8 > 0) {  // 8*2 -> 4*4
+    n8--;
+    rl.r[rl.n++] = 4;
+    rl.r[rl.n++] = 4;
+  } else if (rem == 1) {
+    rl.r[rl.n++] = 2;
+  } else if (rem == 2) {
+    rl.r[rl.n++] = 4;
+  }
+  for (int i = 0; i < n8; i++) rl.r[rl.n++] = 8;
+  return rl;
+}
+
+void set_max_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::unordered_map<const void*, size_t> done;
+  std::lock_guard<std::mutex> g(mu);
+  auto it = done.find(func);
+  if (it != done.end() && it->second >= bytes) return;
+  MLC_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  done[func] = bytes;
+}
+
+FftPlan2D::~FftPlan2D() {
+  if (twx) cudaFree(twx);
+  if (twy) cudaFree(twy);
+}
+
+// exp(-2 pi i m / N), m in [0, N), evaluated in long double with the angle reduced to
+// the first octant so that each entry is correctly rounded to FP64 in practice.
+static void twiddle_table(int N, std::vector<double>& re, std::vector<double>& im) {
+  re.resize(N);
+  im.resize(N);
+  const long double TWO_PI = 6.283185307179586476925286766559005768L;
+  for (int m = 0; m < N; m++) {
+    // reduce m/N to [0, 1/8] using the symmetries of cos/sin
+    long q8 = (long)m * 8;  // octant index via integer arithmetic
+    int oct = (int)(q8 / N);
+    long double frac;  // angle fraction of a full turn within the octant frame
+    long double c, s;
+    // angle a = 2 pi m / N; write m/N = oct/8 + r with r in [0, 1/8)
+    long double r = ((long double)m - (long double)oct * N / 8.0L) / N;
+    (void)frac;
+    long double a = TWO_PI * r;
+    long double ca = cosl(a), sa = sinl(a);
+    const long double h = 0.70710678118654752440084436210484903928L;
+    // rotate by oct * 45 degrees
+    switch (oct & 7) {
+      case 0: c = ca; s = sa; break;
+      case 1: c = h * (ca - sa); s = h * (ca + sa); break;
+      case 2: c = -sa; s = ca; break;
+      case 3: c = -h * (ca + sa); s = h * (ca - sa); break;
+      case 4: c = -ca; s = -sa; break;
+      case 5: c = -h * (ca - sa); s = -h * (ca + sa); break;
+      case 6: c = sa; s = -ca; break;
+      default: c = h * (ca + sa); s = -h * (ca - sa); break;
+    }
+    // exact values where they are known
+    if ((long)m * 4 % N == 0) {
+      long k = (long)m * 4 / N;
+      c = (k == 0) ? 1 : (k == 2) ? -1 : 0;
+      s = (k == 1) ? 1 : (k == 3) ? -1 : 0;
+    }
+    re[m] = (double)c;
+    im[m] = -(double)s;  // forward sign
+  }
+}
+
+template <typename T>
+static void* upload_twiddles(int N) {
+  std::vector<double> re, im;
+  twiddle_table(N, re, im);
+  std::vector<C2<T>> h(N);
+  for (int m = 0; m < N; m++) h[m] = C2<T>{(T)re[m], (T)im[m]};
+  void* d = nullptr;
+  MLC_CUDA(cudaMalloc(&d, sizeof(C2<T>) * N));
+  MLC_CUDA(cudaMemcpy(d, h.data(), sizeof(C2<T>) * N, cudaMemcpyHostToDevice));
+  return d;
+}
+
+static void split_columns(int Ny, int& N1, int& N2) {
+  int best = 1;
+  for (int d = 1; (long)d * d <= Ny; d++)
+    if (Ny % d == 0) best = d;
+  N1 = best;
+  N2 = Ny / best;
+}
+
+FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
+  auto key = std::make_tuple(Nx, Ny, prec);
+  auto it = ctx->plans.find(key);
+  if (it != ctx->plans.end()) return it->second.get();
+  MLC_REQUIRE(Nx >= 4 && Ny >= 2 && Nx % 2 == 0, MLC_ERR_ARG, "map sides must be even, Nx >= 4");
+  std::unique_ptr<FftPlan2D> p(new FftPlan2D());
+  p->Nx = Nx;
+  p->Ny = Ny;
+  p->prec = prec;
+  p->M = Nx / 2;
+  p->Wc = Nx / 2 + 1;
+  p->Wp = (int)round_up(p->Wc, 16);
+  p->elem = prec == MLC_F64 ? sizeof(C2<double>) : sizeof(C2<float>);
+  p->CW = prec == MLC_F64 ? 8 : 16;
+  split_columns(Ny, p->N1, p->N2);
+  p->rlM = factor_radices(p->M);
+  p->rlN1 = factor_radices(p->N1);
+  p->rlN2 = factor_radices(p->N2);
+  MLC_REQUIRE(p->rlM.n >= 0 && p->rlN1.n >= 0 && p->rlN2.n >= 0, MLC_ERR_ARG,
+              "map sides must factor into 2, 3 and 5");
+  size_t row_smem = 2 * (size_t)(p->M + 1) * p->elem;
+  MLC_REQUIRE(row_smem <= 220 * 1024, MLC_ERR_LIMIT,
+              "map row too long for one shared-memory row transform (Nx <= 13000 FP64, 26000 FP32)");
+  MLC_REQUIRE(2 * (size_t)p->N2 * p->CW * p->elem <= 200 * 1024, MLC_ERR_LIMIT, "column length too large");
+  if (prec == MLC_F64) {
+    p->twx = upload_twiddles<double>(Nx);
+    p->twy = upload_twiddles<double>(Ny);
+  } else {
+    p->twx = upload_twiddles<float>(Nx);
+    p->twy = upload_twiddles<float>(Ny);
+  }
+  FftPlan2D* raw = p.get();
+  ctx->plans[key] = std::move(p);
+  return raw;
+}
+
+// ---------------------------------------------------------------- row loaders
+
+template <typename T, typename Tin>
+struct RealRows {
+  const Tin* p;
+  long ld;
+  __device__ __forceinline__ C2<T> pair(int row, int n) const {
+    const Tin* r = p + (long)row * ld + 2 * n;
+    return C2<T>{(T)r[0], (T)r[1]};
+  }
+};
+
+// Row j of the compacted wrapped profile: j < h is kernel row j (profile row h + j);
+// j >= h is kernel row Ny - 2h + j (profile row j - h).  Columns follow
+// Kernel::setKernel (magnification_map.cpp:186-193).
+template <typename T>
+struct ProfileRows {
+  const double* prof;
+  int N, h, Nx;
+  __device__ __forceinline__ T at(int pr, int m) const {
+    if (m < h) return (T)prof[(long)pr * N + h + m];
+    if (m >= Nx - h) return (T)prof[(long)pr * N + m - (Nx - h)];
+    return (T)0;
+  }
+  __device__ __forceinline__ C2<T> pair(int j, int n) const {
+    int pr = (j < h) ? h + j : j - h;
+    return C2<T>{at(pr, 2 * n), at(pr, 2 * n + 1)};
+  }
+};
+
+// ---------------------------------------------------------------- row kernels
+
+// Real FFT of one row per CTA; writes Nx/2+1 complex values and zero padding up to Wp.
+template <typename T, typename Loader>
+__global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__ out, long pitch, int M,
+                                                  RadixList rl, const C2<T>* __restrict__ twx) {
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
+  C2<T>* b = a + (M + 1);
+  const int row = blockIdx.x;
+  for (int n = threadIdx.x; n < M; n += blockDim.x) a[n] = ld.pair(row, n);
+  __syncthreads();
+  C2<T>* Z = fft_smem<T, false, 1>(a, b, M, rl, twx, 2);
+  C2<T>* o = out + (long)row * pitch;
+  for (int k = threadIdx.x; k <= M; k += blockDim.x) {
+    C2<T> zk = Z[k == M ? 0 : k];
+    C2<T> zc = cconj(Z[k == 0 ? 0 : M - k]);
+    C2<T> s = cadd(zk, zc);
+    C2<T> wd = cmul(ldc(twx + k), csub(zk, zc));  // W_Nx^k (Z - conj Z')
+    o[k] = C2<T>{(T)0.5 * (s.x + wd.y), (T)0.5 * (s.y - wd.x)};
+  }
+  for (int k = M + 1 + threadIdx.x; k < pitch; k += blockDim.x) o[k] = C2<T>{(T)0, (T)0};
+}
+
+// Inverse real FFT (unnormalised, like cuFFT Z2D) of one spectrum row per CTA.
+template <typename T>
+__global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, long pitch, T* __restrict__ out,
+                                                  long ldo, int M, RadixList rl, const C2<T>* __restrict__ twx) {
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
+  C2<T>* b = a + (M + 1);
+  const int row = blockIdx.x;
+  const C2<T>* src = in + (long)row * pitch;
+  for (int k = threadIdx.x; k <= M; k += blockDim.x) a[k] = src[k];
+  __syncthreads();
+  for (int k = threadIdx.x; k < M; k += blockDim.x) {
+    C2<T> xk = a[k];
+    C2<T> xm = cconj(a[M - k]);
+    C2<T> e = cadd(xk, xm);
+    C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
+    b[k] = C2<T>{e.x - o.y, e.y + o.x};
+  }
+  __syncthreads();
+  C2<T>* z = fft_smem<T, true, 1>(b, a, M, rl, twx, 2);
+  C2<T>* dst = reinterpret_cast<C2<T>*>(out + (long)row * ldo);
+  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = z[n];
+}
+
+// ---------------------------------------------------------------- column kernels
+
+// In-place sub-pass over the row set {set*set_mul + j*j_mul : j < L} of one strip of CW
+// columns.  post_tw multiplies output j by W_Ny^(+/- set*j).
+template <typename T, int CW, bool INV>
+__global__ void __launch_bounds__(256) k_colpass(C2<T>* __restrict__ buf, long pitch, int L, long set_mul,
+                                                 long j_mul, RadixList rl, const C2<T>* __restrict__ twy,
+                                                 int tw_stride, int post_tw) {
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
+  C2<T>* b = a + L * CW;
+  const int set = blockIdx.y;
+  const long col0 = (long)blockIdx.x * CW;
+  const long base = (long)set * set_mul;
+  for (int idx = threadIdx.x; idx < L * CW; idx += blockDim.x) {
+    int j = idx / CW, c = idx % CW;
+    a[idx] = buf[(base + j * j_mul) * pitch + col0 + c];
+  }
+  __syncthreads();
+  C2<T>* r = fft_smem<T, INV, CW>(a, b, L, rl, twy, tw_stride);
+  for (int idx = threadIdx.x; idx < L * CW; idx += blockDim.x) {
+    int j = idx / CW, c = idx % CW;
+    C2<T> v = r[idx];
+    if (post_tw) {
+      C2<T> w = ldc(twy + (long)set * j);  // set*j < Ny for both sub-pass kinds
+      v = INV ? cmulc(v, w) : cmul(v, w);
+    }
+    buf[(base + j * j_mul) * pitch + col0 + c] = v;
+  }
+}
+
+// P1 of the fused convolution, one CTA per (strip, k1).
+template <typename T, int CW>
+__global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
+                                                    long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
+                                                    int N1, int N2, RadixList rl2,
+                                                    const C2<T>* __restrict__ twy, T scale) {
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
+  C2<T>* b = a + N2 * CW;
+  const int k1 = blockIdx.y;
+  const long col0 = (long)blockIdx.x * CW;
+  // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 k1)
+  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
+    const int n2 = idx / CW, c = idx % CW;
+    C2<T> acc{(T)0, (T)0};
+    for (int n1 = 0; (long)n1 * N2 + n2 < h; n1++) {
+      const long j = (long)n1 * N2 + n2;
+      C2<T> kv = Kx[j * pitch + col0 + c];
+      C2<T> w = ldc(twy + (long)((n1 * (long)k1) % N1) * N2);
+      acc = cadd(acc, cmul(kv, w));
+    }
+    const long lo = (long)Ny - h;  // first non-zero high row
+    int n1s = (int)((lo - n2 + N2 - 1) / N2);
+    if (n1s < 0) n1s = 0;
+    for (int n1 = n1s; n1 < N1; n1++) {
+      const long n = (long)n1 * N2 + n2;
+      const long j = n - (Ny - 2L * h);
+      C2<T> kv = Kx[j * pitch + col0 + c];
+      C2<T> w = ldc(twy + (long)((n1 * (long)k1) % N1) * N2);
+      acc = cadd(acc, cmul(kv, w));
+    }
+    a[idx] = cmul(acc, ldc(twy + (long)n2 * k1));
+  }
+  __syncthreads();
+  C2<T>* K = fft_smem<T, false, CW>(a, b, N2, rl2, twy, N1);
+  C2<T>* other = (K == a) ? b : a;
+  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
+    const int k2 = idx / CW, c = idx % CW;
+    C2<T> f = Fmap[((long)k1 * N2 + k2) * pitch + col0 + c];
+    K[idx] = cscale(cmul(f, K[idx]), scale);
+  }
+  __syncthreads();
+  C2<T>* U = fft_smem<T, true, CW>(K, other, N2, rl2, twy, N1);
+  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
+    const int n2 = idx / CW, c = idx % CW;
+    C2<T> v = cmulc(U[idx], ldc(twy + (long)n2 * k1));
+    out[((long)k1 * N2 + n2) * pitch + col0 + c] = v;
+  }
+}
+
+// ---------------------------------------------------------------- plain-path helpers
+
+template <typename T>
+__global__ void k_wrap_full(const double* __restrict__ prof, int N, int Nx, int Ny, T* __restrict__ out) {
+  const int h = N / 2;
+  const long total = (long)Nx * Ny;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / Nx), x = (int)(i % Nx);
+    int pr = -1, pc = -1;
+    if (y < h) pr = h + y;
+    else if (y >= Ny - h) pr = y - (Ny - h);
+    if (x < h) pc = h + x;
+    else if (x >= Nx - h) pc = x - (Nx - h);
+    out[i] = (pr >= 0 && pc >= 0) ? (T)prof[(long)pr * N + pc] : (T)0;
+  }
+}
+
+// kernel_multiplyFFTs (gpu_functions.cu:571-577): Fk = Fmap * Fk / norm, in place.
+template <typename T>
+__global__ void k_multiply(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ Fk, long n, T scale) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    C2<T> m = cmul(Fmap[i], Fk[i]);
+    Fk[i] = C2<T>{m.x * scale, m.y * scale};
+  }
+}
+
+// ---------------------------------------------------------------- host orchestration
+
+template <typename T, typename Loader>
+static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, int nrows, void* out) {
+  if (nrows <= 0) return;
+  size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
+  auto kern = k_rows_r2c<T, Loader>;
+  set_max_smem((const void*)kern, smem);
+  kern<<<nrows, 512, smem, ctx->stream>>>(ld, (C2<T>*)out, p.Wp, p.M, p.rlM, (const C2<T>*)p.twx);
+  MLC_CHECK_LAUNCH();
+}
+
+template <typename T>
+static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, void* out) {
+  size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
+  auto kern = k_rows_c2r<T>;
+  set_max_smem((const void*)kern, smem);
+  kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (T*)out, p.Nx, p.M, p.rlM,
+                                         (const C2<T>*)p.twx);
+  MLC_CHECK_LAUNCH();
+}
+
+// kind 'A': row sets {n2 + N2*j}, length N1; kind 'B': row blocks {k1*N2 + j}, length N2.
+template <typename T, bool INV>
+static void launch_colpass(mlc_ctx* ctx, const FftPlan2D& p, void* buf, char kind, int post_tw) {
+  constexpr int CW = sizeof(T) == 8 ? 8 : 16;
+  const int nstrips = ceil_div(p.Wc, CW);
+  int L, nsets, tw_stride;
+  long set_mul, j_mul;
+  RadixList rl;
+  if (kind == 'A') {
+    L = p.N1; nsets = p.N2; set_mul = 1; j_mul = p.N2; tw_stride = p.N2; rl = p.rlN1;
+  } else {
+    L = p.N2; nsets = p.N1; set_mul = p.N2; j_mul = 1; tw_stride = p.N1; rl = p.rlN2;
+  }
+  if (L == 1 && !post_tw) return;
+  size_t smem = 2 * (size_t)L * CW * sizeof(C2<T>);
+  auto kern = k_colpass<T, CW, INV>;
+  set_max_smem((const void*)kern, smem);
+  dim3 grid(nstrips, nsets);
+  kern<<<grid, 256, smem, ctx->stream>>>((C2<T>*)buf, p.Wp, L, set_mul, j_mul, rl, (const C2<T>*)p.twy,
+                                         tw_stride, post_tw);
+  MLC_CHECK_LAUNCH();
+}
+
+template <typename T>
+static void forward_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec) {
+  if (in_dtype == MLC_F64)
+    launch_rows_r2c<T>(ctx, p, RealRows<T, double>{(const double*)in, p.Nx}, p.Ny, spec);
+  else
+    launch_rows_r2c<T>(ctx, p, RealRows<T, float>{(const float*)in, p.Nx}, p.Ny, spec);
+  launch_colpass<T, false>(ctx, p, spec, 'A', 1);
+  launch_colpass<T, false>(ctx, p, spec, 'B', 0);
+}
+
+void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec) {
+  if (p.prec == MLC_F64) forward_impl<double>(ctx, p, in, in_dtype, spec);
+  else forward_impl<float>(ctx, p, in, in_dtype, spec);
+}
+
+template <typename T>
+static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
+                            void* out) {
+  constexpr int CW = sizeof(T) == 8 ? 8 : 16;
+  const int h = pN / 2;
+  MLC_REQUIRE(pN % 2 == 0 && 2 * h <= p.Ny && 2 * h <= p.Nx, MLC_ERR_LIMIT,
+              "profile raster larger than the map");
+  void* kx = ws_get(ctx, WS_KX, (size_t)(2 * h > 0 ? 2 * h : 1) * p.Wp * sizeof(C2<T>));
+  void* tmp = ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
+  launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
+  const int nstrips = ceil_div(p.Wc, CW);
+  size_t smem = 2 * (size_t)p.N2 * CW * sizeof(C2<T>);
+  auto kern = k_conv_fused<T, CW>;
+  set_max_smem((const void*)kern, smem);
+  dim3 grid(nstrips, p.N1);
+  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
+  kern<<<grid, 256, smem, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp, (const C2<T>*)kx, h, p.Ny,
+                                         p.N1, p.N2, p.rlN2, (const C2<T>*)p.twy, scale);
+  MLC_CHECK_LAUNCH();
+  launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
+  launch_rows_c2r<T>(ctx, p, tmp, out);
+}
+
+template <typename T>
+static void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
+                            void* out) {
+  MLC_REQUIRE(pN % 2 == 0 && pN <= p.Ny && pN <= p.Nx, MLC_ERR_LIMIT, "profile raster larger than the map");
+  void* kreal = ws_get(ctx, WS_KREAL, (size_t)p.Nx * p.Ny * sizeof(T));
+  void* kspec = ws_get(ctx, WS_KSPEC, p.spec_bytes());
+  const long total = (long)p.Nx * p.Ny;
+  int grid = (int)std::min<long>((total + 255) / 256, (long)ctx->sm_count * 16);
+  k_wrap_full<T><<<grid, 256, 0, ctx->stream>>>(prof, pN, p.Nx, p.Ny, (T*)kreal);
+  MLC_CHECK_LAUNCH();
+  forward_impl<T>(ctx, p, kreal, sizeof(T) == 8 ? MLC_F64 : MLC_F32, kspec);
+  const long n = (long)p.Ny * p.Wp;
+  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
+  grid = (int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 16);
+  k_multiply<T><<<grid, 256, 0, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)kspec, n, scale);
+  MLC_CHECK_LAUNCH();
+  launch_colpass<T, true>(ctx, p, kspec, 'B', 1);
+  launch_colpass<T, true>(ctx, p, kspec, 'A', 0);
+  launch_rows_c2r<T>(ctx, p, kspec, out);
+}
+
+void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
+  if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, out);
+  else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, out);
+}
+
+void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
+  if (p.prec == MLC_F64) conv_plain_impl<double>(ctx, p, Fmap, prof, pN, out);
+  else conv_plain_impl<float>(ctx, p, Fmap, prof, pN, out);
+}
+
+}  // namespace mlc

@@ -1,0 +1,160 @@
+// Hand-written mixed-radix Stockham FFT for sm_103a: in-shared-memory batched
+// transforms (radix 2, 3, 4, 5, 8) used by the row passes (one image row per CTA) and
+// the column passes (a 128-byte strip of columns per CTA, four-step split N = N1*N2).
+#pragma once
+
+#include "mlc_common.cuh"
+
+namespace mlc {
+
+struct RadixList {
+  int n;
+  int r[24];
+};
+
+// Radix list for length L (2^a 3^b 5^c), or n = -1 when L has another factor.
+RadixList factor_radices(int L);
+
+// ---------------------------------------------------------------- small DFTs
+
+template <typename T, int R, bool INV>
+struct Dft;
+
+template <typename T, bool INV>
+struct Dft<T, 2, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    C2<T> a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <typename T, bool INV>
+struct Dft<T, 3, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    const T h = (T)0.86602540378443864676372317075294;  // sin(2 pi / 3)
+    C2<T> s = cadd(v[1], v[2]);
+    C2<T> d = csub(v[1], v[2]);
+    C2<T> m = C2<T>{v[0].x - (T)0.5 * s.x, v[0].y - (T)0.5 * s.y};
+    C2<T> id = mul_mi<T, INV>(d);  // -i d (forward) / +i d (inverse)
+    v[0] = cadd(v[0], s);
+    v[1] = C2<T>{m.x + h * id.x, m.y + h * id.y};
+    v[2] = C2<T>{m.x - h * id.x, m.y - h * id.y};
+  }
+};
+
+template <typename T, bool INV>
+struct Dft<T, 4, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    C2<T> a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+    C2<T> a2 = cadd(v[1], v[3]), a3 = mul_mi<T, INV>(csub(v[1], v[3]));
+    v[0] = cadd(a0, a2);
+    v[2] = csub(a0, a2);
+    v[1] = cadd(a1, a3);
+    v[3] = csub(a1, a3);
+  }
+};
+
+template <typename T, bool INV>
+struct Dft<T, 5, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    const T c1 = (T)0.30901699437494742410229341718282;   // cos(2 pi/5)
+    const T c2 = (T)-0.80901699437494742410229341718282;  // cos(4 pi/5)
+    const T s1 = (T)0.95105651629515357211643933337938;   // sin(2 pi/5)
+    const T s2 = (T)0.58778525229247312916870595463907;   // sin(4 pi/5)
+    C2<T> x0 = v[0];
+    C2<T> sa = cadd(v[1], v[4]), da = csub(v[1], v[4]);
+    C2<T> sb = cadd(v[2], v[3]), db = csub(v[2], v[3]);
+    C2<T> p1 = C2<T>{x0.x + c1 * sa.x + c2 * sb.x, x0.y + c1 * sa.y + c2 * sb.y};
+    C2<T> p2 = C2<T>{x0.x + c2 * sa.x + c1 * sb.x, x0.y + c2 * sa.y + c1 * sb.y};
+    C2<T> q1 = C2<T>{s1 * da.x + s2 * db.x, s1 * da.y + s2 * db.y};
+    C2<T> q2 = C2<T>{s2 * da.x - s1 * db.x, s2 * da.y - s1 * db.y};
+    C2<T> iq1 = mul_mi<T, INV>(q1), iq2 = mul_mi<T, INV>(q2);
+    v[0] = cadd(x0, cadd(sa, sb));
+    v[1] = cadd(p1, iq1);
+    v[4] = csub(p1, iq1);
+    v[2] = cadd(p2, iq2);
+    v[3] = csub(p2, iq2);
+  }
+};
+
+template <typename T, bool INV>
+struct Dft<T, 8, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    const T r = (T)0.70710678118654752440084436210485;
+    C2<T> e[4] = {v[0], v[2], v[4], v[6]};
+    C2<T> o[4] = {v[1], v[3], v[5], v[7]};
+    Dft<T, 4, INV>::run(e);
+    Dft<T, 4, INV>::run(o);
+    // o[q] *= W8^q ; forward W8 = (1 - i)/sqrt2, inverse (1 + i)/sqrt2
+    C2<T> o1 = INV ? C2<T>{r * (o[1].x - o[1].y), r * (o[1].x + o[1].y)}
+                   : C2<T>{r * (o[1].x + o[1].y), r * (o[1].y - o[1].x)};
+    C2<T> o2 = mul_mi<T, INV>(o[2]);
+    C2<T> o3 = INV ? C2<T>{-r * (o[3].x + o[3].y), r * (o[3].x - o[3].y)}
+                   : C2<T>{r * (o[3].y - o[3].x), -r * (o[3].x + o[3].y)};
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);
+    v[5] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);
+    v[6] = csub(e[2], o2);
+    v[3] = cadd(e[3], o3);
+    v[7] = csub(e[3], o3);
+  }
+};
+
+// ---------------------------------------------------------------- Stockham stage
+// src/dst are [L][CW] complex arrays in shared memory; tw is the length-(L*tw_stride)
+// table exp(-2 pi i m / (L*tw_stride)) in global memory.
+template <typename T, int R, bool INV, int CW>
+__device__ __forceinline__ void stockham_stage(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int L,
+                                               int Ns, const C2<T>* __restrict__ tw, int tw_stride) {
+  const int Lr = L / R;
+  const int nb = Lr * CW;
+  const int twstep = (L / (Ns * R)) * tw_stride;
+  for (int bt = threadIdx.x; bt < nb; bt += blockDim.x) {
+    const int c = bt % CW;
+    const int j = bt / CW;
+    const int k = j % Ns;
+    C2<T> v[R];
+#pragma unroll
+    for (int i = 0; i < R; i++) v[i] = src[(j + i * Lr) * CW + c];
+    if (Ns > 1) {
+#pragma unroll
+      for (int i = 1; i < R; i++) {
+        C2<T> w = ldc(tw + (long)i * k * twstep);
+        v[i] = INV ? cmulc(v[i], w) : cmul(v[i], w);
+      }
+    }
+    Dft<T, R, INV>::run(v);
+    const int d = (j - k) * R + k;
+#pragma unroll
+    for (int i = 0; i < R; i++) dst[(d + i * Ns) * CW + c] = v[i];
+  }
+}
+
+// Batched length-L transform of the CW columns held in a ([L][CW]); b is scratch of the
+// same size.  Returns the buffer that holds the natural-order result.  Ends synchronised.
+template <typename T, bool INV, int CW>
+__device__ C2<T>* fft_smem(C2<T>* a, C2<T>* b, int L, const RadixList& rl, const C2<T>* __restrict__ tw,
+                           int tw_stride) {
+  int Ns = 1;
+  for (int p = 0; p < rl.n; ++p) {
+    const int r = rl.r[p];
+    switch (r) {
+      case 2: stockham_stage<T, 2, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
+      case 3: stockham_stage<T, 3, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
+      case 4: stockham_stage<T, 4, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
+      case 5: stockham_stage<T, 5, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
+      default: stockham_stage<T, 8, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
+    }
+    __syncthreads();
+    C2<T>* t = a;
+    a = b;
+    b = t;
+    Ns *= r;
+  }
+  return a;
+}
+
+}  // namespace mlc

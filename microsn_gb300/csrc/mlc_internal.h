@@ -1,0 +1,105 @@
+// Internal host-side state of the library: context, workspace pool, maps, FFT plans.
+#pragma once
+
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "fft.cuh"
+#include "mlc_common.cuh"
+
+namespace mlc {
+
+// Plan for 2-D real transforms of an Ny x Nx image: rows are real FFTs of length Nx
+// (a complex FFT of length M = Nx/2 plus the split post-process); columns are complex
+// FFTs of length Ny = N1 * N2 done as two in-place sub-passes over row sets.
+struct FftPlan2D {
+  int Nx = 0, Ny = 0, prec = 0;
+  int M = 0;   // Nx / 2
+  int Wc = 0;  // Nx / 2 + 1 spectrum columns
+  int Wp = 0;  // spectrum pitch (complex elements), multiple of 16
+  int N1 = 1, N2 = 1;
+  int CW = 16;  // columns per strip: 128 bytes of complex data
+  RadixList rlM{}, rlN1{}, rlN2{};
+  void* twx = nullptr;  // Nx-entry table exp(-2 pi i m / Nx)
+  void* twy = nullptr;  // Ny-entry table exp(-2 pi i m / Ny)
+  size_t elem = 0;      // sizeof(C2<T>)
+  size_t spec_bytes() const { return (size_t)Ny * Wp * elem; }
+  ~FftPlan2D();
+};
+
+enum WsSlot {
+  WS_SPEC_TMP = 0,
+  WS_KX,
+  WS_PROFILE,
+  WS_KREAL,
+  WS_KSPEC,
+  WS_CONV_OUT,
+  WS_SORT_KEYS,
+  WS_SORT_VALS,
+  WS_SORT_HIST,
+  WS_PAIR_ACC,
+  WS_SMALL,
+  WS_LOC,
+  WS_NSLOTS
+};
+
+}  // namespace mlc
+
+struct mlc_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  std::string err;
+  void* ws_ptr[mlc::WS_NSLOTS] = {};
+  size_t ws_size[mlc::WS_NSLOTS] = {};
+  std::map<std::tuple<int, int, int>, std::unique_ptr<mlc::FftPlan2D>> plans;
+};
+
+struct mlc_map {
+  mlc_ctx* ctx = nullptr;
+  int Nx = 0, Ny = 0, prec = 0;
+  void* data = nullptr;  // Ny x Nx real
+  void* spec = nullptr;  // forward spectrum, digit-transposed row order
+  bool spec_valid = false;
+};
+
+namespace mlc {
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) MLC_CUDA(cudaSetDevice(dev));
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+void* ws_get(mlc_ctx* ctx, int slot, size_t bytes);
+
+// Raise a kernel's dynamic shared-memory limit once.
+void set_max_smem(const void* func, size_t bytes);
+
+// FFT and convolution (fft.cu)
+FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec);
+void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec);
+void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof_dev, int pN,
+                void* out_real);
+void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof_dev, int pN,
+                void* out_real);
+
+// Host profile rasters (profile.cpp)
+int profile_dims(const mlc_profile& p);
+int profile_raster(const mlc_profile& p, double* out, long cap);
+
+// Sampling (sample.cu)
+void sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int Nprof, int Nloc, const int* lx,
+                    const int* ly, double* LC, double* DLC);
+
+}  // namespace mlc

@@ -1,0 +1,189 @@
+// Light-curve sampling: nearest-pixel reads at fixed locations (the reference's
+// kernel_sample) and bilinear sampling along straight source tracks with the
+// magnitude conversion fused in; plus the offset-minimised chi2 against one observed
+// curve.
+#include <cmath>
+
+#include "mlc_internal.h"
+
+namespace mlc {
+
+// kernel_sample (simulating_lcurves/src/gpu_functions.cu:604-620).
+__global__ void k_sample_nearest(const double* __restrict__ map, int Nx, int Ny, int k, int Nprof, int Nloc,
+                                 const int* __restrict__ lx, const int* __restrict__ ly, double* __restrict__ LC,
+                                 double* __restrict__ DLC) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= Nloc) return;
+  const int x = lx[id], y = ly[id];
+  const double v = (x >= 0 && x < Nx && y >= 0 && y < Ny) ? map[(long)y * Nx + x] : __longlong_as_double(0x7ff8000000000000ll);
+  LC[(long)id * Nprof + k] = v;
+  if (k > 0) DLC[(long)id * (Nprof - 1) + k - 1] = v - LC[(long)id * Nprof + k - 1];
+}
+
+void sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int Nprof, int Nloc, const int* lx,
+                    const int* ly, double* LC, double* DLC) {
+  if (Nloc <= 0) return;
+  k_sample_nearest<<<ceil_div(Nloc, 256), 256, 0, ctx->stream>>>(map, Nx, Ny, k, Nprof, Nloc, lx, ly, LC, DLC);
+  MLC_CHECK_LAUNCH();
+}
+
+// Bilinear weights of RectGrid::interp2d_bilinear (rectGrid.cpp:349-378) on pixel
+// centres j + 1/2.  The position is split into an exact integer base (bx, by) and a
+// small offset (fx, fy) so that FP32 keeps sub-pixel precision far from the origin.
+template <typename T>
+struct Bilin {
+  int jl, jr, il, iu;
+  T w0, w1, w2, w3;  // (iu,jl) (iu,jr) (il,jl) (il,jr)
+  bool inside;
+};
+
+template <typename T>
+__device__ __forceinline__ Bilin<T> bilin_weights(long bx, T fx, long by, T fy, int Nx, int Ny) {
+  Bilin<T> B;
+  // absolute coordinate = b + f ; hull of centres is [0.5, N - 0.5]
+  const T flx = floor(fx), fly = floor(fy);
+  const long jx = bx + (long)flx, iy = by + (long)fly;  // pixel containing the point
+  const T rx = fx - flx, ry = fy - fly;                 // in [0, 1)
+  B.inside = !((jx < 0) || (jx == 0 && rx < (T)0.5) || (jx > Nx - 1) || (jx == Nx - 1 && rx > (T)0.5) ||
+               (iy < 0) || (iy == 0 && ry < (T)0.5) || (iy > Ny - 1) || (iy == Ny - 1 && ry > (T)0.5));
+  const T dx = rx - (T)0.5, dy = ry - (T)0.5;
+  const long jl = (dx < 0) ? jx - 1 : jx;
+  const long iu = (dy < 0) ? iy : iy + 1;
+  // a = x - centre(jl), b = centre(jl+1) - x, c = centre(iu) - y, d = y - centre(iu-1)
+  const T a = (dx < 0) ? rx + (T)0.5 : dx;
+  const T b = (T)1 - a;
+  const T d = (dy < 0) ? ry + (T)0.5 : dy;
+  const T c = (T)1 - d;
+  B.jl = (int)jl;
+  B.jr = (int)min(jl + 1, (long)Nx - 1);
+  B.iu = (int)min(iu, (long)Ny - 1);
+  B.il = (int)(iu - 1);
+  B.w0 = b * d;
+  B.w1 = a * d;
+  B.w2 = b * c;
+  B.w3 = a * c;
+  return B;
+}
+
+template <typename T>
+__device__ __forceinline__ T bilin_read(const T* __restrict__ m, const Bilin<T>& B, int Nx) {
+  T z = B.w0 * __ldg(m + (long)B.iu * Nx + B.jl);
+  z += B.w1 * __ldg(m + (long)B.iu * Nx + B.jr);
+  z += B.w2 * __ldg(m + (long)B.il * Nx + B.jl);
+  z += B.w3 * __ldg(m + (long)B.il * Nx + B.jr);
+  return z;
+}
+
+__device__ __forceinline__ double mlc_log10(double x) { return log10(x); }
+__device__ __forceinline__ float mlc_log10(float x) { return log10f(x); }
+
+template <typename T>
+struct MapList {
+  const T* m[16];
+};
+
+// One warp per track; lanes walk the track's epochs.  For every epoch the position
+// and weights are computed once and reused for each of the nm maps of this launch.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sample_tracks(MapList<T> maps, int nm, int Nx, int Ny, int ntracks,
+                                                       const T* __restrict__ x0, const T* __restrict__ y0,
+                                                       const T* __restrict__ phi, const T* __restrict__ v,
+                                                       const int64_t* __restrict__ off, const T* __restrict__ t,
+                                                       int mag, T* __restrict__ out, long E, int m_base) {
+  const int lane = threadIdx.x & 31;
+  const long track = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (track >= ntracks) return;
+  const T X0 = x0[track], Y0 = y0[track], V = v[track];
+  T sn, cs;
+  if (sizeof(T) == 8) {
+    double s_, c_;
+    sincos((double)phi[track], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  } else {
+    float s_, c_;
+    sincosf((float)phi[track], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  }
+  const long bx = (long)floor(X0), by = (long)floor(Y0);
+  const T fx0 = X0 - (T)bx, fy0 = Y0 - (T)by;
+  const int64_t e0 = off[track], e1 = off[track + 1];
+  for (int64_t e = e0 + lane; e < e1; e += 32) {
+    const T vt = V * t[e];
+    const T fx = fx0 + vt * cs, fy = fy0 + vt * sn;
+    const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
+    for (int q = 0; q < nm; q++) {
+      T mu = B.inside ? bilin_read<T>(maps.m[q], B, Nx) : (T)0;
+      out[(long)(m_base + q) * E + e] = mag ? (T)-2.5 * mlc_log10(mu) : mu;
+    }
+  }
+}
+
+template <typename T>
+static void sample_tracks_impl(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny,
+                               int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
+                               const int64_t* off, const void* t, int mag, void* out, long E) {
+  for (int base = 0; base < nmaps; base += 16) {
+    MapList<T> ml{};
+    const int nm = std::min(16, nmaps - base);
+    for (int q = 0; q < nm; q++) ml.m[q] = (const T*)maps_host[base + q];
+    const int warps_per_block = 8;
+    const int grid = ceil_div(ntracks, warps_per_block);
+    k_sample_tracks<T><<<grid, 256, 0, ctx->stream>>>(ml, nm, Nx, Ny, ntracks, (const T*)x0, (const T*)y0,
+                                                      (const T*)phi, (const T*)v, off, (const T*)t, mag,
+                                                      (T*)out, E, base);
+    MLC_CHECK_LAUNCH();
+  }
+}
+
+void sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny, int prec,
+                   int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
+                   const int64_t* off, const void* t, int mag, void* out, long E) {
+  if (ntracks <= 0 || nmaps <= 0) return;
+  if (prec == MLC_F64)
+    sample_tracks_impl<double>(ctx, maps_host, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E);
+  else
+    sample_tracks_impl<float>(ctx, maps_host, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E);
+}
+
+// Offset-minimised chi2, one warp per curve, FP64 accumulation:
+// dm = sum w (o - m) / W ; chi2 = sum w (o - m - dm)^2 (two passes, no cancellation).
+template <typename T>
+__global__ void __launch_bounds__(256) k_chi2_offset(int ncurves, int T_, const T* __restrict__ m,
+                                                     const double* __restrict__ obs, const double* __restrict__ w,
+                                                     double W, double* __restrict__ chi2, double* __restrict__ dm) {
+  const int lane = threadIdx.x & 31;
+  const long k = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (k >= ncurves) return;
+  const T* mk = m + k * T_;
+  double sr = 0.0;
+  for (int e = lane; e < T_; e += 32) sr += __ldg(w + e) * (__ldg(obs + e) - (double)mk[e]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sr += __shfl_xor_sync(0xffffffffu, sr, o);
+  const double off = sr / W;
+  double c = 0.0;
+  for (int e = lane; e < T_; e += 32) {
+    const double r = __ldg(obs + e) - (double)mk[e] - off;
+    c += __ldg(w + e) * r * r;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0) {
+    chi2[k] = c;
+    if (dm) dm[k] = off;
+  }
+}
+
+void chi2_offset(mlc_ctx* ctx, int prec, int ncurves, int T_, const void* m, const double* obs_dev,
+                 const double* w_dev, double W, double* chi2, double* dm) {
+  if (ncurves <= 0) return;
+  const int grid = ceil_div(ncurves, 8);
+  if (prec == MLC_F64)
+    k_chi2_offset<double><<<grid, 256, 0, ctx->stream>>>(ncurves, T_, (const double*)m, obs_dev, w_dev, W, chi2, dm);
+  else
+    k_chi2_offset<float><<<grid, 256, 0, ctx->stream>>>(ncurves, T_, (const float*)m, obs_dev, w_dev, W, chi2, dm);
+  MLC_CHECK_LAUNCH();
+}
+
+}  // namespace mlc

@@ -1,0 +1,75 @@
+"""Bilinear track sampling and offset-minimised chi2 on the GPU vs the oracle."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from microsn_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _tracks(n, N, seed, dtype):
+    x0, y0, phi, v, off, t = synth.tracks(n, N, 3.0, seed, epochs=(5, 60), v_range=(0.01, 0.2))
+    dev = "cuda:0"
+    T = lambda a: torch.as_tensor(np.asarray(a, dtype), device=dev)
+    return (x0, y0, phi, v, off, t), (T(x0), T(y0), T(phi), T(v), torch.as_tensor(off, device=dev), T(t))
+
+
+def test_tracks_f64_match_oracle(ctx):
+    import microsn_gb300 as mlc
+    N = 160
+    maps = [synth.lognormal_map(N, seed=s) for s in (1, 2, 3)]
+    host, dev = _tracks(500, N, 4, np.float64)
+    tmaps = [torch.as_tensor(m, device="cuda:0") for m in maps]
+    for mag in (True, False):
+        out = mlc.sample_tracks(ctx, tmaps, N, N, *dev, mag=mag).cpu().numpy()
+        for q, m in enumerate(maps):
+            ref = oracle.sample_tracks(m, *host, mag=mag)
+            if mag:
+                assert np.max(np.abs(out[q] - ref)) < 1e-9
+            else:
+                assert np.max(np.abs(out[q] - ref) / np.abs(ref)) < 1e-9
+
+
+def test_tracks_degenerate_equals_nearest(ctx):
+    import microsn_gb300 as mlc
+    N = 64
+    mp = synth.lognormal_map(N, seed=7)
+    rng = np.random.default_rng(0)
+    lx = rng.integers(0, N, 200); ly = rng.integers(0, N, 200)
+    dev = "cuda:0"
+    x0 = torch.as_tensor(lx + 0.5, dtype=torch.float64, device=dev)
+    y0 = torch.as_tensor(ly + 0.5, dtype=torch.float64, device=dev)
+    z = torch.zeros(200, dtype=torch.float64, device=dev)
+    off = torch.arange(0, 201, dtype=torch.int64, device=dev)
+    t = torch.ones(200, dtype=torch.float64, device=dev)
+    out = mlc.sample_tracks(ctx, [torch.as_tensor(mp, device=dev)], N, N, x0, y0, z, z, off, t, mag=False)
+    assert np.array_equal(out.cpu().numpy()[0], mp[ly, lx])
+
+
+def test_tracks_f32_tolerance(ctx):
+    import microsn_gb300 as mlc
+    N = 2000
+    mp = synth.lognormal_map(N, seed=11)
+    host, dev = _tracks(2000, N, 5, np.float32)
+    host64 = tuple(np.asarray(a, np.float64) if i != 4 else a for i, a in enumerate(host))
+    out = mlc.sample_tracks(ctx, [torch.as_tensor(mp.astype(np.float32), device="cuda:0")], N, N, *dev,
+                            mag=True).cpu().numpy()[0]
+    ref = oracle.sample_tracks(mp.astype(np.float32).astype(np.float64), *host64, mag=True)
+    # FP32 positions and bilinear weights: 2e-4 mag
+    assert np.max(np.abs(out - ref)) < 2e-4, np.max(np.abs(out - ref))
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_chi2_offset(ctx, prec):
+    import microsn_gb300 as mlc
+    rng = np.random.default_rng(3)
+    m = rng.normal(0, 1, (1000, 50))
+    o = rng.normal(0, 1, 50); w = 1 / (rng.random(50) * 0.1 + 0.02) ** 2
+    dt = torch.float64 if prec == "f64" else torch.float32
+    mt = torch.as_tensor(m, dtype=dt, device="cuda:0")
+    chi2, dm = mlc.chi2_offset(ctx, mt, o, w)
+    ref, dmr = oracle.chi2_offset(mt.double().cpu().numpy(), o, w)
+    np.testing.assert_allclose(chi2.cpu().numpy(), ref, rtol=1e-12)
+    np.testing.assert_allclose(dm.cpu().numpy(), dmr, rtol=1e-12, atol=1e-14)
