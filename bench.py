@@ -1,0 +1,463 @@
+#!/usr/bin/env python
+"""Throughput of the light-curve hot path on one GB300 (light curves/s).
+
+Workload (the batched-profiles-and-tracks configuration): a 10000 x 10000 FP32
+magnification map (inverse ray shooting, kappa_* = 0.45, gamma = 0.35, width 20
+Einstein radii, seed 2) convolved with 16 profiles -- uniform disc and thin disc
+(exponential shape), half-light radii 2, 4, 8, 16, 32, 48, 64, 96 px -- then 10^6
+straight tracks (epochs uniform in 20..200 over 3 observing seasons with gaps)
+sampled bilinearly on every convolved map and converted to magnitudes.  One light
+curve = one track x one profile.  A step = map spectrum + 16 fused convolutions +
+sampling of all tracks on all 16 maps.
+
+Also reported: the plain one-launch-per-stage FP64 form of the same step, e2e
+throughput through the library with host buffers (H2D of the map and tracks, D2H of
+all light curves inside the timed region), per-kernel CUDA-event times, the roofline
+of the dominant kernel, GPU clocks during the timed region and an FP64 CPU baseline
+(the oracle port on the host cores, on a bounded sample).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "light curves/s and pair-chi2/s on 1 GB300, batched vs plain, at <=1e-5 rel err vs FP64"
+UNIT = "light curves/s"
+
+N_MAP, WIDTH, KAPPA, GAMMA, MAP_SEED = 10000, 20.0, 0.45, 0.35, 2
+RHALF_PX = [2, 4, 8, 16, 32, 48, 64, 96]
+SHAPES = ["uniform", "exponential"]
+N_TRACKS, EPOCHS, SEASONS, TRACK_SEED = 1_000_000, (20, 200), 3, 3
+V_RANGE = (0.05, 1.0)  # pixels / day
+SEASON_LEN, GAP = 120.0, 245.0
+MARGIN = 2 * max(RHALF_PX) + 2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--small", action="store_true", help="reduced sizes (debug only; not a bench number)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 form")
+    return ap.parse_args()
+
+
+def workload_config(small=False):
+    n = 2000 if small else N_MAP
+    nt = 20000 if small else N_TRACKS
+    return dict(workload="batched profiles and tracks: 10000^2 FP32 map x 16 profiles, 10^6 tracks" if not small
+                else "debug-small", map=f"{n}x{n} ray-shot kappa*={KAPPA} gamma={GAMMA} width={WIDTH} R_E seed {MAP_SEED}",
+                profiles=f"{SHAPES} x rhalf {RHALF_PX} px", tracks=nt,
+                epochs=f"U{{{EPOCHS[0]}..{EPOCHS[1]}}} in {SEASONS} seasons", velocity_px_per_day=list(V_RANGE),
+                l2="inputs larger than L2: every map is 400 MB (FP32), L2 is 129 MB", n=n)
+
+
+# ----------------------------------------------------------------------------- tracks on the device
+
+def make_tracks_torch(ntracks, nmap, seed, device, dtype):
+    """Vectorised, seeded track set: same distribution as microsn_gb300.synth.tracks."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    n = torch.randint(EPOCHS[0], EPOCHS[1] + 1, (ntracks,), generator=g)
+    off = torch.zeros(ntracks + 1, dtype=torch.int64)
+    off[1:] = torch.cumsum(n, 0)
+    E = int(off[-1])
+    tid = torch.repeat_interleave(torch.arange(ntracks), n)
+    j = torch.arange(E) - off[tid]  # epoch index within its track
+    nk = n[tid]
+    # epochs spread over the seasons in order; jitter inside each slot keeps them sorted
+    season = (j * SEASONS) // nk
+    first = (season * nk + SEASONS - 1) // SEASONS
+    cnt = ((season + 1) * nk + SEASONS - 1) // SEASONS - first
+    u = torch.rand(E, generator=g, dtype=torch.float64)
+    q = ((j - first).double() + u) / cnt.double()
+    t = season.double() * (SEASON_LEN + GAP) + q * SEASON_LEN
+    phi = torch.rand(ntracks, generator=g, dtype=torch.float64) * 2 * 3.141592653589793
+    v = V_RANGE[0] + (V_RANGE[1] - V_RANGE[0]) * torch.rand(ntracks, generator=g, dtype=torch.float64)
+    tmax = t[off[1:] - 1]
+    room = 0.9 * (nmap - 2 * MARGIN)  # keep every track inside the map
+    v = torch.where(v * tmax > room, room / tmax.clamp(min=1e-300), v)
+    L = v * tmax
+    cx, sy = torch.cos(phi), torch.sin(phi)
+    lo = MARGIN + torch.clamp(-L * cx, min=0)
+    hi = nmap - MARGIN - torch.clamp(L * cx, min=0)
+    x0 = lo + (hi - lo) * torch.rand(ntracks, generator=g, dtype=torch.float64)
+    lo = MARGIN + torch.clamp(-L * sy, min=0)
+    hi = nmap - MARGIN - torch.clamp(L * sy, min=0)
+    y0 = lo + (hi - lo) * torch.rand(ntracks, generator=g, dtype=torch.float64)
+    host = dict(x0=x0, y0=y0, phi=phi, v=v, off=off, t=t)
+    dev = {k: (a.to(device=device, dtype=dtype) if a.dtype == torch.float64 else a.to(device)) for k, a in host.items()}
+    return host, dev, E
+
+
+def profiles_for(n):
+    import microsn_gb300 as mlc
+    pix = WIDTH / n
+    return [mlc.profile(s, r * pix, pix, ref_compat=False) for s in SHAPES for r in RHALF_PX]
+
+
+# ----------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.lines = []
+        self.p = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- roofline helpers
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(name, n, E, nprof, e=4):
+    """Algorithmic bytes of one launch of each kernel at this workload (FP32, e = 4 B)."""
+    Wc = n // 2 + 1
+    spec = n * Wc * 2 * e  # complex half spectrum
+    real = n * n * e
+    table = {
+        "fft_rows_r2c": real + spec,           # read a real map, write its row spectra
+        "fft_rows_c2r": spec + real,           # read row spectra, write a real map
+        "fft_col_A": 2 * spec,                 # in-place column sub-pass: read + write
+        "fft_col_B": 2 * spec,
+        "conv_fused_spectrum": 2 * spec,       # read map spectrum, write product sub-pass output
+        "sample_tracks": E * e + (n // 1) * 0 + nprof * real + E * nprof * e,  # t in, one read of each map, LCs out
+    }
+    return table.get(name)
+
+
+def load_traffic():
+    """DRAM bytes per launch from the committed ncu summary (scaled there to a full launch)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+# ----------------------------------------------------------------------------- CPU baseline (oracle port)
+
+def cpu_baseline(mp64, host_tracks, n, ntr_sample=20000, workers=None):
+    """FP64 oracle port on the host cores: scipy FFT convolution of the full map with one
+    profile, and bilinear sampling + magnitudes of ntr_sample tracks on it (threads over
+    track chunks).  Scaled to light curves/s for the whole workload."""
+    import concurrent.futures as cf
+
+    import numpy as np
+
+    import oracle
+    from microsn_gb300 import profile_raster
+    oracle.build()
+    workers = workers or os.cpu_count()
+    prof = profile_raster(profiles_for(n)[len(RHALF_PX) + 3])  # thin disc, 16 px
+    t0 = time.perf_counter()
+    cm = oracle.conv_fft_workers(mp64, prof, workers=workers)
+    t_conv = time.perf_counter() - t0
+    off = host_tracks["off"].numpy()
+    ntr = min(ntr_sample, len(off) - 1)
+    sl = slice(0, ntr)
+    x0 = host_tracks["x0"].numpy()[sl]; y0 = host_tracks["y0"].numpy()[sl]
+    phi = host_tracks["phi"].numpy()[sl]; v = host_tracks["v"].numpy()[sl]
+    o = off[: ntr + 1]
+    t = host_tracks["t"].numpy()[: o[-1]]
+    chunks = np.array_split(np.arange(ntr), workers)
+
+    def run(ix):
+        if len(ix) == 0:
+            return 0
+        a, b = ix[0], ix[-1] + 1
+        oo = o[a:b + 1] - o[a]
+        oracle.sample_tracks(cm, x0[a:b], y0[a:b], phi[a:b], v[a:b], oo, t[o[a]:o[b]])
+        return b - a
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(workers) as ex:
+        list(ex.map(run, chunks))
+    t_samp = time.perf_counter() - t0
+    per_profile = t_conv + t_samp * (N_TRACKS / ntr)
+    value = N_TRACKS / per_profile
+    return {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"oracle FP64: scipy.fft convolution of the full {n}^2 map with one thin-disc profile "
+                      f"({t_conv:.2f} s) + bilinear magnitudes of {ntr} tracks ({t_samp:.2f} s), scaled to "
+                      f"{N_TRACKS} tracks x 16 profiles"}
+
+
+# ----------------------------------------------------------------------------- reference arm
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+
+    from microsn_gb300 import synth
+    n = 2000 if args.small else N_MAP
+    mp = synth.lognormal_map(n, seed=MAP_SEED)
+    host, _, E = make_tracks_torch(N_TRACKS if not args.small else 20000, n, TRACK_SEED, "cpu", torch.float64)
+    vals = []
+    res = None
+    for s in range(args.warmup + args.steps):
+        res = cpu_baseline(mp, host, n, ntr_sample=10000)
+        if s >= args.warmup:
+            vals.append(res["value"])
+    value = statistics.mean(vals) if vals else res["value"]
+    ms = 16 * N_TRACKS / value * 1000.0
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lognormal map; same tracks)",
+           "config": workload_config(args.small),
+           "cpu_baseline": {"kind": res["kind"], "cores": res["cores"], "sample": res["sample"], "value": value,
+                            "unit": UNIT},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ----------------------------------------------------------------------------- main arm
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    from microsn_gb300 import build as B
+    from microsn_gb300 import synth
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    B.build()
+    dev = f"cuda:{local}"
+    torch.cuda.set_device(local)
+    n = 2000 if args.small else N_MAP
+    ntracks = 20000 if args.small else N_TRACKS
+    ctx = mlc.Context(local)
+    stream = torch.cuda.current_stream(local)
+
+    # ---- inputs resident in HBM
+    mp_t, meta = synth.rayshoot_gpu(ctx, n, WIDTH, KAPPA, GAMMA, seed=MAP_SEED + rank, rays_per_pixel=4.0,
+                                    dtype=torch.float32)
+    m = mlc.Map(ctx, mp_t, "f32")
+    host_tr, tr, E = make_tracks_torch(ntracks, n, TRACK_SEED + rank, dev, torch.float32)
+    profs = profiles_for(n)
+    convs = [torch.empty((n, n), dtype=torch.float32, device=dev) for _ in profs]
+    out = torch.empty((len(profs), E), dtype=torch.float32, device=dev)
+
+    def step():
+        m.refresh()
+        for k, p in enumerate(profs):
+            mlc.convolve(ctx, m, p, "fused", out=convs[k])
+        mlc.sample_tracks(ctx, convs, n, n, tr["x0"], tr["y0"], tr["phi"], tr["v"], tr["off"], tr["t"], mag=True,
+                          out=out)
+
+    for _ in range(max(args.warmup, 1)):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- timed region (device-resident inputs)
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    time.sleep(0.3)
+    l0 = ctx.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - l0
+    ms_total = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    lc_per_step = len(profs) * ntracks
+    value = world * lc_per_step / (ms_step / 1000.0)
+
+    # ---- per-kernel CUDA-event times over the same steps (separate pass: events add a little overhead)
+    ctx.set_timing(True)
+    ksteps = min(args.steps, 3)
+    for _ in range(ksteps):
+        step()
+    kt = ctx.kernel_times(reset=True)
+    ctx.set_timing(False)
+    per_step = {k: v[0] / ksteps for k, v in kt.items()}
+    total_k = sum(per_step.values())
+    dom = max(per_step, key=per_step.get)
+    dom_launch_ms = kt[dom][0] / kt[dom][1]
+    alg = algorithmic_bytes(dom, n, E, len(profs))
+    hbm, peak_kind = peaks()
+    traffic = load_traffic().get(dom)
+    roof = None
+    if alg is not None:
+        ach = alg / (dom_launch_ms / 1000.0) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": traffic, "algorithmic_bytes": alg, "launch_ms": dom_launch_ms,
+                "peak_source": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)",
+                "share_of_step": per_step[dom] / total_k if total_k else None}
+    kernels = {k: {"ms_per_step": v, "launches_per_step": kt[k][1] / ksteps,
+                   "GB_per_s": (algorithmic_bytes(k, n, E, len(profs)) / (kt[k][0] / kt[k][1] / 1000.0) / 1e9)
+                   if algorithmic_bytes(k, n, E, len(profs)) else None} for k, v in per_step.items()}
+
+    # ---- e2e through the library with host buffers
+    h_map = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+    h_map.copy_(mp_t.cpu())
+    h_tr = {k: torch.empty_like(tr[k], device="cpu").pin_memory() for k in tr}
+    for k in tr:
+        h_tr[k].copy_(tr[k].cpu())
+    h_out = torch.empty((len(profs), E), dtype=torch.float32, pin_memory=True)
+    dmap = m.tensor()
+    bi = h_map.numel() * 4 + sum(h_tr[k].numel() * h_tr[k].element_size() for k in h_tr)
+    bo = h_out.numel() * 4
+
+    def e2e_step():
+        dmap.copy_(h_map, non_blocking=True)
+        for k in tr:
+            tr[k].copy_(h_tr[k], non_blocking=True)
+        step()
+        h_out.copy_(out, non_blocking=True)
+
+    e2e_step()
+    barrier()
+    esteps = max(1, min(args.steps, 3))
+    e0.record(stream)
+    for _ in range(esteps):
+        e2e_step()
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / esteps
+    e2e_val = world * lc_per_step / (e2e_ms / 1000.0)
+    del h_out
+
+    # ---- the plain one-launch-per-stage FP64 form of the same step
+    plain = None
+    if not args.no_plain:
+        m64 = mlc.Map(ctx, mp_t.double(), "f64")
+        convs64 = [torch.empty((n, n), dtype=torch.float64, device=dev) for _ in range(2)]
+        tr64 = {k: (a.to(dev, torch.float64) if a.dtype == torch.float64 else a.to(dev)) for k, a in host_tr.items()}
+        out64 = torch.empty((1, E), dtype=torch.float64, device=dev)
+
+        def step64():
+            m64.refresh()
+            for k, p in enumerate(profs):
+                c = convs64[k % 2]
+                mlc.convolve(ctx, m64, p, "plain", out=c)
+                mlc.sample_tracks(ctx, [c], n, n, tr64["x0"], tr64["y0"], tr64["phi"], tr64["v"], tr64["off"],
+                                  tr64["t"], mag=True, out=out64)
+
+        step64()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        step64()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1)
+        plain = {"value": world * lc_per_step / (pms / 1000.0), "unit": UNIT, "ms_per_step": pms, "dtype": "f64",
+                 "form": "full-size wrapped kernel + forward FFT + multiply + inverse FFT + sampling, per profile",
+                 "batched_over_plain": value / (world * lc_per_step / (pms / 1000.0))}
+        del m64, convs64, tr64, out64
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(mp_t.double().cpu().numpy(), host_tr, n)
+
+    if rank == 0:
+        res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic: seeded inverse-ray-shot map, seeded tracks (no public dataset)",
+               "config": workload_config(args.small), "roofline": roof, "cpu_baseline": cpu,
+               "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
+                       "ms_per_step": e2e_ms},
+               "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
+               "light_curves_per_step": lc_per_step, "epochs_per_step": E}
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+
+
+if __name__ == "__main__":
+    main()

@@ -88,6 +88,16 @@ const char* mlc_ctx_last_error(const mlc_ctx* ctx);
 size_t mlc_ctx_workspace_bytes(const mlc_ctx* ctx);
 /* Library version (major*10000 + minor*100 + patch). */
 int mlc_version(void);
+/* Number of kernels this context has launched so far. */
+unsigned long long mlc_ctx_launch_count(const mlc_ctx* ctx);
+/* Per-kernel CUDA-event timing on the context's stream (off by default).  Turning it
+ * on brackets every launch with events; mlc_ctx_kernel_times synchronises, then writes
+ * up to cap entries of (name, total milliseconds, launches) -- names as a
+ * '\n'-separated list into names_host (size name_cap) -- and returns the entry count
+ * (or a negative status).  reset != 0 clears the totals afterwards. */
+int mlc_ctx_set_timing(mlc_ctx* ctx, int on);
+int mlc_ctx_kernel_times(mlc_ctx* ctx, char* names_host, int name_cap, double* ms_host, long* launches_host,
+                         int cap, int reset);
 
 /* ======================================================================= profiles (host) */
 
@@ -111,6 +121,9 @@ int mlc_map_data(mlc_map* map, void** dev_ptr);
 /* Forward spectrum of the map (computed once and cached), replacing the
  * cufftExecD2Z of the map (gpu_functions.cu:171-176). */
 int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map);
+/* Recompute the cached spectrum from the map's current pixels (after they were
+ * rewritten through mlc_map_data). */
+int mlc_map_refresh(mlc_ctx* ctx, mlc_map* map);
 
 /* ======================================================================= convolution */
 

@@ -46,6 +46,10 @@ SIGNATURES = {
     "mlc_ctx_synchronize": (i32, [vp]),
     "mlc_ctx_last_error": (C.c_char_p, [vp]),
     "mlc_ctx_workspace_bytes": (C.c_size_t, [vp]),
+    "mlc_ctx_launch_count": (C.c_ulonglong, [vp]),
+    "mlc_ctx_set_timing": (i32, [vp, i32]),
+    "mlc_ctx_kernel_times": (i32, [vp, C.c_char_p, i32, vp, vp, i32, i32]),
+    "mlc_map_refresh": (i32, [vp, vp]),
     "mlc_profile_dims": (i32, [C.POINTER(MlcProfile), P_i32]),
     "mlc_profile_raster": (i32, [C.POINTER(MlcProfile), vp, C.c_long, P_i32]),
     "mlc_map_create": (i32, [vp, vp, i32, i32, i32, i32, i32, C.POINTER(vp)]),

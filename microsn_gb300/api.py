@@ -63,6 +63,22 @@ class Context:
     def workspace_bytes(self) -> int:
         return int(self.L.mlc_ctx_workspace_bytes(self.h))
 
+    def launch_count(self) -> int:
+        return int(self.L.mlc_ctx_launch_count(self.h))
+
+    def set_timing(self, on: bool):
+        self.check(self.L.mlc_ctx_set_timing(self.h, int(on)))
+
+    def kernel_times(self, reset: bool = True) -> dict:
+        """{kernel name: (total ms, launches)} from the per-launch CUDA events."""
+        names = C.create_string_buffer(1 << 16)
+        ms = np.zeros(256); n_l = np.zeros(256, np.int64)
+        n = self.L.mlc_ctx_kernel_times(self.h, names, len(names), _ptr(ms), _ptr(n_l), 256, int(reset))
+        if n < 0:
+            self.check(-n)
+        keys = names.value.decode().split("\n")[:n]
+        return {k: (float(ms[i]), int(n_l[i])) for i, k in enumerate(keys)}
+
     def close(self):
         if getattr(self, "h", None):
             self.L.mlc_ctx_destroy(self.h)
@@ -91,6 +107,19 @@ def profile_raster(p: MlcProfile) -> np.ndarray:
     if st:
         raise MlcError(st, "profile raster failed")
     return out.reshape(n.value, n.value)
+
+
+class _CudaArray:
+    """Minimal __cuda_array_interface__ holder to view library-owned device memory in torch."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"data": (ptr, False), "shape": shape, "typestr": typestr, "version": 2}
+
+
+def _wrap_device_ptr(ptr, shape, dtype, device):
+    typestr = "<f8" if dtype == torch.float64 else "<f4"
+    with torch.cuda.device(device):
+        return torch.as_tensor(_CudaArray(ptr, shape, typestr), device=f"cuda:{device}")
 
 
 class Map:
@@ -129,6 +158,14 @@ class Map:
 
     def prepare(self):
         self.ctx.check(self.ctx.L.mlc_map_prepare(self.ctx.h, self.h))
+
+    def refresh(self):
+        """Recompute the spectrum from the current pixels."""
+        self.ctx.check(self.ctx.L.mlc_map_refresh(self.ctx.h, self.h))
+
+    def tensor(self) -> torch.Tensor:
+        """A torch view of the map's device pixels (shares memory with the library)."""
+        return _wrap_device_ptr(self.data_ptr(), (self.Ny, self.Nx), self.dtype, self.ctx.device)
 
     def close(self):
         if getattr(self, "h", None):

@@ -117,6 +117,51 @@ int mlc_ctx_destroy(mlc_ctx* ctx) {
   return MLC_OK;
 }
 
+unsigned long long mlc_ctx_launch_count(const mlc_ctx* ctx) { return ctx ? ctx->launches : 0ull; }
+
+static void resolve_timings(mlc_ctx* ctx) {
+  if (ctx->pending.empty()) return;
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (auto& p : ctx->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    auto& e = ctx->ktimes[p.name];
+    e.first += ms;
+    e.second += 1;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  ctx->pending.clear();
+}
+
+int mlc_ctx_set_timing(mlc_ctx* ctx, int on) {
+  return guarded(ctx, [&] {
+    resolve_timings(ctx);
+    ctx->timing = on != 0;
+  });
+}
+
+int mlc_ctx_kernel_times(mlc_ctx* ctx, char* names_host, int name_cap, double* ms_host, long* launches_host, int cap,
+                         int reset) {
+  if (!ctx || !names_host || !ms_host || !launches_host || cap < 0 || name_cap < 1) return -MLC_ERR_ARG;
+  int n = 0;
+  int st = guarded(ctx, [&] {
+    resolve_timings(ctx);
+    std::string names;
+    for (auto& kv : ctx->ktimes) {
+      if (n >= cap) break;
+      names += kv.first + "\n";
+      ms_host[n] = kv.second.first;
+      launches_host[n] = kv.second.second;
+      n++;
+    }
+    MLC_REQUIRE((int)names.size() < name_cap, MLC_ERR_LIMIT, "names buffer too small");
+    std::memcpy(names_host, names.c_str(), names.size() + 1);
+    if (reset) ctx->ktimes.clear();
+  });
+  return st ? -st : n;
+}
+
 int mlc_ctx_set_stream(mlc_ctx* ctx, void* stream) {
   if (!ctx) return MLC_ERR_ARG;
   ctx->stream = (cudaStream_t)stream;
@@ -234,6 +279,14 @@ static void map_prepare(mlc_ctx* ctx, mlc_map* map) {
 int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map) {
   if (!map) return fail(ctx, MLC_ERR_ARG, "null map");
   return guarded(ctx, [&] { map_prepare(ctx, map); });
+}
+
+int mlc_map_refresh(mlc_ctx* ctx, mlc_map* map) {
+  if (!map) return fail(ctx, MLC_ERR_ARG, "null map");
+  return guarded(ctx, [&] {
+    map->spec_valid = false;
+    map_prepare(ctx, map);
+  });
 }
 
 static const double* upload_profile(mlc_ctx* ctx, const mlc_profile& pr, int* pN) {

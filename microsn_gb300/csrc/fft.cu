@@ -362,7 +362,10 @@ static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, 
   size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
   auto kern = k_rows_r2c<T, Loader>;
   set_max_smem((const void*)kern, smem);
-  kern<<<nrows, 512, smem, ctx->stream>>>(ld, (C2<T>*)out, p.Wp, p.M, p.rlM, (const C2<T>*)p.twx);
+  {
+    MLC_KSCOPE(ctx, "fft_rows_r2c");
+    kern<<<nrows, 512, smem, ctx->stream>>>(ld, (C2<T>*)out, p.Wp, p.M, p.rlM, (const C2<T>*)p.twx);
+  }
   MLC_CHECK_LAUNCH();
 }
 
@@ -371,8 +374,11 @@ static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, vo
   size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
   auto kern = k_rows_c2r<T>;
   set_max_smem((const void*)kern, smem);
-  kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (T*)out, p.Nx, p.M, p.rlM,
+  {
+    MLC_KSCOPE(ctx, "fft_rows_c2r");
+    kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (T*)out, p.Nx, p.M, p.rlM,
                                          (const C2<T>*)p.twx);
+  }
   MLC_CHECK_LAUNCH();
 }
 
@@ -394,8 +400,11 @@ static void launch_colpass(mlc_ctx* ctx, const FftPlan2D& p, void* buf, char kin
   auto kern = k_colpass<T, CW, INV>;
   set_max_smem((const void*)kern, smem);
   dim3 grid(nstrips, nsets);
-  kern<<<grid, 256, smem, ctx->stream>>>((C2<T>*)buf, p.Wp, L, set_mul, j_mul, rl, (const C2<T>*)p.twy,
+  {
+    MLC_KSCOPE(ctx, kind == 'A' ? "fft_col_A" : "fft_col_B");
+    kern<<<grid, 256, smem, ctx->stream>>>((C2<T>*)buf, p.Wp, L, set_mul, j_mul, rl, (const C2<T>*)p.twy,
                                          tw_stride, post_tw);
+  }
   MLC_CHECK_LAUNCH();
 }
 
@@ -430,8 +439,11 @@ static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
   set_max_smem((const void*)kern, smem);
   dim3 grid(nstrips, p.N1);
   const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
-  kern<<<grid, 256, smem, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp, (const C2<T>*)kx, h, p.Ny,
+  {
+    MLC_KSCOPE(ctx, "conv_fused_spectrum");
+    kern<<<grid, 256, smem, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp, (const C2<T>*)kx, h, p.Ny,
                                          p.N1, p.N2, p.rlN2, (const C2<T>*)p.twy, scale);
+  }
   MLC_CHECK_LAUNCH();
   launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
   launch_rows_c2r<T>(ctx, p, tmp, out);
@@ -445,13 +457,19 @@ static void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
   void* kspec = ws_get(ctx, WS_KSPEC, p.spec_bytes());
   const long total = (long)p.Nx * p.Ny;
   int grid = (int)std::min<long>((total + 255) / 256, (long)ctx->sm_count * 16);
-  k_wrap_full<T><<<grid, 256, 0, ctx->stream>>>(prof, pN, p.Nx, p.Ny, (T*)kreal);
+  {
+    MLC_KSCOPE(ctx, "conv_plain_wrap");
+    k_wrap_full<T><<<grid, 256, 0, ctx->stream>>>(prof, pN, p.Nx, p.Ny, (T*)kreal);
+  }
   MLC_CHECK_LAUNCH();
   forward_impl<T>(ctx, p, kreal, sizeof(T) == 8 ? MLC_F64 : MLC_F32, kspec);
   const long n = (long)p.Ny * p.Wp;
   const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
   grid = (int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 16);
-  k_multiply<T><<<grid, 256, 0, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)kspec, n, scale);
+  {
+    MLC_KSCOPE(ctx, "conv_plain_multiply");
+    k_multiply<T><<<grid, 256, 0, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)kspec, n, scale);
+  }
   MLC_CHECK_LAUNCH();
   launch_colpass<T, true>(ctx, p, kspec, 'B', 1);
   launch_colpass<T, true>(ctx, p, kspec, 'A', 0);

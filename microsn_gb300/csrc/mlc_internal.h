@@ -53,6 +53,15 @@ struct mlc_ctx {
   cudaStream_t stream = nullptr;
   int sm_count = 0;
   std::string err;
+  // launch accounting and optional per-kernel CUDA-event timing
+  unsigned long long launches = 0;
+  bool timing = false;
+  struct Pending {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<Pending> pending;
+  std::map<std::string, std::pair<double, long>> ktimes;  // name -> (ms, launches)
   void* ws_ptr[mlc::WS_NSLOTS] = {};
   size_t ws_size[mlc::WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int>, std::unique_ptr<mlc::FftPlan2D>> plans;
@@ -82,6 +91,29 @@ struct DeviceGuard {
 };
 
 void* ws_get(mlc_ctx* ctx, int slot, size_t bytes);
+
+// Scope around one kernel launch: counts it and, when the context's timing is on,
+// brackets it with CUDA events on the context's stream.
+struct KernelScope {
+  mlc_ctx* ctx;
+  const char* name;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KernelScope(mlc_ctx* c, const char* n) : ctx(c), name(n) {
+    ctx->launches++;
+    if (ctx->timing) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, ctx->stream);
+    }
+  }
+  ~KernelScope() {
+    if (a) {
+      cudaEventRecord(b, ctx->stream);
+      ctx->pending.push_back({name, a, b});
+    }
+  }
+};
+#define MLC_KSCOPE(ctx, name) ::mlc::KernelScope ks_##__LINE__((ctx), (name))
 
 // Raise a kernel's dynamic shared-memory limit once.
 void set_max_smem(const void* func, size_t bytes);

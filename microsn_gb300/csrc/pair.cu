@@ -192,11 +192,17 @@ void pair_setup(mlc_ctx* ctx, int Nloc, int Nprof, const double* LCA, const doub
   MLC_REQUIRE(P <= 0xFFFFFFFFl, MLC_ERR_LIMIT, "Nloc^2 above 2^32-1");
   uint64_t* keys = (uint64_t*)ws_get(ctx, WS_PAIR_ACC, sizeof(uint64_t) * P + sizeof(uint32_t) * P + 4096);
   uint32_t* idx = reinterpret_cast<uint32_t*>(keys + P);
-  k_pair_z<<<grid_for(ctx, P), 256, 0, ctx->stream>>>(LCA, LCB, Nloc, Nprof, keys, idx);
+  {
+    MLC_KSCOPE(ctx, "pair_z");
+    k_pair_z<<<grid_for(ctx, P), 256, 0, ctx->stream>>>(LCA, LCB, Nloc, Nprof, keys, idx);
+  }
   MLC_CHECK_LAUNCH();
   radix_sort_u64_u32(ctx, P, keys, idx);
   if (rank) {
-    k_invert_perm<<<grid_for(ctx, P), 256, 0, ctx->stream>>>(idx, P, rank);
+    {
+      MLC_KSCOPE(ctx, "pair_rank");
+      k_invert_perm<<<grid_for(ctx, P), 256, 0, ctx->stream>>>(idx, P, rank);
+    }
     MLC_CHECK_LAUNCH();
   }
   if (Nbins > 0) {
@@ -205,7 +211,10 @@ void pair_setup(mlc_ctx* ctx, int Nloc, int Nprof, const double* LCA, const doub
     uint64_t* dek = (uint64_t*)ws_get(ctx, WS_SMALL, sizeof(uint64_t) * Nbins + sizeof(uint32_t) * Nbins);
     uint32_t* dup = reinterpret_cast<uint32_t*>(dek + Nbins);
     MLC_CUDA(cudaMemcpyAsync(dek, ek.data(), sizeof(uint64_t) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
-    k_upper_bound<<<ceil_div(Nbins, 256), 256, 0, ctx->stream>>>(keys, P, dek, Nbins, dup);
+    {
+      MLC_KSCOPE(ctx, "pair_upper_bound");
+      k_upper_bound<<<ceil_div(Nbins, 256), 256, 0, ctx->stream>>>(keys, P, dek, Nbins, dup);
+    }
     MLC_CHECK_LAUNCH();
     std::vector<uint32_t> up(Nbins);
     MLC_CUDA(cudaMemcpyAsync(up.data(), dup, sizeof(uint32_t) * Nbins, cudaMemcpyDeviceToHost, ctx->stream));
@@ -256,9 +265,15 @@ static Interp build_interp(mlc_ctx* ctx, int Njp, const int* indA, const int* in
                 "interpolation index out of the profile range");
   }
   if (n > 0) {
-    k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCA, DLCA, Nloc, Nprof, Njp, iA, fA, I.mA);
+    {
+      MLC_KSCOPE(ctx, "pair_interp");
+      k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCA, DLCA, Nloc, Nprof, Njp, iA, fA, I.mA);
+    }
     MLC_CHECK_LAUNCH();
-    k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCB, DLCB, Nloc, Nprof, Njp, iB, fB, I.mB);
+    {
+      MLC_KSCOPE(ctx, "pair_interp");
+      k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCB, DLCB, Nloc, Nprof, Njp, iB, fB, I.mB);
+    }
     MLC_CHECK_LAUNCH();
   }
   return I;
@@ -269,7 +284,10 @@ void pair_chi2_ratio(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, co
                      const double* DLCA, const double* LCB, const double* DLCB, const uint32_t* rank, double* chi2) {
   Interp I = build_interp(ctx, Njp, indA, indB, facA, facB, d, s, Nloc, Nprof, LCA, DLCA, LCB, DLCB);
   dim3 grid(ceil_div(Nloc, 32), ceil_div(Nloc, 8));
-  k_pair_chi2_ratio<<<grid, 256, 0, ctx->stream>>>(I.mA, I.mB, Nloc, Njp, I.d, I.s, rank, chi2);
+  {
+    MLC_KSCOPE(ctx, "pair_chi2_ratio");
+    k_pair_chi2_ratio<<<grid, 256, 0, ctx->stream>>>(I.mA, I.mB, Nloc, Njp, I.d, I.s, rank, chi2);
+  }
   MLC_CHECK_LAUNCH();
 }
 
@@ -283,7 +301,10 @@ void bin_chi2(mlc_ctx* ctx, int Nbins, const uint32_t* lower_host, const uint32_
   uint32_t* np = lo + Nbins;
   MLC_CUDA(cudaMemcpyAsync(lo, lower_host, sizeof(uint32_t) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
   MLC_CUDA(cudaMemcpyAsync(np, nper_host, sizeof(uint32_t) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
-  k_bin_means<<<Nbins, 256, 0, ctx->stream>>>(chi2_sorted, lo, np, bc, be);
+  {
+    MLC_KSCOPE(ctx, "pair_bin_means");
+    k_bin_means<<<Nbins, 256, 0, ctx->stream>>>(chi2_sorted, lo, np, bc, be);
+  }
   MLC_CHECK_LAUNCH();
   MLC_CUDA(cudaMemcpyAsync(bchi2_host, bc, sizeof(double) * Nbins, cudaMemcpyDeviceToHost, ctx->stream));
   MLC_CUDA(cudaMemcpyAsync(bexp_host, be, sizeof(double) * Nbins, cudaMemcpyDeviceToHost, ctx->stream));
@@ -306,8 +327,11 @@ void pair_bin_fused(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, con
   const size_t smem = (sizeof(double) * 3 + sizeof(unsigned)) * Nbins;
   set_max_smem((const void*)k_pair_bin_fused, smem);
   dim3 grid(ceil_div(Nloc, 256), ceil_div(Nloc, 8));
-  k_pair_bin_fused<<<grid, 256, smem, ctx->stream>>>(I.mA, I.mB, LCA, LCB, Nloc, Nprof, Njp, I.d, I.s, Nbins, de,
+  {
+    MLC_KSCOPE(ctx, "pair_bin_fused");
+    k_pair_bin_fused<<<grid, 256, smem, ctx->stream>>>(I.mA, I.mB, LCA, LCB, Nloc, Nprof, Njp, I.d, I.s, Nbins, de,
                                                       gs, ge, gc);
+  }
   MLC_CHECK_LAUNCH();
   std::vector<double> hs(Nbins), he(Nbins);
   std::vector<unsigned long long> hc(Nbins);

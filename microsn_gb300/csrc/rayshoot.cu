@@ -56,8 +56,11 @@ extern "C" int mlc_rayshoot(void* ctx_, const float* lenses_xy, int nl, double k
     MLC_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)N * N, ctx->stream));
     const long total = nrx * nry;
     const int grid = (int)std::min<long>((total + 255) / 256, (long)ctx->sm_count * 8);
-    k_rayshoot<<<grid, 256, 0, ctx->stream>>>((const float2*)lenses_xy, nl, (float)kappa_c, (float)gamma, x0, y0,
+    {
+      MLC_KSCOPE(ctx, "rayshoot");
+      k_rayshoot<<<grid, 256, 0, ctx->stream>>>((const float2*)lenses_xy, nl, (float)kappa_c, (float)gamma, x0, y0,
                                               dx, nrx, nry, (float)(width / 2), N, counts);
+    }
     MLC_CHECK_LAUNCH();
     return MLC_OK;
   } catch (const Error& e) {

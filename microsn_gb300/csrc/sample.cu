@@ -23,7 +23,10 @@ __global__ void k_sample_nearest(const double* __restrict__ map, int Nx, int Ny,
 void sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int Nprof, int Nloc, const int* lx,
                     const int* ly, double* LC, double* DLC) {
   if (Nloc <= 0) return;
-  k_sample_nearest<<<ceil_div(Nloc, 256), 256, 0, ctx->stream>>>(map, Nx, Ny, k, Nprof, Nloc, lx, ly, LC, DLC);
+  {
+    MLC_KSCOPE(ctx, "sample_nearest");
+    k_sample_nearest<<<ceil_div(Nloc, 256), 256, 0, ctx->stream>>>(map, Nx, Ny, k, Nprof, Nloc, lx, ly, LC, DLC);
+  }
   MLC_CHECK_LAUNCH();
 }
 
@@ -130,9 +133,12 @@ static void sample_tracks_impl(mlc_ctx* ctx, const void* const* maps_host, int n
     for (int q = 0; q < nm; q++) ml.m[q] = (const T*)maps_host[base + q];
     const int warps_per_block = 8;
     const int grid = ceil_div(ntracks, warps_per_block);
-    k_sample_tracks<T><<<grid, 256, 0, ctx->stream>>>(ml, nm, Nx, Ny, ntracks, (const T*)x0, (const T*)y0,
+    {
+      MLC_KSCOPE(ctx, "sample_tracks");
+      k_sample_tracks<T><<<grid, 256, 0, ctx->stream>>>(ml, nm, Nx, Ny, ntracks, (const T*)x0, (const T*)y0,
                                                       (const T*)phi, (const T*)v, off, (const T*)t, mag,
                                                       (T*)out, E, base);
+    }
     MLC_CHECK_LAUNCH();
   }
 }
@@ -180,9 +186,15 @@ void chi2_offset(mlc_ctx* ctx, int prec, int ncurves, int T_, const void* m, con
   if (ncurves <= 0) return;
   const int grid = ceil_div(ncurves, 8);
   if (prec == MLC_F64)
-    k_chi2_offset<double><<<grid, 256, 0, ctx->stream>>>(ncurves, T_, (const double*)m, obs_dev, w_dev, W, chi2, dm);
+    {
+      MLC_KSCOPE(ctx, "chi2_offset");
+      k_chi2_offset<double><<<grid, 256, 0, ctx->stream>>>(ncurves, T_, (const double*)m, obs_dev, w_dev, W, chi2, dm);
+    }
   else
-    k_chi2_offset<float><<<grid, 256, 0, ctx->stream>>>(ncurves, T_, (const float*)m, obs_dev, w_dev, W, chi2, dm);
+    {
+      MLC_KSCOPE(ctx, "chi2_offset");
+      k_chi2_offset<float><<<grid, 256, 0, ctx->stream>>>(ncurves, T_, (const float*)m, obs_dev, w_dev, W, chi2, dm);
+    }
   MLC_CHECK_LAUNCH();
 }
 

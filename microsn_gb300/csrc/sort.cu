@@ -1,11 +1,14 @@
 // Hand-written stable LSD radix sort (8-bit digits) of 64-bit keys carrying 32-bit
 // values, and warp-aggregated shared-memory histograms.
 //
-// One pass per digit: (1) k_digit_hist counts every digit of every tile in a single read
-// of the keys (all eight digits at once, so digit positions where all keys agree are
-// skipped); (2) k_scan_digit turns the per-tile counts of one digit position into global
-// scatter offsets; (3) k_scatter ranks each key inside its tile with __match_any_sync
-// in element order (stable) and scatters key and value.
+// Up front, k_digit_hist counts all eight digits of every tile in one read of the keys;
+// their totals give each digit's global start and let passes where all keys share a
+// digit be skipped.  Then one pass per remaining digit: (1) per-tile counts of that
+// digit in the keys' current order (the up-front counts serve the first pass only,
+// since each scatter permutes the keys); (2) k_scan_digit turns them into scatter
+// offsets; (3) k_scatter ranks each key inside its tile with __match_any_sync in
+// element order (stable) and scatters key and value.  Every scatter address is checked
+// against n; a violation sets an error flag instead of writing.
 #include <cub/block/block_scan.cuh>
 
 #include "mlc_internal.h"
@@ -68,6 +71,21 @@ __global__ void __launch_bounds__(1024) k_scan_digit(const uint32_t* __restrict_
   }
 }
 
+// Per-tile counts of one digit position in the current key order: hist [digit][tile].
+__global__ void __launch_bounds__(SORT_THREADS) k_tile_hist(const uint64_t* __restrict__ keys, long n, int ntiles,
+                                                            int shift, uint32_t* __restrict__ hist) {
+  __shared__ uint32_t cnt[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) cnt[i] = 0;
+  __syncthreads();
+  const long t0 = (long)blockIdx.x * SORT_TILE;
+  for (int q = 0; q < SORT_ITEMS; q++) {
+    const long i = t0 + (long)q * SORT_THREADS + threadIdx.x;
+    if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 0xff], 1u);
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < 256; d += blockDim.x) hist[(long)d * ntiles + blockIdx.x] = cnt[d];
+}
+
 // totals[p*256 + d] = number of keys whose digit p is d
 __global__ void __launch_bounds__(256) k_digit_totals(const uint32_t* __restrict__ hist, int ntiles,
                                                       unsigned long long* __restrict__ totals) {
@@ -88,7 +106,7 @@ __global__ void __launch_bounds__(256) k_digit_totals(const uint32_t* __restrict
 __global__ void __launch_bounds__(SORT_THREADS) k_scatter(const uint64_t* __restrict__ kin,
                                                           const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                                                           uint32_t* __restrict__ vout, long n, int ntiles, int shift,
-                                                          const uint32_t* __restrict__ offs) {
+                                                          const uint32_t* __restrict__ offs, int* __restrict__ err) {
   __shared__ uint32_t wcnt[SORT_WARPS][256];  // per-warp running digit counts, then warp bases
   __shared__ uint32_t gbase[256];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -134,9 +152,13 @@ __global__ void __launch_bounds__(SORT_THREADS) k_scatter(const uint64_t* __rest
     const long i = t0 + q * 32 + lane;
     if (i < n) {
       const unsigned d = (unsigned)((key[q] >> shift) & 0xff);
-      const uint32_t dst = gbase[d] + wcnt[warp][d] + rank[q];
-      kout[dst] = key[q];
-      vout[dst] = vin[i];
+      const uint64_t dst = (uint64_t)gbase[d] + wcnt[warp][d] + rank[q];
+      if (dst < (uint64_t)n) {
+        kout[dst] = key[q];
+        vout[dst] = vin[i];
+      } else {
+        atomicExch(err, 1);
+      }
     }
   }
 }
@@ -149,13 +171,21 @@ void radix_sort_u64_u32(mlc_ctx* ctx, long n, uint64_t* keys, uint32_t* vals) {
   uint64_t* k2 = (uint64_t*)ws_get(ctx, WS_SORT_KEYS, sizeof(uint64_t) * n);
   uint32_t* v2 = (uint32_t*)ws_get(ctx, WS_SORT_VALS, sizeof(uint32_t) * n);
   uint32_t* hist = (uint32_t*)ws_get(ctx, WS_SORT_HIST,
-                                     sizeof(uint32_t) * (256 * (size_t)ntiles * 9 + 8 * 256) + 8 * 256 * 8);
+                                     sizeof(uint32_t) * (256 * (size_t)ntiles * 9 + 8 * 256) + 8 * 256 * 8 + 64);
   uint32_t* offs = hist + (size_t)8 * 256 * ntiles;
   uint32_t* dbase = offs + (size_t)256 * ntiles;
   unsigned long long* dtot = reinterpret_cast<unsigned long long*>(dbase + 8 * 256);
-  k_digit_hist<<<ntiles, SORT_THREADS, 0, ctx->stream>>>(keys, n, ntiles, hist);
+  int* derr = reinterpret_cast<int*>(dtot + 8 * 256);
+  MLC_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), ctx->stream));
+  {
+    MLC_KSCOPE(ctx, "sort_digit_hist");
+    k_digit_hist<<<ntiles, SORT_THREADS, 0, ctx->stream>>>(keys, n, ntiles, hist);
+  }
   MLC_CHECK_LAUNCH();
-  k_digit_totals<<<8 * 256, 256, 0, ctx->stream>>>(hist, ntiles, dtot);
+  {
+    MLC_KSCOPE(ctx, "sort_digit_totals");
+    k_digit_totals<<<8 * 256, 256, 0, ctx->stream>>>(hist, ntiles, dtot);
+  }
   MLC_CHECK_LAUNCH();
   // Digit totals to the host: digit bases, and positions where all keys agree are skipped.
   std::vector<unsigned long long> h(8 * 256);
@@ -178,11 +208,24 @@ void radix_sort_u64_u32(mlc_ctx* ctx, long n, uint64_t* keys, uint32_t* vals) {
   uint32_t* va = vals;
   uint64_t* kb = k2;
   uint32_t* vb = v2;
+  bool first = true;
   for (int p = 0; p < 8; p++) {
     if (trivial[p]) continue;
-    k_scan_digit<<<256, 1024, 0, ctx->stream>>>(hist + (size_t)p * 256 * ntiles, ntiles, dbase + p * 256, offs);
+    if (!first) {  // per-tile counts of digit p in the current order
+      MLC_KSCOPE(ctx, "sort_tile_hist");
+      k_tile_hist<<<ntiles, SORT_THREADS, 0, ctx->stream>>>(ka, n, ntiles, 8 * p, hist + (size_t)p * 256 * ntiles);
+    }
     MLC_CHECK_LAUNCH();
-    k_scatter<<<ntiles, SORT_THREADS, 0, ctx->stream>>>(ka, va, kb, vb, n, ntiles, 8 * p, offs);
+    first = false;
+    {
+      MLC_KSCOPE(ctx, "sort_scan");
+      k_scan_digit<<<256, 1024, 0, ctx->stream>>>(hist + (size_t)p * 256 * ntiles, ntiles, dbase + p * 256, offs);
+    }
+    MLC_CHECK_LAUNCH();
+    {
+      MLC_KSCOPE(ctx, "sort_scatter");
+      k_scatter<<<ntiles, SORT_THREADS, 0, ctx->stream>>>(ka, va, kb, vb, n, ntiles, 8 * p, offs, derr);
+    }
     MLC_CHECK_LAUNCH();
     std::swap(ka, kb);
     std::swap(va, vb);
@@ -191,6 +234,10 @@ void radix_sort_u64_u32(mlc_ctx* ctx, long n, uint64_t* keys, uint32_t* vals) {
     MLC_CUDA(cudaMemcpyAsync(keys, ka, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     MLC_CUDA(cudaMemcpyAsync(vals, va, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, ctx->stream));
   }
+  int herr = 0;
+  MLC_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  MLC_REQUIRE(herr == 0, MLC_ERR_CUDA, "radix sort: scatter offset out of range (inconsistent digit counts)");
 }
 
 __global__ void k_f64_to_keys(double* __restrict__ v, long n) {
@@ -212,10 +259,16 @@ __global__ void k_keys_to_f64(double* __restrict__ v, long n) {
 void sort_f64_u32(mlc_ctx* ctx, long n, double* keys, uint32_t* vals) {
   if (n <= 1) return;
   const int grid = (int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 16);
-  k_f64_to_keys<<<grid, 256, 0, ctx->stream>>>(keys, n);
+  {
+    MLC_KSCOPE(ctx, "sort_keys_in");
+    k_f64_to_keys<<<grid, 256, 0, ctx->stream>>>(keys, n);
+  }
   MLC_CHECK_LAUNCH();
   radix_sort_u64_u32(ctx, n, reinterpret_cast<uint64_t*>(keys), vals);
-  k_keys_to_f64<<<grid, 256, 0, ctx->stream>>>(keys, n);
+  {
+    MLC_KSCOPE(ctx, "sort_keys_out");
+    k_keys_to_f64<<<grid, 256, 0, ctx->stream>>>(keys, n);
+  }
   MLC_CHECK_LAUNCH();
 }
 
@@ -258,7 +311,10 @@ void histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, 
   const size_t smem = sizeof(uint32_t) * nbins;
   set_max_smem((const void*)k_hist_f64, smem);
   const int grid = (int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 8);
-  k_hist_f64<<<grid, 256, smem, ctx->stream>>>(v, n, nbins, lo, (hi - lo) / nbins, logscale, counts_dev);
+  {
+    MLC_KSCOPE(ctx, "histogram");
+    k_hist_f64<<<grid, 256, smem, ctx->stream>>>(v, n, nbins, lo, (hi - lo) / nbins, logscale, counts_dev);
+  }
   MLC_CHECK_LAUNCH();
 }
 

@@ -141,6 +141,9 @@ def tracks(ntracks: int, Nmap: int, margin: float, seed: int, epochs=(20, 200), 
     phi = rng.random(ntracks) * 2 * np.pi
     v = v_range[0] + (v_range[1] - v_range[0]) * rng.random(ntracks)
     tmax = t[off[1:] - 1] if E else np.zeros(ntracks)
+    # keep every track inside [margin, Nmap - margin]: cap the speed where the span is too long
+    room = 0.9 * (Nmap - 2 * margin)
+    v = np.where(v * tmax > room, room / np.maximum(tmax, 1e-300), v)
     L = v * tmax
     lo = margin + np.maximum(0, -L * np.cos(phi))
     hi = Nmap - margin - np.maximum(0, L * np.cos(phi))
