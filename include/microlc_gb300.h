@@ -115,6 +115,7 @@ int mlc_profile_raster(const mlc_profile* p, double* out_host, long cap, int* N)
  * else on the host.  Nx and Ny must be even and factor into 2, 3 and 5. */
 int mlc_map_create(mlc_ctx* ctx, const void* data, int data_is_device, int data_dtype, int Nx, int Ny,
                    int precision, mlc_map** out);
+/* Frees the map's device memory (waits for the device); valid after its context was destroyed. */
 int mlc_map_destroy(mlc_map* map);
 /* Device pointer to the map's pixels (precision of the map). */
 int mlc_map_data(mlc_map* map, void** dev_ptr);

@@ -9,6 +9,7 @@ libmicrolc_gb300.so.  Errors raise :class:`MlcError` with the library's message.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -48,6 +49,7 @@ class Context:
         if st != 0:
             raise MlcError(st, "mlc_ctx_create failed (is this an sm_103 GPU?)")
         self.h = h
+        self._maps = weakref.WeakSet()
 
     def check(self, st: int):
         if st != 0:
@@ -81,6 +83,8 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
+            for m in list(getattr(self, "_maps", ())):
+                m.close()
             self.L.mlc_ctx_destroy(self.h)
             self.h = None
 
@@ -145,6 +149,7 @@ class Map:
         h = C.c_void_p()
         ctx.check(ctx.L.mlc_map_create(ctx.h, ptr, on_dev, dt, self.Nx, self.Ny, self.prec, C.byref(h)))
         self.h = h
+        ctx._maps.add(self)
         ctx.synchronize()
 
     @property

@@ -210,6 +210,7 @@ int mlc_map_create(mlc_ctx* ctx, const void* data, int data_is_device, int data_
   int st = guarded(ctx, [&] {
     plan_get(ctx, Nx, Ny, precision);  // validates the sizes
     m->ctx = ctx;
+    m->device = ctx->device;
     m->Nx = Nx;
     m->Ny = Ny;
     m->prec = precision;
@@ -253,8 +254,8 @@ int mlc_map_destroy(mlc_map* map) {
   if (!map) return MLC_ERR_ARG;
   int prev = -1;
   cudaGetDevice(&prev);
-  cudaSetDevice(map->ctx->device);
-  cudaStreamSynchronize(map->ctx->stream);
+  cudaSetDevice(map->device);
+  // cudaFree waits for the device; the context may already be gone
   if (map->data) cudaFree(map->data);
   if (map->spec) cudaFree(map->spec);
   if (prev >= 0) cudaSetDevice(prev);

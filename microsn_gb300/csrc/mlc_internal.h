@@ -69,6 +69,7 @@ struct mlc_ctx {
 
 struct mlc_map {
   mlc_ctx* ctx = nullptr;
+  int device = 0;  // kept here so that destroying a map never touches its context
   int Nx = 0, Ny = 0, prec = 0;
   void* data = nullptr;  // Ny x Nx real
   void* spec = nullptr;  // forward spectrum, digit-transposed row order
