@@ -53,14 +53,22 @@ def parse():
     ap.add_argument("--small", action="store_true", help="reduced sizes (debug only; not a bench number)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 form")
+    ap.add_argument("--n", type=int, default=None, help="map side (profiling cases only; not a bench number)")
+    ap.add_argument("--tracks", type=int, default=None, help="track count (profiling cases only)")
     return ap.parse_args()
 
 
-def workload_config(small=False):
-    n = 2000 if small else N_MAP
-    nt = 20000 if small else N_TRACKS
-    return dict(workload="batched profiles and tracks: 10000^2 FP32 map x 16 profiles, 10^6 tracks" if not small
-                else "debug-small", map=f"{n}x{n} ray-shot kappa*={KAPPA} gamma={GAMMA} width={WIDTH} R_E seed {MAP_SEED}",
+def sizes_for(args):
+    n = args.n or (2000 if args.small else N_MAP)
+    nt = args.tracks or (20000 if args.small else N_TRACKS)
+    return n, nt
+
+
+def workload_config(args):
+    n, nt = sizes_for(args)
+    full = (n, nt) == (N_MAP, N_TRACKS)
+    return dict(workload="batched profiles and tracks: 10000^2 FP32 map x 16 profiles, 10^6 tracks" if full
+                else f"profiling case {n}^2 x {nt} tracks (not the bench workload)", map=f"{n}x{n} ray-shot kappa*={KAPPA} gamma={GAMMA} width={WIDTH} R_E seed {MAP_SEED}",
                 profiles=f"{SHAPES} x rhalf {RHALF_PX} px", tracks=nt,
                 epochs=f"U{{{EPOCHS[0]}..{EPOCHS[1]}}} in {SEASONS} seasons", velocity_px_per_day=list(V_RANGE),
                 l2="inputs larger than L2: every map is 400 MB (FP32), L2 is 129 MB", n=n)
@@ -256,9 +264,9 @@ def run_reference(args):
     import torch
 
     from microsn_gb300 import synth
-    n = 2000 if args.small else N_MAP
+    n, nt = sizes_for(args)
     mp = synth.lognormal_map(n, seed=MAP_SEED)
-    host, _, E = make_tracks_torch(N_TRACKS if not args.small else 20000, n, TRACK_SEED, "cpu", torch.float64)
+    host, _, E = make_tracks_torch(nt, n, TRACK_SEED, "cpu", torch.float64)
     vals = []
     res = None
     for s in range(args.warmup + args.steps):
@@ -270,7 +278,7 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lognormal map; same tracks)",
-           "config": workload_config(args.small),
+           "config": workload_config(args),
            "cpu_baseline": {"kind": res["kind"], "cores": res["cores"], "sample": res["sample"], "value": value,
                             "unit": UNIT},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -300,8 +308,7 @@ def main():
     B.build()
     dev = f"cuda:{local}"
     torch.cuda.set_device(local)
-    n = 2000 if args.small else N_MAP
-    ntracks = 20000 if args.small else N_TRACKS
+    n, ntracks = sizes_for(args)
     ctx = mlc.Context(local)
     stream = torch.cuda.current_stream(local)
 
@@ -447,7 +454,7 @@ def main():
                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f32",
                "data": "synthetic: seeded inverse-ray-shot map, seeded tracks (no public dataset)",
-               "config": workload_config(args.small), "roofline": roof, "cpu_baseline": cpu,
+               "config": workload_config(args), "roofline": roof, "cpu_baseline": cpu,
                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
                        "ms_per_step": e2e_ms},
                "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
