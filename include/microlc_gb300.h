@@ -218,6 +218,21 @@ int mlc_sort_f64_u32(mlc_ctx* ctx, long n, double* keys, uint32_t* vals);
 int mlc_histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, double hi, int logscale,
                       uint64_t* counts_host);
 
+/* The histogram above without any device allocation.  No counterpart in the reference
+ * (its binning allocates with thrust on every call).  For callers that cannot allocate
+ * device memory -- inside a framework that owns the whole device pool, in plugins or
+ * callbacks that may only use memory they are given, or in call sequences later replayed
+ * from a captured stream.  The per-bin counters live in a fixed array compiled into the
+ * library (96 KB on every device that loads it, held until the process exits), so no
+ * cudaMalloc, cudaFree or allocating library routine is called.  nbins is limited to
+ * 12000; larger requests return MLC_ERR_LIMIT.  The first call on a device resolves the
+ * array's device address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  Every call clears the counters it uses, but all calls
+ * on a device share the one array: calls that overlap on the GPU (other streams, other
+ * contexts, other host threads) race and must be serialised by the caller. */
+int mlc_histogram_f64_noalloc(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, double hi, int logscale,
+                              uint64_t* counts_host);
+
 /* ======================================================================= host-side stages (C++, FP64) */
 
 /* setup_chi2_calculation (cpu_functions.cpp:80-144) with find_indices (:28-45), M = {MA, MB},

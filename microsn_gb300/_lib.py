@@ -68,6 +68,7 @@ SIGNATURES = {
                                  vp]),
     "mlc_sort_f64_u32": (i32, [vp, C.c_long, vp, vp]),
     "mlc_histogram_f64": (i32, [vp, C.c_long, vp, i32, f64, f64, i32, vp]),
+    "mlc_histogram_f64_noalloc": (i32, [vp, C.c_long, vp, i32, f64, f64, i32, vp]),
     "mlc_setup_chi2": (i32, [f64, f64, f64, f64, i32, vp, vp, vp, i32, vp, i32, P_i32, vp, vp, vp, vp, vp, vp,
                              P_f64]),
     "mlc_locations_grid": (i32, [i32, i32, i32, vp, vp]),

@@ -11,6 +11,9 @@
 // against n; a violation sets an error flag instead of writing.
 #include <cub/block/block_scan.cuh>
 
+#include <mutex>
+#include <unordered_map>
+
 #include "mlc_internal.h"
 
 namespace mlc {
@@ -319,3 +322,72 @@ void histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, 
 }
 
 }  // namespace mlc
+
+// ---------------------------------------------------------------- histogram without allocation
+//
+// For callers that must not allocate device memory: code running while another
+// framework owns the whole device memory pool, host callbacks and plugins that may only
+// use memory they were handed, or a sequence that is later replayed from a captured
+// stream.  The per-bin counters live in a fixed file-scope device array instead of the
+// context's workspace, so this entry point calls no cudaMalloc, cudaFree or allocating
+// library routine.  The array is loaded with the library and stays allocated on every
+// device that loads it until the process exits.
+namespace mlc {
+namespace {
+
+constexpr int kNoAllocMaxBins = 12000;  // 96 KB of uint64 counters per device
+static __device__ __align__(256) unsigned long long g_noalloc_hist[kNoAllocMaxBins];
+
+std::mutex g_noalloc_mu;
+std::unordered_map<int, void*> g_noalloc_addr;  // device ordinal -> device address of the array
+
+// Device address of the array on the current device, resolved once per device.  In host
+// code the symbol is only a host-side stand-in, never a device address.
+void* noalloc_counters(int device) {
+  std::lock_guard<std::mutex> g(g_noalloc_mu);
+  auto it = g_noalloc_addr.find(device);
+  if (it != g_noalloc_addr.end()) return it->second;
+  void* p = nullptr;
+  MLC_CUDA(cudaGetSymbolAddress(&p, g_noalloc_hist));
+  g_noalloc_addr[device] = p;
+  return p;
+}
+
+}  // namespace
+}  // namespace mlc
+
+extern "C" int mlc_histogram_f64_noalloc(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, double hi,
+                                         int logscale, uint64_t* counts_host) {
+  using namespace mlc;
+  if (!ctx) return MLC_ERR_ARG;
+  if ((n > 0 && !v) || !counts_host || n < 0 || !(hi > lo)) {
+    ctx->err = "mlc_histogram_f64_noalloc: null pointer, negative n or hi <= lo";
+    return MLC_ERR_ARG;
+  }
+  if (nbins < 1 || nbins > kNoAllocMaxBins) {
+    ctx->err = "mlc_histogram_f64_noalloc: nbins must be in [1, 12000] (fixed counter array)";
+    return MLC_ERR_LIMIT;
+  }
+  try {
+    DeviceGuard g(ctx->device);
+    unsigned long long* counts = (unsigned long long*)noalloc_counters(ctx->device);
+    // the array keeps the previous call's counts: clear the bins this call uses
+    MLC_CUDA(cudaMemsetAsync(counts, 0, sizeof(unsigned long long) * nbins, ctx->stream));
+    if (n > 0) {
+      const size_t smem = sizeof(uint32_t) * nbins;
+      set_max_smem((const void*)k_hist_f64, smem);
+      const int grid = (int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 8);
+      {
+        MLC_KSCOPE(ctx, "histogram_noalloc");
+        k_hist_f64<<<grid, 256, smem, ctx->stream>>>(v, n, nbins, lo, (hi - lo) / nbins, logscale, counts);
+      }
+      MLC_CHECK_LAUNCH();
+    }
+    MLC_CUDA(cudaMemcpyAsync(counts_host, counts, sizeof(uint64_t) * nbins, cudaMemcpyDeviceToHost, ctx->stream));
+    MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+    return MLC_OK;
+  } catch (const Error& e) {
+    ctx->err = e.what();
+    return e.code;
+  }
+}
