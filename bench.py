@@ -193,7 +193,9 @@ def algorithmic_bytes(name, n, E, nprof, e=4):
         "fft_col_A": 2 * spec,                 # in-place column sub-pass: read + write
         "fft_col_B": 2 * spec,
         "conv_fused_spectrum": 2 * spec,       # read map spectrum, write product sub-pass output
-        "sample_tracks": E * e + (n // 1) * 0 + nprof * real + E * nprof * e,  # t in, one read of each map, LCs out
+        "sample_tracks": E * e + nprof * real + E * nprof * e,  # t in, one read of each map, LCs out
+        "sample_tracks_il": E * e + nprof * real + E * nprof * e,
+        "interleave": 2 * nprof * real,          # read nprof planar maps, write the interleaved map
     }
     return table.get(name)
 
@@ -319,14 +321,16 @@ def main():
     host_tr, tr, E = make_tracks_torch(ntracks, n, TRACK_SEED + rank, dev, torch.float32)
     profs = profiles_for(n)
     convs = [torch.empty((n, n), dtype=torch.float32, device=dev) for _ in profs]
+    imap = torch.empty((n, n, 16), dtype=torch.float32, device=dev)
     out = torch.empty((len(profs), E), dtype=torch.float32, device=dev)
 
     def step():
         m.refresh()
         for k, p in enumerate(profs):
             mlc.convolve(ctx, m, p, "fused", out=convs[k])
-        mlc.sample_tracks(ctx, convs, n, n, tr["x0"], tr["y0"], tr["phi"], tr["v"], tr["off"], tr["t"], mag=True,
-                          out=out)
+        mlc.interleave_maps(ctx, convs, n, n, 16, out=imap)
+        mlc.sample_tracks_interleaved(ctx, imap, len(profs), tr["x0"], tr["y0"], tr["phi"], tr["v"], tr["off"],
+                                      tr["t"], mag=True, out=out)
 
     for _ in range(max(args.warmup, 1)):
         step()

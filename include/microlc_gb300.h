@@ -162,6 +162,18 @@ int mlc_sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int
                       int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
                       const int64_t* off, const void* t, int mag, void* out);
 
+/* Interleave nmaps (<= 16) maps of Ny x Nx pixels pixel by pixel: out[(y*Nx+x)*stride + q]
+ * (stride a power of two >= nmaps, slots q >= nmaps zeroed).  The layout the interleaved
+ * sampler reads: one contiguous 4*stride-byte (FP32) read per bilinear corner. */
+int mlc_interleave_maps(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny, int precision,
+                        int stride, void* out);
+
+/* mlc_sample_tracks on an interleaved map (mlc_interleave_maps): same tracks, same
+ * arithmetic and output layout out[q*E + e] for q < nmaps. */
+int mlc_sample_tracks_interleaved(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny,
+                                  int precision, int ntracks, const void* x0, const void* y0, const void* phi,
+                                  const void* v, const int64_t* off, const void* t, int mag, void* out);
+
 /* ======================================================================= chi2 vs one observed curve */
 
 /* Offset-minimised chi2 of ncurves magnitude curves of T epochs (m, row-major, the

@@ -6,14 +6,14 @@ pairwise, sort and binning), as hand-written sm_103a CUDA kernels behind the C A
 include/microlc_gb300.h.  This package is the Python host mirror of that ABI.
 """
 from .api import (Chi2Vars, Context, Map, bin_chi2, bin_edges, calculate_chi2, chi2_offset, convolve,
-                  expanding_source, histogram_f64, locations_grid, locations_random, pair_bin_fused, profile,
-                  profile_raster, read_gerlumph, sample_tracks, setup_chi2_calculation, setup_integral,
+                  expanding_source, histogram_f64, interleave_maps, locations_grid, locations_random, pair_bin_fused, profile,
+                  profile_raster, read_gerlumph, sample_tracks, sample_tracks_interleaved, setup_chi2_calculation, setup_integral,
                   sort_f64_u32, trapezium)
 from ._lib import MlcError
 
 __all__ = [
     "Chi2Vars", "Context", "Map", "MlcError", "bin_chi2", "bin_edges", "calculate_chi2", "chi2_offset", "convolve",
     "expanding_source", "histogram_f64", "locations_grid", "locations_random", "pair_bin_fused", "profile",
-    "profile_raster", "read_gerlumph", "sample_tracks", "setup_chi2_calculation", "setup_integral", "sort_f64_u32",
+    "profile_raster", "read_gerlumph", "sample_tracks", "sample_tracks_interleaved", "interleave_maps", "setup_chi2_calculation", "setup_integral", "sort_f64_u32",
     "trapezium",
 ]

@@ -61,6 +61,8 @@ SIGNATURES = {
     "mlc_sample_nearest": (i32, [vp, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
     "mlc_sample_tracks": (i32, [vp, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
     "mlc_chi2_offset": (i32, [vp, i32, i32, i32, vp, vp, vp, vp, vp]),
+    "mlc_interleave_maps": (i32, [vp, vp, i32, i32, i32, i32, i32, vp]),
+    "mlc_sample_tracks_interleaved": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
     "mlc_pair_setup": (i32, [vp, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
     "mlc_pair_chi2_ratio": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]),
     "mlc_bin_chi2": (i32, [vp, i32, vp, vp, vp, vp, vp]),

@@ -221,6 +221,29 @@ def sample_tracks(ctx: Context, maps, Nx: int, Ny: int, x0, y0, phi, v, off, t, 
     return out
 
 
+def interleave_maps(ctx: Context, maps, Nx: int, Ny: int, stride: int = 16, out: torch.Tensor | None = None):
+    """Pixel-interleaved copy of up to 16 maps: (Ny, Nx, stride)."""
+    dt = maps[0].dtype
+    arr = (C.c_void_p * len(maps))(*[C.c_void_p(mm.data_ptr()) for mm in maps])
+    if out is None:
+        out = torch.empty((Ny, Nx, stride), dtype=dt, device=maps[0].device)
+    ctx.check(ctx.L.mlc_interleave_maps(ctx.h, arr, len(maps), Nx, Ny, _PREC[dt], stride, _ptr(out)))
+    return out
+
+
+def sample_tracks_interleaved(ctx: Context, imap: torch.Tensor, nmaps: int, x0, y0, phi, v, off, t, mag=True,
+                              out: torch.Tensor | None = None):
+    Ny, Nx, stride = imap.shape
+    dt = x0.dtype
+    E = int(off[-1].item())
+    if out is None:
+        out = torch.empty((nmaps, E), dtype=dt, device=x0.device)
+    ctx.check(ctx.L.mlc_sample_tracks_interleaved(ctx.h, _ptr(imap), stride, nmaps, Nx, Ny, _PREC[dt], x0.numel(),
+                                                  _ptr(x0), _ptr(y0), _ptr(phi), _ptr(v), _ptr(off), _ptr(t),
+                                                  int(mag), _ptr(out)))
+    return out
+
+
 def chi2_offset(ctx: Context, m: torch.Tensor, obs, w):
     """Offset-minimised chi2 of each row of m against obs with weights w."""
     n, T = m.shape

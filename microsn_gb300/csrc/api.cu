@@ -11,6 +11,10 @@ namespace mlc {
 void sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny, int prec,
                    int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
                    const int64_t* off, const void* t, int mag, void* out, long E);
+void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out);
+void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
+                      const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
+                      const void* t, int mag, void* out, long E);
 void chi2_offset(mlc_ctx* ctx, int prec, int ncurves, int T_, const void* m, const double* obs_dev,
                  const double* w_dev, double W, double* chi2, double* dm);
 void pair_setup(mlc_ctx* ctx, int Nloc, int Nprof, const double* LCA, const double* LCB, int Nbins,
@@ -361,6 +365,36 @@ int mlc_sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int
       MLC_CUDA(cudaStreamSynchronize(ctx->stream));
     }
     sample_tracks(ctx, maps_host, nmaps, Nx, Ny, precision, ntracks, x0, y0, phi, v, off, t, mag, out, (long)E);
+  });
+}
+
+static bool pow2_le16(int s) { return s == 1 || s == 2 || s == 4 || s == 8 || s == 16; }
+
+int mlc_interleave_maps(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny, int precision,
+                        int stride, void* out) {
+  if (!ctx || !maps_host || !out) return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (nmaps < 1 || nmaps > 16 || !pow2_le16(stride) || stride < nmaps || Nx < 1 || Ny < 1 ||
+      (precision != MLC_F64 && precision != MLC_F32))
+    return fail(ctx, MLC_ERR_ARG, "need 1 <= nmaps <= stride, stride in {1,2,4,8,16}");
+  for (int i = 0; i < nmaps; i++)
+    if (!maps_host[i]) return fail(ctx, MLC_ERR_ARG, "null map pointer");
+  return guarded(ctx, [&] { interleave(ctx, maps_host, nmaps, (long)Nx * Ny, precision, stride, out); });
+}
+
+int mlc_sample_tracks_interleaved(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny,
+                                  int precision, int ntracks, const void* x0, const void* y0, const void* phi,
+                                  const void* v, const int64_t* off, const void* t, int mag, void* out) {
+  if (!ctx || !imap || !x0 || !y0 || !phi || !v || !off || !t || !out) return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (nmaps < 1 || !pow2_le16(stride) || stride < nmaps || Nx < 2 || Ny < 2 || ntracks < 0 ||
+      (precision != MLC_F64 && precision != MLC_F32))
+    return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  return guarded(ctx, [&] {
+    int64_t E = 0;
+    if (ntracks > 0) {
+      MLC_CUDA(cudaMemcpyAsync(&E, off + ntracks, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+      MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    sample_tracks_il(ctx, imap, stride, nmaps, Nx, Ny, precision, ntracks, x0, y0, phi, v, off, t, mag, out, (long)E);
   });
 }
 

@@ -28,10 +28,11 @@
 
 namespace mlc {
 
-RadixList factor_radices(int L) {
+RadixList factor_radices(int L, int tw_stride) {
   RadixList rl{};
   rl.n = 0;
-  if (L < 1) {
+  rl.L = L;
+  if (L < 1 || L > 65535) {
     rl.n = -1;
     return rl;
   }
@@ -55,6 +56,14 @@ RadixList factor_radices(int L) {
     rl.r[rl.n++] = 4;
   }
   for (int i = 0; i < n8; i++) rl.r[rl.n++] = 8;
+  int Ns = 1;
+  for (int p = 0; p < rl.n; p++) {
+    rl.Ns[p] = Ns;
+    // exact j / Ns = umulhi(j, magic) for j * Ns < 2^32 (here j < L <= 65535)
+    rl.magic[p] = Ns > 1 ? (uint32_t)((0x100000000ull + Ns - 1) / Ns) : 0u;
+    rl.twstep[p] = (L / (Ns * rl.r[p])) * tw_stride;
+    Ns *= rl.r[p];
+  }
   return rl;
 }
 
@@ -148,9 +157,9 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
   p->elem = prec == MLC_F64 ? sizeof(C2<double>) : sizeof(C2<float>);
   p->CW = prec == MLC_F64 ? 8 : 16;
   split_columns(Ny, p->N1, p->N2);
-  p->rlM = factor_radices(p->M);
-  p->rlN1 = factor_radices(p->N1);
-  p->rlN2 = factor_radices(p->N2);
+  p->rlM = factor_radices(p->M, 2);
+  p->rlN1 = factor_radices(p->N1, p->N2);
+  p->rlN2 = factor_radices(p->N2, p->N1);
   MLC_REQUIRE(p->rlM.n >= 0 && p->rlN1.n >= 0 && p->rlN2.n >= 0, MLC_ERR_ARG,
               "map sides must factor into 2, 3 and 5");
   size_t row_smem = 2 * (size_t)(p->M + 1) * p->elem;
@@ -211,7 +220,7 @@ __global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__
   const int row = blockIdx.x;
   for (int n = threadIdx.x; n < M; n += blockDim.x) a[n] = ld.pair(row, n);
   __syncthreads();
-  C2<T>* Z = fft_smem<T, false, 1>(a, b, M, rl, twx, 2);
+  C2<T>* Z = fft_smem<T, false, 1>(a, b, rl, twx);
   C2<T>* o = out + (long)row * pitch;
   for (int k = threadIdx.x; k <= M; k += blockDim.x) {
     C2<T> zk = Z[k == M ? 0 : k];
@@ -242,7 +251,7 @@ __global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, 
     b[k] = C2<T>{e.x - o.y, e.y + o.x};
   }
   __syncthreads();
-  C2<T>* z = fft_smem<T, true, 1>(b, a, M, rl, twx, 2);
+  C2<T>* z = fft_smem<T, true, 1>(b, a, rl, twx);
   C2<T>* dst = reinterpret_cast<C2<T>*>(out + (long)row * ldo);
   for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = z[n];
 }
@@ -266,7 +275,7 @@ __global__ void __launch_bounds__(256) k_colpass(C2<T>* __restrict__ buf, long p
     a[idx] = buf[(base + j * j_mul) * pitch + col0 + c];
   }
   __syncthreads();
-  C2<T>* r = fft_smem<T, INV, CW>(a, b, L, rl, twy, tw_stride);
+  C2<T>* r = fft_smem<T, INV, CW>(a, b, rl, twy);
   for (int idx = threadIdx.x; idx < L * CW; idx += blockDim.x) {
     int j = idx / CW, c = idx % CW;
     C2<T> v = r[idx];
@@ -287,32 +296,30 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
   extern __shared__ unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + N2 * CW;
+  C2<T>* w1 = b + N2 * CW;  // W_N1^(n1 k1) for n1 < N1, this CTA's k1
   const int k1 = blockIdx.y;
   const long col0 = (long)blockIdx.x * CW;
+  for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * k1) % N1) * N2);
+  __syncthreads();
   // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 k1)
+  const int lo = Ny - h;  // first non-zero high row
   for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
-    const int n2 = idx / CW, c = idx % CW;
+    const int n2 = idx / CW, c = idx & (CW - 1);
     C2<T> acc{(T)0, (T)0};
-    for (int n1 = 0; (long)n1 * N2 + n2 < h; n1++) {
+    for (int n1 = 0; n1 * N2 + n2 < h; n1++) {
       const long j = (long)n1 * N2 + n2;
-      C2<T> kv = Kx[j * pitch + col0 + c];
-      C2<T> w = ldc(twy + (long)((n1 * (long)k1) % N1) * N2);
-      acc = cadd(acc, cmul(kv, w));
+      acc = cadd(acc, cmul(Kx[j * pitch + col0 + c], w1[n1]));
     }
-    const long lo = (long)Ny - h;  // first non-zero high row
-    int n1s = (int)((lo - n2 + N2 - 1) / N2);
+    int n1s = (lo - n2 + N2 - 1) / N2;
     if (n1s < 0) n1s = 0;
     for (int n1 = n1s; n1 < N1; n1++) {
-      const long n = (long)n1 * N2 + n2;
-      const long j = n - (Ny - 2L * h);
-      C2<T> kv = Kx[j * pitch + col0 + c];
-      C2<T> w = ldc(twy + (long)((n1 * (long)k1) % N1) * N2);
-      acc = cadd(acc, cmul(kv, w));
+      const long j = (long)n1 * N2 + n2 - (Ny - 2L * h);
+      acc = cadd(acc, cmul(Kx[j * pitch + col0 + c], w1[n1]));
     }
-    a[idx] = cmul(acc, ldc(twy + (long)n2 * k1));
+    a[idx] = cmul(acc, ldc(twy + n2 * k1));
   }
   __syncthreads();
-  C2<T>* K = fft_smem<T, false, CW>(a, b, N2, rl2, twy, N1);
+  C2<T>* K = fft_smem<T, false, CW>(a, b, rl2, twy);
   C2<T>* other = (K == a) ? b : a;
   for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
     const int k2 = idx / CW, c = idx % CW;
@@ -320,7 +327,7 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
     K[idx] = cscale(cmul(f, K[idx]), scale);
   }
   __syncthreads();
-  C2<T>* U = fft_smem<T, true, CW>(K, other, N2, rl2, twy, N1);
+  C2<T>* U = fft_smem<T, true, CW>(K, other, rl2, twy);
   for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
     const int n2 = idx / CW, c = idx % CW;
     C2<T> v = cmulc(U[idx], ldc(twy + (long)n2 * k1));
@@ -434,7 +441,7 @@ static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
   void* tmp = ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
   launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
   const int nstrips = ceil_div(p.Wc, CW);
-  size_t smem = 2 * (size_t)p.N2 * CW * sizeof(C2<T>);
+  size_t smem = (2 * (size_t)p.N2 * CW + p.N1) * sizeof(C2<T>);
   auto kern = k_conv_fused<T, CW>;
   set_max_smem((const void*)kern, smem);
   dim3 grid(nstrips, p.N1);

@@ -7,13 +7,21 @@
 
 namespace mlc {
 
+// Stage plan of one batched transform length: radix, sub-transform size Ns before the
+// stage, the 32-bit multiplier that divides by Ns (j / Ns = umulhi(j, magic) for the
+// j < 2^16 used here; Ns == 1 is special-cased), and the twiddle-table step.
 struct RadixList {
   int n;
-  int r[24];
+  int L;
+  int r[20];
+  int Ns[20];
+  uint32_t magic[20];
+  int twstep[20];
 };
 
-// Radix list for length L (2^a 3^b 5^c), or n = -1 when L has another factor.
-RadixList factor_radices(int L);
+// Radix plan for length L (2^a 3^b 5^c) whose twiddles come from a table of
+// L*tw_stride entries, or n = -1 when L has another factor.
+RadixList factor_radices(int L, int tw_stride);
 
 // ---------------------------------------------------------------- small DFTs
 
@@ -108,26 +116,33 @@ struct Dft<T, 8, INV> {
 // table exp(-2 pi i m / (L*tw_stride)) in global memory.
 template <typename T, int R, bool INV, int CW>
 __device__ __forceinline__ void stockham_stage(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int L,
-                                               int Ns, const C2<T>* __restrict__ tw, int tw_stride) {
+                                               int Ns, uint32_t magic, int twstep, const C2<T>* __restrict__ tw) {
   const int Lr = L / R;
   const int nb = Lr * CW;
-  const int twstep = (L / (Ns * R)) * tw_stride;
   for (int bt = threadIdx.x; bt < nb; bt += blockDim.x) {
-    const int c = bt % CW;
-    const int j = bt / CW;
-    const int k = j % Ns;
+    const int c = bt & (CW - 1);
+    const int j = bt / CW;  // CW is a power of two
+    int q, k;
+    if (Ns == 1) {
+      q = j;
+      k = 0;
+    } else {
+      q = (int)__umulhi((uint32_t)j, magic);
+      k = j - q * Ns;
+    }
     C2<T> v[R];
 #pragma unroll
     for (int i = 0; i < R; i++) v[i] = src[(j + i * Lr) * CW + c];
     if (Ns > 1) {
+      const int kt = k * twstep;
 #pragma unroll
       for (int i = 1; i < R; i++) {
-        C2<T> w = ldc(tw + (long)i * k * twstep);
+        C2<T> w = ldc(tw + i * kt);
         v[i] = INV ? cmulc(v[i], w) : cmul(v[i], w);
       }
     }
     Dft<T, R, INV>::run(v);
-    const int d = (j - k) * R + k;
+    const int d = q * Ns * R + k;
 #pragma unroll
     for (int i = 0; i < R; i++) dst[(d + i * Ns) * CW + c] = v[i];
   }
@@ -136,23 +151,23 @@ __device__ __forceinline__ void stockham_stage(const C2<T>* __restrict__ src, C2
 // Batched length-L transform of the CW columns held in a ([L][CW]); b is scratch of the
 // same size.  Returns the buffer that holds the natural-order result.  Ends synchronised.
 template <typename T, bool INV, int CW>
-__device__ C2<T>* fft_smem(C2<T>* a, C2<T>* b, int L, const RadixList& rl, const C2<T>* __restrict__ tw,
-                           int tw_stride) {
-  int Ns = 1;
+__device__ C2<T>* fft_smem(C2<T>* a, C2<T>* b, const RadixList& rl, const C2<T>* __restrict__ tw) {
+  const int L = rl.L;
   for (int p = 0; p < rl.n; ++p) {
-    const int r = rl.r[p];
-    switch (r) {
-      case 2: stockham_stage<T, 2, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
-      case 3: stockham_stage<T, 3, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
-      case 4: stockham_stage<T, 4, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
-      case 5: stockham_stage<T, 5, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
-      default: stockham_stage<T, 8, INV, CW>(a, b, L, Ns, tw, tw_stride); break;
+    const int Ns = rl.Ns[p];
+    const uint32_t mg = rl.magic[p];
+    const int ts = rl.twstep[p];
+    switch (rl.r[p]) {
+      case 2: stockham_stage<T, 2, INV, CW>(a, b, L, Ns, mg, ts, tw); break;
+      case 3: stockham_stage<T, 3, INV, CW>(a, b, L, Ns, mg, ts, tw); break;
+      case 4: stockham_stage<T, 4, INV, CW>(a, b, L, Ns, mg, ts, tw); break;
+      case 5: stockham_stage<T, 5, INV, CW>(a, b, L, Ns, mg, ts, tw); break;
+      default: stockham_stage<T, 8, INV, CW>(a, b, L, Ns, mg, ts, tw); break;
     }
     __syncthreads();
     C2<T>* t = a;
     a = b;
     b = t;
-    Ns *= r;
   }
   return a;
 }

@@ -153,6 +153,157 @@ void sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx
     sample_tracks_impl<float>(ctx, maps_host, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E);
 }
 
+// ---------------------------------------------------------------- profile-interleaved maps
+//
+// With nm maps of one source sampled at the same positions, a planar layout costs every
+// bilinear corner one random 8-byte read per map, which HBM serves as a 64-byte granule.
+// Interleaving the maps pixel by pixel ([y][x][stride], stride >= nm, a power of two)
+// makes a corner one contiguous 4*stride-byte read for all maps at once.
+
+// out[p*stride + q] = maps[q][p] (q < nm), 0 for nm <= q < stride.  A CTA moves a tile of
+// 256 pixels: coalesced loads of each map's 256 values into shared memory, then the tile's
+// 256*stride contiguous outputs are written with consecutive threads on consecutive words.
+template <typename T>
+__global__ void __launch_bounds__(256) k_interleave(MapList<T> maps, int nm, int stride, long npix,
+                                                   T* __restrict__ out) {
+  __shared__ T tile[16][257];
+  const long ntiles = (npix + 255) / 256;
+  for (long tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const long p0 = tb * 256;
+    const int np = (int)min(256L, npix - p0);
+    for (int q = 0; q < stride; q++) {
+      const long p = p0 + threadIdx.x;
+      tile[q][threadIdx.x] = (q < nm && threadIdx.x < np) ? __ldg(maps.m[q] + p) : (T)0;
+    }
+    __syncthreads();
+    T* o = out + p0 * stride;
+    const int nout = np * stride;
+    for (int i = threadIdx.x; i < nout; i += blockDim.x) {
+      const int px = i / stride, q = i - px * stride;
+      o[i] = tile[q][px];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int NM>
+struct Pix {
+  T v[NM];
+};
+
+template <typename T, int NM>
+__device__ __forceinline__ void load_pix(const T* __restrict__ p, T* v) {
+  if constexpr (sizeof(T) * NM % 16 == 0) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+    float4* d = reinterpret_cast<float4*>(v);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) * NM / 16); i++) d[i] = __ldg(q + i);
+  } else {
+#pragma unroll
+    for (int i = 0; i < NM; i++) v[i] = __ldg(p + i);
+  }
+}
+
+// One warp per track, lanes over epochs; each epoch reads 4 corners x NM interleaved
+// values and writes nm_out light-curve values out[q*E + e].
+template <typename T, int NM>
+__global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ imap, int Nx, int Ny, int ntracks,
+                                                          const T* __restrict__ x0, const T* __restrict__ y0,
+                                                          const T* __restrict__ phi, const T* __restrict__ v,
+                                                          const int64_t* __restrict__ off, const T* __restrict__ t,
+                                                          int mag, T* __restrict__ out, long E, int nm_out) {
+  const int lane = threadIdx.x & 31;
+  const long track = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (track >= ntracks) return;
+  const T X0 = x0[track], Y0 = y0[track], V = v[track];
+  T sn, cs;
+  if (sizeof(T) == 8) {
+    double s_, c_;
+    sincos((double)phi[track], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  } else {
+    float s_, c_;
+    sincosf((float)phi[track], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  }
+  const long bx = (long)floor(X0), by = (long)floor(Y0);
+  const T fx0 = X0 - (T)bx, fy0 = Y0 - (T)by;
+  const int64_t e0 = off[track], e1 = off[track + 1];
+  for (int64_t e = e0 + lane; e < e1; e += 32) {
+    const T vt = V * t[e];
+    const T fx = fx0 + vt * cs, fy = fy0 + vt * sn;
+    const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
+    T acc[NM];
+    if (B.inside) {
+      T a[NM], b[NM], c[NM], d[NM];
+      load_pix<T, NM>(imap + ((long)B.iu * Nx + B.jl) * NM, a);
+      load_pix<T, NM>(imap + ((long)B.iu * Nx + B.jr) * NM, b);
+      load_pix<T, NM>(imap + ((long)B.il * Nx + B.jl) * NM, c);
+      load_pix<T, NM>(imap + ((long)B.il * Nx + B.jr) * NM, d);
+#pragma unroll
+      for (int q = 0; q < NM; q++) {
+        T z = B.w0 * a[q];
+        z += B.w1 * b[q];
+        z += B.w2 * c[q];
+        z += B.w3 * d[q];
+        acc[q] = z;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < NM; q++) acc[q] = (T)0;
+    }
+#pragma unroll
+    for (int q = 0; q < NM; q++)
+      if (q < nm_out) out[(long)q * E + e] = mag ? (T)-2.5 * mlc_log10(acc[q]) : acc[q];
+  }
+}
+
+void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out) {
+  const int grid = (int)std::min<long>((npix + 255) / 256, (long)ctx->sm_count * 16);
+  if (prec == MLC_F64) {
+    MapList<double> ml{};
+    for (int q = 0; q < nmaps; q++) ml.m[q] = (const double*)maps_host[q];
+    MLC_KSCOPE(ctx, "interleave");
+    k_interleave<double><<<grid, 256, 0, ctx->stream>>>(ml, nmaps, stride, npix, (double*)out);
+  } else {
+    MapList<float> ml{};
+    for (int q = 0; q < nmaps; q++) ml.m[q] = (const float*)maps_host[q];
+    MLC_KSCOPE(ctx, "interleave");
+    k_interleave<float><<<grid, 256, 0, ctx->stream>>>(ml, nmaps, stride, npix, (float*)out);
+  }
+  MLC_CHECK_LAUNCH();
+}
+
+template <typename T>
+static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int ntracks,
+                           const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
+                           const void* t, int mag, void* out, long E) {
+  const int grid = ceil_div(ntracks, 8);
+#define MLC_IL_LAUNCH(NMV)                                                                                    k_sample_tracks_il<T, NMV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, Nx, Ny, ntracks, (const T*)x0,                                                              (const T*)y0, (const T*)phi, (const T*)v, off,                                                              (const T*)t, mag, (T*)out, E, nmaps)
+  MLC_KSCOPE(ctx, "sample_tracks_il");
+  switch (stride) {
+    case 1: MLC_IL_LAUNCH(1); break;
+    case 2: MLC_IL_LAUNCH(2); break;
+    case 4: MLC_IL_LAUNCH(4); break;
+    case 8: MLC_IL_LAUNCH(8); break;
+    default: MLC_IL_LAUNCH(16); break;
+  }
+#undef MLC_IL_LAUNCH
+}
+
+void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
+                      const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
+                      const void* t, int mag, void* out, long E) {
+  if (ntracks <= 0) return;
+  if (prec == MLC_F64)
+    sample_il_impl<double>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E);
+  else
+    sample_il_impl<float>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E);
+  MLC_CHECK_LAUNCH();
+}
+
 // Offset-minimised chi2, one warp per curve, FP64 accumulation:
 // dm = sum w (o - m) / W ; chi2 = sum w (o - m - dm)^2 (two passes, no cancellation).
 template <typename T>

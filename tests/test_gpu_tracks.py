@@ -73,3 +73,22 @@ def test_chi2_offset(ctx, prec):
     ref, dmr = oracle.chi2_offset(mt.double().cpu().numpy(), o, w)
     np.testing.assert_allclose(chi2.cpu().numpy(), ref, rtol=1e-12)
     np.testing.assert_allclose(dm.cpu().numpy(), dmr, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.parametrize("dtype,nm,stride", [(np.float32, 16, 16), (np.float64, 3, 4), (np.float32, 5, 8),
+                                            (np.float32, 1, 1)])
+def test_interleaved_sampling_equals_planar(ctx, dtype, nm, stride):
+    import microsn_gb300 as mlc
+    N = 300
+    tdt = torch.float32 if dtype == np.float32 else torch.float64
+    maps = [torch.as_tensor(synth.lognormal_map(N, seed=20 + q), dtype=tdt, device="cuda:0") for q in range(nm)]
+    host, dev = _tracks(3000, N, 8, dtype)
+    il = mlc.interleave_maps(ctx, maps, N, N, stride)
+    ref_il = torch.zeros((N, N, stride), dtype=tdt, device="cuda:0")
+    for q in range(nm):
+        ref_il[:, :, q] = maps[q]
+    assert torch.equal(il, ref_il)
+    for mag in (True, False):
+        a = mlc.sample_tracks(ctx, maps, N, N, *dev, mag=mag)
+        b = mlc.sample_tracks_interleaved(ctx, il, nm, *dev, mag=mag)
+        assert torch.equal(a, b)
