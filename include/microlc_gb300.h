@@ -218,6 +218,41 @@ int mlc_pair_bin_fused(mlc_ctx* ctx, int Njp, const int* indA_host, const int* i
                        const double* LCB, const double* DLCB, int Nbins, const double* edges_host,
                        double* binned_chi2_host, double* binned_exp_host, uint32_t* nper_host);
 
+/* ======================================================================= pair stage (magnitude-difference form) */
+
+#define MLC_PAIR_PLAIN 0  /* FP64 on CUDA cores, one launch per stage (chi2 chunk, histogram, candidates) */
+#define MLC_PAIR_TENSOR 1 /* exact sliced-integer cross term on the tensor cores, fused epilogue */
+
+typedef struct {
+  double delta;        /* quantisation step of the centred, weighted curves (tensor form) */
+  double threshold;    /* top-k candidate threshold used */
+  long long refined;   /* near-identical pairs recomputed in FP64 (tensor form) */
+  long long candidates;
+  int passes;          /* passes over the pairs (1 unless the threshold had to move) */
+} mlc_pair_stats;
+
+/* Pairwise magnitude-difference chi2 between NA curves A and NB curves B (device FP32,
+ * row-major, T epochs shared by all curves):
+ *     chi2_ij = sum_t w_t (d_t - (A_it - B_jt) - c_ij)^2,
+ * c_ij = 0, or with offset != 0 the constant magnitude offset that minimises it.
+ * w_host: T weights (1/sigma^2); d_host: T observed difference (nullable = 0).  Outputs:
+ * hist_host (nbins uint64 counts of log10 chi2 in [lo_log10, hi_log10), nbins <= 4096),
+ * the k smallest chi2 with their (i, j) (ascending, ties by i*NB+j; k = 0 skips), and,
+ * when chi2_out is not NULL, the NA x NB FP32 chi2 matrix (device).  No reference
+ * counterpart: the reference's pair statistic is the flux ratio (kernel_chi2,
+ * gpu_functions.cu:700-750; chi2/chi2_functions.cuh:35-68); this is its magnitude form.
+ * MLC_PAIR_TENSOR needs T <= 128; its chi2 values are those of the curves quantised to
+ * 24 bits (relative error ~1e-6 against FP64). */
+int mlc_pair_chi2_magdiff(mlc_ctx* ctx, int method, int NA, int NB, int T, const float* A, const float* B,
+                          const double* w_host, const double* d_host, int offset, int nbins, double lo_log10,
+                          double hi_log10, uint64_t* hist_host, int k, double* topk_val_host, int64_t* topk_i_host,
+                          int64_t* topk_j_host, float* chi2_out, mlc_pair_stats* stats);
+
+/* FP64 chi2 of npairs listed pairs (ia, ib device int64), same statistic. */
+int mlc_pair_chi2_magdiff_list(mlc_ctx* ctx, int NA, int NB, int T, const float* A, const float* B,
+                               const double* w_host, const double* d_host, int offset, long npairs,
+                               const int64_t* ia, const int64_t* ib, double* chi2);
+
 /* ======================================================================= sort / histogram */
 
 /* Stable ascending sort of n FP64 keys (in place) carrying uint32 values (in place);

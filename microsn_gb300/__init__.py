@@ -9,6 +9,7 @@ from .api import (Chi2Vars, Context, Map, bin_chi2, bin_edges, calculate_chi2, c
                   expanding_source, histogram_f64, interleave_maps, locations_grid, locations_random, pair_bin_fused, profile,
                   profile_raster, read_gerlumph, sample_tracks, sample_tracks_interleaved, setup_chi2_calculation, setup_integral,
                   sort_f64_u32, trapezium)
+from .api import pair_chi2_magdiff, pair_chi2_magdiff_list  # noqa: F401
 from ._lib import MlcError
 
 __all__ = [

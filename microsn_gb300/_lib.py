@@ -24,6 +24,11 @@ class MlcProfile(C.Structure):
                 ("u", C.c_double)]
 
 
+class MlcPairStats(C.Structure):
+    _fields_ = [("delta", C.c_double), ("threshold", C.c_double), ("refined", C.c_longlong),
+                ("candidates", C.c_longlong), ("passes", C.c_int)]
+
+
 class MlcError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"mlc error {code}: {msg}")
@@ -70,6 +75,9 @@ SIGNATURES = {
                                  vp]),
     "mlc_sort_f64_u32": (i32, [vp, C.c_long, vp, vp]),
     "mlc_histogram_f64": (i32, [vp, C.c_long, vp, i32, f64, f64, i32, vp]),
+    "mlc_pair_chi2_magdiff": (i32, [vp, i32, i32, i32, i32, vp, vp, vp, vp, i32, i32, f64, f64, vp, i32, vp, vp, vp,
+                                    vp, vp]),
+    "mlc_pair_chi2_magdiff_list": (i32, [vp, i32, i32, i32, vp, vp, vp, vp, i32, C.c_long, vp, vp, vp]),
     "mlc_histogram_f64_noalloc": (i32, [vp, C.c_long, vp, i32, f64, f64, i32, vp]),
     "mlc_setup_chi2": (i32, [f64, f64, f64, f64, i32, vp, vp, vp, i32, vp, i32, P_i32, vp, vp, vp, vp, vp, vp,
                              P_f64]),

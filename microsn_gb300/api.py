@@ -335,6 +335,40 @@ def pair_bin_fused(ctx: Context, v: Chi2Vars, LCA, DLCA, LCB, DLCB, edges):
     return bc, be, nper
 
 
+def pair_chi2_magdiff(ctx: Context, A: torch.Tensor, B: torch.Tensor, w, d=None, offset: bool = False,
+                      method: str = "tensor", nbins: int = 1000, lo: float = -2.0, hi: float = 8.0, k: int = 0,
+                      want_matrix: bool = False):
+    """Magnitude-difference pair chi2: returns dict(hist, topk_val, topk_i, topk_j, matrix, stats)."""
+    from ._lib import MlcPairStats
+    NA, T = A.shape
+    NB = B.shape[0]
+    w = _np(w, np.float64)
+    dd = None if d is None else _np(d, np.float64)
+    hist = np.zeros(nbins, np.uint64)
+    tv = np.zeros(max(k, 1)); ti = np.zeros(max(k, 1), np.int64); tj = np.zeros(max(k, 1), np.int64)
+    mat = torch.empty((NA, NB), dtype=torch.float32, device=A.device) if want_matrix else None
+    st = MlcPairStats()
+    ctx.check(ctx.L.mlc_pair_chi2_magdiff(ctx.h, 1 if method == "tensor" else 0, NA, NB, T, _ptr(A.contiguous()),
+                                          _ptr(B.contiguous()), _ptr(w), _ptr(dd), int(offset), nbins, lo, hi,
+                                          _ptr(hist), k, _ptr(tv), _ptr(ti), _ptr(tj), _ptr(mat), C.byref(st)))
+    return dict(hist=hist, topk_val=tv[:k], topk_i=ti[:k], topk_j=tj[:k], matrix=mat,
+                stats=dict(delta=st.delta, threshold=st.threshold, refined=st.refined, candidates=st.candidates,
+                           passes=st.passes))
+
+
+def pair_chi2_magdiff_list(ctx: Context, A: torch.Tensor, B: torch.Tensor, w, ia, ib, d=None, offset=False):
+    NA, T = A.shape
+    NB = B.shape[0]
+    w = _np(w, np.float64)
+    dd = None if d is None else _np(d, np.float64)
+    ia = torch.as_tensor(np.asarray(ia, np.int64), device=A.device)
+    ib = torch.as_tensor(np.asarray(ib, np.int64), device=A.device)
+    out = torch.empty(ia.numel(), dtype=torch.float64, device=A.device)
+    ctx.check(ctx.L.mlc_pair_chi2_magdiff_list(ctx.h, NA, NB, T, _ptr(A.contiguous()), _ptr(B.contiguous()), _ptr(w),
+                                               _ptr(dd), int(offset), ia.numel(), _ptr(ia), _ptr(ib), _ptr(out)))
+    return out
+
+
 def sort_f64_u32(ctx: Context, keys: torch.Tensor, vals: torch.Tensor):
     """Stable in-place radix sort of FP64 keys with 32-bit values (int32 tensor)."""
     ctx.check(ctx.L.mlc_sort_f64_u32(ctx.h, keys.numel(), _ptr(keys), _ptr(vals)))

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "mlc_internal.h"
+#include "pairdiff.h"
 
 namespace mlc {
 void sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny, int prec,
@@ -29,6 +30,7 @@ void pair_bin_fused(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, con
                     const double* DLCA, const double* LCB, const double* DLCB, int Nbins, const double* edges_host,
                     double* bchi2_host, double* bexp_host, uint32_t* nper_host);
 void sort_f64_u32(mlc_ctx* ctx, long n, double* keys, uint32_t* vals);
+
 void histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, double hi, int logscale,
                    unsigned long long* counts_dev);
 
@@ -472,6 +474,48 @@ int mlc_pair_bin_fused(mlc_ctx* ctx, int Njp, const int* indA_host, const int* i
   return guarded(ctx, [&] {
     pair_bin_fused(ctx, Njp, indA_host, indB_host, facA_host, facB_host, d_host, s_host, Nloc, Nprof, LCA, DLCA,
                    LCB, DLCB, Nbins, edges_host, binned_chi2_host, binned_exp_host, nper_host);
+  });
+}
+
+int mlc_pair_chi2_magdiff(mlc_ctx* ctx, int method, int NA, int NB, int T, const float* A, const float* B,
+                          const double* w_host, const double* d_host, int offset, int nbins, double lo_log10,
+                          double hi_log10, uint64_t* hist_host, int k, double* topk_val_host, int64_t* topk_i_host,
+                          int64_t* topk_j_host, float* chi2_out, mlc_pair_stats* stats) {
+  if (!ctx || !A || !B || !w_host || (k > 0 && (!topk_val_host || !topk_i_host || !topk_j_host)))
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (method != MLC_PAIR_PLAIN && method != MLC_PAIR_TENSOR) return fail(ctx, MLC_ERR_ARG, "unknown method");
+  if (NA < 1 || NB < 1 || T < 1 || k < 0 || nbins < 1 || !(hi_log10 > lo_log10))
+    return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  if ((long long)NA * NB > (1LL << 40)) return fail(ctx, MLC_ERR_LIMIT, "more than 2^40 pairs");
+  return guarded(ctx, [&] {
+    PdResult r;
+    pairdiff_run(ctx, method, A, B, NA, NB, T, w_host, d_host, offset, nbins, lo_log10, hi_log10, hist_host, k,
+                 topk_val_host, topk_i_host, topk_j_host, chi2_out, r);
+    if (stats) {
+      stats->delta = r.delta;
+      stats->threshold = r.thr;
+      stats->refined = r.nrefined;
+      stats->candidates = r.ncand;
+      stats->passes = r.passes;
+    }
+  });
+}
+
+int mlc_pair_chi2_magdiff_list(mlc_ctx* ctx, int NA, int NB, int T, const float* A, const float* B,
+                               const double* w_host, const double* d_host, int offset, long npairs,
+                               const int64_t* ia, const int64_t* ib, double* chi2) {
+  if (!ctx || !A || !B || !w_host || !ia || !ib || !chi2) return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (NA < 1 || NB < 1 || T < 1 || npairs < 0) return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  return guarded(ctx, [&] {
+    double W = 0.0;
+    for (int t = 0; t < T; t++) W += w_host[t];
+    MLC_REQUIRE(W > 0, MLC_ERR_ARG, "weights sum to zero");
+    double* buf = (double*)ws_get(ctx, WS_SMALL, sizeof(double) * 2 * T);
+    MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+    MLC_CUDA(cudaMemcpy(buf, w_host, sizeof(double) * T, cudaMemcpyHostToDevice));
+    if (d_host) MLC_CUDA(cudaMemcpy(buf + T, d_host, sizeof(double) * T, cudaMemcpyHostToDevice));
+    pairdiff_plain(ctx, A, B, NA, NB, T, buf, d_host ? buf + T : nullptr, W, offset, npairs, (const long*)ia,
+                   (const long*)ib, chi2);
   });
 }
 

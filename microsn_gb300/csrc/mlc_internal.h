@@ -43,6 +43,7 @@ enum WsSlot {
   WS_PAIR_ACC,
   WS_SMALL,
   WS_LOC,
+  WS_PAIR_CAND,  // pair-stage candidates, refinement list, counters, histogram
   WS_NSLOTS
 };
 

@@ -1,0 +1,222 @@
+// Pairwise magnitude-difference chi2 between simulated curves of two lensed images.
+//
+//   chi2_ij = sum_t w_t (d_t - (a_it - b_jt) - c_ij)^2
+//
+// with c_ij = 0, or (offset form) the magnitude offset that minimises it,
+// c_ij = sum w (d - a + b) / sum w.  No counterpart in the reference, whose pair
+// statistic is the flux ratio (gpu_functions.cu:739-740, chi2/chi2_functions.cuh:59-64);
+// this is the separable form, chi2 = |Q_j - P_i|^2 with P_i = sqrt(w) (a_i - abar_i) and
+// Q_j = sqrt(w) (b_j + d - bbar_j) (bars: weighted means, only in the offset form).
+//
+// This file holds the plain FP64 form (one thread per pair, CUDA cores) and the
+// preparation used by the tensor-core form (pairtc.cu): per-curve centring and
+// weighting in FP64, one global quantisation step, 24-bit integers split into three
+// signed 8-bit slices stored as bf16 (exact), and the exact squared norms.
+#include <cmath>
+#include <vector>
+
+#include "mlc_internal.h"
+#include "pairdiff.h"
+
+namespace mlc {
+
+// ---------------------------------------------------------------- plain FP64 form
+
+// One thread per pair (i, j): FP64 two-pass form (offset first, then the sum of squares).
+__global__ void __launch_bounds__(256) k_pairdiff_plain(const float* __restrict__ A, const float* __restrict__ B,
+                                                        int NA, int NB, int T, const double* __restrict__ w,
+                                                        const double* __restrict__ d, double W, int offset,
+                                                        long npairs, const long* __restrict__ ia,
+                                                        const long* __restrict__ ib, double* __restrict__ chi2) {
+  const long n = ia ? npairs : (long)NA * NB;
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
+    const long i = ia ? ia[p] : p / NB, j = ia ? ib[p] : p % NB;
+    const float* a = A + i * T;
+    const float* b = B + j * T;
+    double c = 0.0;
+    if (offset) {
+      double sr = 0.0;
+      for (int t = 0; t < T; t++) sr += w[t] * ((d ? d[t] : 0.0) - ((double)a[t] - (double)b[t]));
+      c = sr / W;
+    }
+    double s = 0.0;
+    for (int t = 0; t < T; t++) {
+      const double r = (d ? d[t] : 0.0) - ((double)a[t] - (double)b[t]) - c;
+      s += w[t] * r * r;
+    }
+    chi2[p] = s;
+  }
+}
+
+void pairdiff_plain(mlc_ctx* ctx, const float* A, const float* B, int NA, int NB, int T, const double* w_dev,
+                    const double* d_dev, double W, int offset, long npairs, const long* ia, const long* ib,
+                    double* chi2) {
+  const long n = ia ? npairs : (long)NA * NB;
+  if (n <= 0) return;
+  const int grid = (int)std::max<long>(1, std::min<long>((n + 255) / 256, (long)ctx->sm_count * 32));
+  {
+    MLC_KSCOPE(ctx, "pairdiff_plain");
+    k_pairdiff_plain<<<grid, 256, 0, ctx->stream>>>(A, B, NA, NB, T, w_dev, d_dev, W, offset, npairs, ia, ib, chi2);
+  }
+  MLC_CHECK_LAUNCH();
+}
+
+// ---------------------------------------------------------------- preparation for the tensor-core form
+
+// Centred, weighted curves in FP64: out[r*T + t] = sqrt(w_t) (x_rt + sgn*d_t - mean_r).
+// side 0: x = a, no d; side 1: x = b, plus d.  Also the per-row max |.| (for the scale).
+__global__ void __launch_bounds__(256) k_pd_center(const float* __restrict__ X, int N, int T,
+                                                   const double* __restrict__ sw, const double* __restrict__ w,
+                                                   const double* __restrict__ d, double W, int offset,
+                                                   double* __restrict__ out, double* __restrict__ rowmax) {
+  const int lane = threadIdx.x & 31;
+  const long r = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= N) return;
+  const float* x = X + r * T;
+  double mean = 0.0;
+  if (offset) {
+    double s = 0.0;
+    for (int t = lane; t < T; t += 32) s += w[t] * ((double)x[t] + (d ? d[t] : 0.0));
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    mean = s / W;
+  }
+  double mx = 0.0;
+  for (int t = lane; t < T; t += 32) {
+    const double v = sw[t] * ((double)x[t] + (d ? d[t] : 0.0) - mean);
+    out[r * T + t] = v;
+    mx = fmax(mx, fabs(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) rowmax[r] = mx;
+}
+
+__global__ void k_pd_maxreduce(const double* __restrict__ v, long n, unsigned long long* __restrict__ out) {
+  double m = 0.0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    m = fmax(m, v[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));  // m >= 0
+}
+
+__device__ __forceinline__ uint16_t bf16_of_small_int(int v) {
+  // v in [-128, 127] is exact in bf16; build the bits from the float
+  const float f = (float)v;
+  return (uint16_t)(__float_as_uint(f) >> 16);
+}
+
+// Quantise to integers q = rint(v / delta) (|q| <= QMAX), split q = s0*65536 + s1*256 + s2
+// with balanced digits in [-128, 127], write the slices into the operand row
+// [slice 0 | slice 1 | slice 2] (Kp = padded T each, zeros beyond T), and the exact
+// squared norm sum q^2.  Rows beyond N (padding up to the tile) are zero.
+__global__ void __launch_bounds__(256) k_pd_quantize(const double* __restrict__ v, int N, int Npad, int T, int Kp,
+                                                     double inv_delta, uint16_t* __restrict__ ops,
+                                                     long long* __restrict__ norm2, int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const long r = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= Npad) return;
+  uint16_t* row = ops + r * (3L * Kp);
+  long long acc = 0;
+  for (int t = lane; t < Kp; t += 32) {
+    int q = 0;
+    if (r < N && t < T) {
+      const double x = rint(v[r * T + t] * inv_delta);
+      if (!(fabs(x) <= (double)PD_QMAX)) atomicExch(err, 1);
+      q = (int)fmax(fmin(x, (double)PD_QMAX), -(double)PD_QMAX);
+    }
+    int s2 = ((q % 256) + 256 + 128) % 256 - 128;  // balanced digit
+    int r1 = (q - s2) / 256;
+    int s1 = ((r1 % 256) + 256 + 128) % 256 - 128;
+    int s0 = (r1 - s1) / 256;
+    row[t] = bf16_of_small_int(s0);
+    row[Kp + t] = bf16_of_small_int(s1);
+    row[2 * Kp + t] = bf16_of_small_int(s2);
+    acc += (long long)q * q;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) norm2[r] = acc;
+}
+
+// Builds both operand sides.  Returns delta (the quantisation step).
+double pairdiff_prepare(mlc_ctx* ctx, const float* A, const float* B, int NA, int NB, int T, const double* w_host,
+                        const double* d_host, int offset, PdOperands& ops) {
+  MLC_REQUIRE(T >= 1 && T <= 4096, MLC_ERR_LIMIT, "T must be in [1, 4096]");
+  ops.T = T;
+  ops.Kp = (int)round_up(T, 64);
+  ops.NA = NA;
+  ops.NB = NB;
+  ops.NApad = (int)round_up(NA, PD_TILE_M);
+  ops.NBpad = (int)round_up(NB, PD_TILE_N);
+  std::vector<double> sw(T), w(w_host, w_host + T), d(T, 0.0);
+  double W = 0.0;
+  for (int t = 0; t < T; t++) {
+    MLC_REQUIRE(w[t] >= 0 && std::isfinite(w[t]), MLC_ERR_ARG, "weights must be finite and >= 0");
+    sw[t] = std::sqrt(w[t]);
+    W += w[t];
+    if (d_host) d[t] = d_host[t];
+  }
+  MLC_REQUIRE(W > 0, MLC_ERR_ARG, "weights sum to zero");
+  // small device tables: sw, w, d, then rowmax (NA+NB), then the global max
+  char* sm = (char*)ws_get(ctx, WS_SMALL, sizeof(double) * (3 * T + NA + NB) + 64);
+  double* dsw = (double*)sm;
+  double* dw = dsw + T;
+  double* dd = dw + T;
+  double* rowmax = dd + T;
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  MLC_CUDA(cudaMemcpy(dsw, sw.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
+  MLC_CUDA(cudaMemcpy(dw, w.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
+  MLC_CUDA(cudaMemcpy(dd, d.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
+  // centred, weighted curves (FP64), both sides
+  double* cen = (double*)ws_get(ctx, WS_KREAL, sizeof(double) * ((size_t)NA + NB) * T);
+  {
+    MLC_KSCOPE(ctx, "pd_center");
+    k_pd_center<<<ceil_div(NA, 8), 256, 0, ctx->stream>>>(A, NA, T, dsw, dw, nullptr, W, offset, cen, rowmax);
+  }
+  {
+    MLC_KSCOPE(ctx, "pd_center");
+    k_pd_center<<<ceil_div(NB, 8), 256, 0, ctx->stream>>>(B, NB, T, dsw, dw, d_host ? dd : nullptr, W, offset,
+                                                          cen + (size_t)NA * T, rowmax + NA);
+  }
+  MLC_CHECK_LAUNCH();
+  unsigned long long* gmax = (unsigned long long*)ws_get(ctx, WS_SORT_HIST, 64);
+  int* derr = (int*)(gmax + 1);
+  MLC_CUDA(cudaMemsetAsync(gmax, 0, 16, ctx->stream));
+  {
+    MLC_KSCOPE(ctx, "pd_maxreduce");
+    k_pd_maxreduce<<<std::max(1, std::min(ceil_div(NA + NB, 256), ctx->sm_count * 4)), 256, 0, ctx->stream>>>(
+        rowmax, (long)NA + NB, gmax);
+  }
+  MLC_CHECK_LAUNCH();
+  unsigned long long hm = 0;
+  MLC_CUDA(cudaMemcpyAsync(&hm, gmax, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  double mx;
+  memcpy(&mx, &hm, 8);
+  const double delta = mx > 0 ? mx / (double)PD_QMAX : 1.0;
+  ops.delta = delta;
+  // operands and norms
+  const size_t rowsA = ops.NApad, rowsB = ops.NBpad;
+  ops.a = (uint16_t*)ws_get(ctx, WS_PAIR_ACC, sizeof(uint16_t) * 3 * ops.Kp * (rowsA + rowsB) +
+                                                  sizeof(long long) * (rowsA + rowsB) + 256);
+  ops.b = ops.a + 3 * (size_t)ops.Kp * rowsA;
+  ops.alpha = (long long*)(ops.b + 3 * (size_t)ops.Kp * rowsB);
+  ops.alpha = (long long*)round_up((long)(uintptr_t)ops.alpha, 16);
+  ops.beta = ops.alpha + rowsA;
+  {
+    MLC_KSCOPE(ctx, "pd_quantize");
+    k_pd_quantize<<<ceil_div(ops.NApad, 8), 256, 0, ctx->stream>>>(cen, NA, ops.NApad, T, ops.Kp, 1.0 / delta, ops.a,
+                                                                   ops.alpha, derr);
+  }
+  {
+    MLC_KSCOPE(ctx, "pd_quantize");
+    k_pd_quantize<<<ceil_div(ops.NBpad, 8), 256, 0, ctx->stream>>>(cen + (size_t)NA * T, NB, ops.NBpad, T, ops.Kp,
+                                                                   1.0 / delta, ops.b, ops.beta, derr);
+  }
+  MLC_CHECK_LAUNCH();
+  int herr = 0;
+  MLC_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  MLC_REQUIRE(herr == 0, MLC_ERR_ARG, "non-finite curve values");
+  return delta;
+}
+
+}  // namespace mlc

@@ -1,0 +1,608 @@
+// Tensor-core form of the pairwise magnitude-difference chi2 (see pairdiff.cu for the
+// statistic).  chi2_ij = |Q_j - P_i|^2 = alpha_i + beta_j - 2 P_i.Q_j on quantised curves
+// P = delta p, Q = delta q (p, q integers, |p|,|q| <= 8355711) held as three signed 8-bit
+// slices p = 65536 s0 + 256 s1 + s2 in bf16.  A slice product summed over T <= 128 epochs
+// stays below 2^24, so every FP32 tensor-core accumulation is exact; the cross term is
+// accumulated per diagonal d = a + b of slice exponents (four TMEM accumulators d = 0..3,
+// eight slice pairs) and assembled in int64:
+//     x = 2^32 X0 + 2^24 X1 + 2^16 X2 + 2^8 X3   (X4 = s2.t2 is left out: |2 X4| <= 2^22 T)
+// chi2 (in delta^2 units) = alpha + beta - 2 x.  Pairs whose value is within 1e6 times the
+// left-out bound of zero are recomputed in FP64 by k_pd_refine, so every reported chi2 is
+// within 1e-6 relative of the exact chi2 of the quantised curves.
+//
+// Kernel layout (one persistent CTA per SM, 12 warps):
+//   warp 0      TMA producer: the work item's 128 A rows (3 slices x Kp, resident in shared
+//               memory) and, double-buffered, each 64-row B tile
+//   warp 1      MMA issuer (one thread): 8 slice pairs x Kp/16 tcgen05.mma per tile into one
+//               of two TMEM buffers (4 accumulators x 64 columns each, 512 columns total)
+//   warp 2      TMEM allocation / release
+//   warps 4-11  epilogue: TMEM -> registers, int64 assembly, log10-chi2 histogram in shared
+//               memory, top-k candidates below a threshold, refinement list, optional matrix
+// Every barrier wait is bounded; a timeout sets the error flag and all roles unwind.
+#include <cuda.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "pairdiff.h"
+#include "tc_ptx.cuh"
+
+namespace mlc {
+
+void radix_sort_u64_u32(mlc_ctx* ctx, long n, uint64_t* keys, uint32_t* vals);
+uint64_t f64_to_key(double d);
+
+namespace {
+
+constexpr int TM = PD_TILE_M, TN = PD_TILE_N;
+constexpr int NSTAGE = 2;
+constexpr int EPI_WARPS = 8;
+constexpr int NTHREADS = (4 + EPI_WARPS) * 32;
+constexpr int TMEM_COLS = 512;
+constexpr int MAX_KP = 128;
+constexpr int MAX_BINS = 4096;
+constexpr int A_BOX = TM * 128;  // bytes of one 64-element K box of A (128 rows x 128 B)
+constexpr int B_BOX = TN * 128;
+
+struct PdParams {
+  int NA, NB, nj, njc, jchunk, nitems, nkb;
+  const long long* alpha;
+  const long long* beta;
+  float delta2;
+  int nbins;
+  float lo, inv_width;
+  unsigned long long* hist;
+  float thr;
+  unsigned int cap;
+  unsigned int* ncand;
+  float* cval;
+  int* ci;
+  int* cj;
+  long long refine_int;
+  unsigned int rcap;
+  unsigned int* nref;
+  int* ri;
+  int* rj;
+  float* out;
+  int* err;
+};
+
+size_t smem_bytes(int nkb, int nbins) {
+  return 1024 + (size_t)3 * nkb * A_BOX + (size_t)NSTAGE * 3 * nkb * B_BOX + 16 * 8 + 16 + sizeof(uint32_t) * nbins;
+}
+
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" ::"r"(EPI_WARPS * 32) : "memory"); }
+
+__global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_constant__ CUtensorMap tmA,
+                                                             const __grid_constant__ CUtensorMap tmB, PdParams P) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int nkb = P.nkb;
+  unsigned char* A_s = sm;
+  unsigned char* B_s = A_s + 3 * nkb * A_BOX;
+  uint64_t* bars = (uint64_t*)(B_s + NSTAGE * 3 * nkb * B_BOX);
+  uint64_t* a_full = bars + 0;
+  uint64_t* a_empty = bars + 1;
+  uint64_t* b_full = bars + 2;   // [2]
+  uint64_t* b_empty = bars + 4;  // [2]
+  uint64_t* t_full = bars + 6;   // [2]
+  uint64_t* t_empty = bars + 8;  // [2]
+  uint32_t* tmem_slot = (uint32_t*)(bars + 16);
+  volatile int* abort_s = (volatile int*)(tmem_slot + 1);
+  uint32_t* hist_s = tmem_slot + 4;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(a_full, 1);
+    tc::mbar_init(a_empty, 1);
+    for (int s = 0; s < 2; s++) {
+      tc::mbar_init(b_full + s, 1);
+      tc::mbar_init(b_empty + s, 1);
+      tc::mbar_init(t_full + s, 1);
+      tc::mbar_init(t_empty + s, EPI_WARPS);
+    }
+    *abort_s = 0;
+    tc::fence_barrier_init();
+  }
+  for (int i = threadIdx.x; i < P.nbins; i += NTHREADS) hist_s[i] = 0;
+  if (warp == 2) tc::tmem_alloc(tmem_slot, TMEM_COLS);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  auto fail = [&]() {
+    *abort_s = 1;
+    atomicExch(P.err, 1);
+  };
+
+  if (warp == 0 && lane == 0) {
+    // ------------------------------------------------ TMA producer
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+    uint32_t cB = 0, n = 0;
+    for (int it = blockIdx.x; it < P.nitems && !*abort_s; it += gridDim.x, n++) {
+      const int itile = it / P.njc, jc = it % P.njc;
+      const int j0 = jc * P.jchunk, j1 = min(P.nj, j0 + P.jchunk);
+      if (!tc::mbar_wait(a_empty, (n & 1) ^ 1)) { fail(); break; }
+      tc::mbar_arrive_expect_tx(a_full, 3 * nkb * A_BOX);
+      for (int bx = 0; bx < 3 * nkb; bx++) tc::tma_load_2d(A_s + bx * A_BOX, &tmA, a_full, bx * 64, itile * TM);
+      for (int jt = j0; jt < j1; jt++, cB++) {
+        const uint32_t s = cB & 1, u = cB >> 1;
+        if (*abort_s || !tc::mbar_wait(b_empty + s, (u & 1) ^ 1)) { fail(); break; }
+        tc::mbar_arrive_expect_tx(b_full + s, 3 * nkb * B_BOX);
+        for (int bx = 0; bx < 3 * nkb; bx++)
+          tc::tma_load_2d(B_s + (s * 3 * nkb + bx) * B_BOX, &tmB, b_full + s, bx * 64, jt * TN);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ------------------------------------------------ MMA issuer
+    const uint32_t idesc = tc::idesc_bf16(TM, TN);
+    uint32_t cB = 0, ct = 0, n = 0;
+    const int ksteps = nkb * 4;  // 16-element K steps per slice
+    for (int it = blockIdx.x; it < P.nitems && !*abort_s; it += gridDim.x, n++) {
+      const int jc = it % P.njc;
+      const int j0 = jc * P.jchunk, j1 = min(P.nj, j0 + P.jchunk);
+      if (!tc::mbar_wait(a_full, n & 1)) { fail(); break; }
+      for (int jt = j0; jt < j1; jt++, cB++, ct++) {
+        const uint32_t s = cB & 1, u = cB >> 1, tb = ct & 1, tu = ct >> 1;
+        if (*abort_s || !tc::mbar_wait(b_full + s, u & 1) || !tc::mbar_wait(t_empty + tb, (tu & 1) ^ 1)) {
+          fail();
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t dbase = tmem + tb * 256;
+        uint32_t first = 0xF;
+        for (int a = 0; a < 3; a++)
+          for (int b = 0; b < 3; b++) {
+            const int d = a + b;
+            if (d > 3) continue;
+            for (int kk = 0; kk < ksteps; kk++) {
+              const int kb = kk >> 2, ko = (kk & 3) * 32;
+              const uint64_t ad = tc::desc_sw128(tc::smem_u32(A_s + (a * nkb + kb) * A_BOX) + ko);
+              const uint64_t bd = tc::desc_sw128(tc::smem_u32(B_s + (s * 3 * nkb + b * nkb + kb) * B_BOX) + ko);
+              tc::mma_bf16(dbase + d * 64, ad, bd, idesc, (first >> d) & 1 ? 0u : 1u);
+              first &= ~(1u << d);
+            }
+          }
+        tc::mma_commit(b_empty + s);
+        tc::mma_commit(t_full + tb);
+      }
+      tc::mma_commit(a_empty);
+    }
+  } else if (warp >= 4) {
+    // ------------------------------------------------ epilogue
+    const int q = warp & 3, h = (warp - 4) >> 2;
+    const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
+    // Every epilogue warp walks the same items and reaches the two named-barrier syncs per
+    // item the same number of times; after an abort it only skips the work.
+    uint32_t ct = 0;
+    for (int it = blockIdx.x; it < P.nitems; it += gridDim.x) {
+      const int itile = it / P.njc, jc = it % P.njc;
+      const int j0 = jc * P.jchunk, j1 = min(P.nj, j0 + P.jchunk);
+      const int i = itile * TM + 32 * q + lane;
+      const bool irow = i < P.NA;
+      const long long al = irow ? P.alpha[i] : 0;
+      for (int jt = j0; jt < j1; jt++, ct++) {
+        const uint32_t tb = ct & 1, tu = ct >> 1;
+        if (*abort_s) break;
+        if (!tc::mbar_wait(t_full + tb, tu & 1)) {
+          fail();
+          break;
+        }
+        tc::fence_after_sync();
+        for (int ch = 0; ch < 4; ch++) {
+          const int col0 = h * 32 + ch * 8;
+          uint32_t r0[8], r1[8], r2[8], r3[8];
+          const uint32_t ta = tmem + tb * 256 + lane_addr + col0;
+          tc::tmem_ld8(ta, r0);
+          tc::tmem_ld8(ta + 64, r1);
+          tc::tmem_ld8(ta + 128, r2);
+          tc::tmem_ld8(ta + 192, r3);
+          tc::tmem_wait_ld();
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            const int j = jt * TN + col0 + c;
+            if (!irow || j >= P.NB) continue;
+            const long long x = ((long long)__float2int_rn(__uint_as_float(r0[c])) << 32) +
+                                ((long long)__float2int_rn(__uint_as_float(r1[c])) << 24) +
+                                ((long long)__float2int_rn(__uint_as_float(r2[c])) << 16) +
+                                ((long long)__float2int_rn(__uint_as_float(r3[c])) << 8);
+            const long long c2 = al + __ldg(P.beta + j) - 2 * x;
+            if (c2 < P.refine_int) {
+              const unsigned k = atomicAdd(P.nref, 1u);
+              if (k < P.rcap) {
+                P.ri[k] = i;
+                P.rj[k] = j;
+              }
+              continue;
+            }
+            const float chi2 = (float)c2 * P.delta2;
+            if (P.out) P.out[(long)i * P.NB + j] = chi2;
+            const int bin = (int)floorf((__log2f(chi2) * 0.30102999566398120f - P.lo) * P.inv_width);
+            if (bin >= 0 && bin < P.nbins) atomicAdd(hist_s + bin, 1u);
+            if (chi2 < P.thr) {
+              const unsigned k = atomicAdd(P.ncand, 1u);
+              if (k < P.cap) {
+                P.cval[k] = chi2;
+                P.ci[k] = i;
+                P.cj[k] = j;
+              }
+            }
+          }
+        }
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(t_empty + tb);
+      }
+      // flush this item's histogram (per item, so the 32-bit shared counters cannot overflow)
+      epi_sync();
+      for (int b = threadIdx.x - 128; b < P.nbins; b += EPI_WARPS * 32) {
+        const uint32_t v = hist_s[b];
+        if (v) {
+          atomicAdd(P.hist + b, (unsigned long long)v);
+          hist_s[b] = 0;
+        }
+      }
+      epi_sync();
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 2) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// Exact FP64 chi2 of listed pairs from the centred, weighted curves (P = cen[i], Q = cen[NA + j]).
+__global__ void __launch_bounds__(256) k_pd_refine(const double* __restrict__ cen, int NA, int T, const int* __restrict__ ri,
+                                                   const int* __restrict__ rj, unsigned n, int nbins, double lo,
+                                                   double width, unsigned long long* __restrict__ hist, float thr,
+                                                   unsigned cap, unsigned* __restrict__ ncand, float* __restrict__ cval,
+                                                   int* __restrict__ ci, int* __restrict__ cj, float* __restrict__ out,
+                                                   int NB) {
+  for (unsigned p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int i = ri[p], j = rj[p];
+    const double* a = cen + (long)i * T;
+    const double* b = cen + ((long)NA + j) * T;
+    double s = 0.0;
+    for (int t = 0; t < T; t++) {
+      const double r = b[t] - a[t];
+      s += r * r;
+    }
+    const float chi2 = (float)s;
+    if (out) out[(long)i * NB + j] = chi2;
+    if (s > 0) {
+      const int bin = (int)floor((log10(s) - lo) / width);
+      if (bin >= 0 && bin < nbins) atomicAdd(hist + bin, 1ull);
+    }
+    if (chi2 < thr) {
+      const unsigned k = atomicAdd(ncand, 1u);
+      if (k < cap) {
+        cval[k] = chi2;
+        ci[k] = i;
+        cj[k] = j;
+      }
+    }
+  }
+}
+
+// chi2 of pseudo-random pairs (integer hash of the sample index) for the top-k threshold.
+__global__ void __launch_bounds__(256) k_pd_sample(const double* __restrict__ cen, int NA, int NB, int T, long S,
+                                                   uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < S; p += (long)gridDim.x * blockDim.x) {
+    uint64_t z = (uint64_t)p * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    const int i = (int)((z & 0xFFFFFFFFull) % (uint64_t)NA), j = (int)((z >> 32) % (uint64_t)NB);
+    const double* a = cen + (long)i * T;
+    const double* b = cen + ((long)NA + j) * T;
+    double s = 0.0;
+    for (int t = 0; t < T; t++) {
+      const double r = b[t] - a[t];
+      s += r * r;
+    }
+    uint64_t u = __double_as_longlong(s);  // s >= 0: the bit pattern orders like the value
+    keys[p] = u;
+    vals[p] = (uint32_t)p;
+  }
+}
+
+// Plain form, stage 2: log10 histogram and top-k candidates of a chunk of FP64 chi2 values
+// (pairs row0*NB + q).  Shared-memory counters, flushed once per CTA.
+__global__ void __launch_bounds__(256) k_pd_hist_cand(const double* __restrict__ chi2, long n, long p0, int NB,
+                                                      int nbins, double lo, double width,
+                                                      unsigned long long* __restrict__ hist, float thr, unsigned cap,
+                                                      unsigned* __restrict__ ncand, float* __restrict__ cval,
+                                                      int* __restrict__ ci, int* __restrict__ cj) {
+  extern __shared__ uint32_t hs[];
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x) hs[b] = 0;
+  __syncthreads();
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+    const double s = chi2[q];
+    if (s > 0) {
+      const int bin = (int)floor((log10(s) - lo) / width);
+      if (bin >= 0 && bin < nbins) atomicAdd(hs + bin, 1u);
+    }
+    if ((float)s < thr) {
+      const unsigned k = atomicAdd(ncand, 1u);
+      if (k < cap) {
+        cval[k] = (float)s;
+        ci[k] = (int)((p0 + q) / NB);
+        cj[k] = (int)((p0 + q) % NB);
+      }
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+    if (hs[b]) atomicAdd(hist + b, (unsigned long long)hs[b]);
+}
+
+__global__ void k_cand_keys(const float* __restrict__ cval, unsigned n, uint64_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    keys[q] = (uint64_t)__float_as_uint(cval[q]);  // chi2 >= 0: bits order like values
+    vals[q] = q;
+  }
+}
+
+__global__ void k_cand_gather(const uint32_t* __restrict__ order, unsigned m, const float* __restrict__ cval,
+                              const int* __restrict__ ci, const int* __restrict__ cj, float* __restrict__ ov,
+                              int* __restrict__ oi, int* __restrict__ oj) {
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x) {
+    const uint32_t s = order[q];
+    ov[q] = cval[s];
+    oi[q] = ci[s];
+    oj[q] = cj[s];
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    MLC_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    MLC_REQUIRE(q == cudaDriverEntryPointSuccess && p, MLC_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+CUtensorMap make_map(void* base, int rows, int kcols, int box_rows) {
+  CUtensorMap m;
+  std::memset(&m, 0, sizeof m);
+  cuuint64_t dims[2] = {(cuuint64_t)kcols, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kcols * 2};
+  cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  MLC_REQUIRE(r == CUDA_SUCCESS, MLC_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+  return m;
+}
+
+}  // namespace
+
+// Tensor-core pair chi2 with fused log10-chi2 histogram and top-k.
+void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int NA, int NB, int T,
+                  const double* w_host, const double* d_host, int offset, int nbins, double lo, double hi,
+                  uint64_t* hist_host, int k, double* tv, int64_t* ti, int64_t* tj, float* out, PdResult& res) {
+  MLC_REQUIRE(method == 1 || T <= 4096, MLC_ERR_LIMIT, "T <= 4096");
+  MLC_REQUIRE(method == 0 || (T >= 1 && T <= MAX_KP), MLC_ERR_LIMIT,
+              "tensor-core pair chi2 supports T <= 128 epochs");
+  MLC_REQUIRE(nbins >= 1 && nbins <= MAX_BINS && hi > lo, MLC_ERR_ARG, "histogram: 1..4096 bins, hi > lo");
+  MLC_REQUIRE(NA >= 1 && NB >= 1 && k >= 0, MLC_ERR_ARG, "bad sizes");
+  PdOperands ops;
+  const double delta = pairdiff_prepare(ctx, A, B, NA, NB, T, w_host, d_host, offset, ops);
+  res.delta = delta;
+  const int nkb = ops.Kp / 64;
+  const double* cen = (const double*)ctx->ws_ptr[WS_KREAL];
+  CUtensorMap tmA = make_map(ops.a, ops.NApad, 3 * ops.Kp, TM);
+  CUtensorMap tmB = make_map(ops.b, ops.NBpad, 3 * ops.Kp, TN);
+  const long long P = (long long)NA * NB;
+
+  // ---- top-k threshold from a sample of pairs
+  const unsigned cap = (unsigned)std::min<long long>(P, 8LL * k + (1LL << 20));
+  double thr = INFINITY;
+  if (k > 0 && P > (long long)cap) {
+    const long S = 1L << 22;
+    uint64_t* sk = (uint64_t*)ws_get(ctx, WS_LOC, (sizeof(uint64_t) + sizeof(uint32_t)) * S);
+    uint32_t* sv = (uint32_t*)(sk + S);
+    {
+      MLC_KSCOPE(ctx, "pd_sample");
+      k_pd_sample<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(cen, NA, NB, T, S, sk, sv);
+    }
+    MLC_CHECK_LAUNCH();
+    radix_sort_u64_u32(ctx, S, sk, sv);
+    const double expect = (double)k * (double)S / (double)P;
+    const long rank = std::min<long>(S - 1, (long)std::ceil(4.0 * expect) + 16);
+    uint64_t u = 0;
+    MLC_CUDA(cudaMemcpy(&u, sk + rank, 8, cudaMemcpyDeviceToHost));
+    double v;
+    std::memcpy(&v, &u, 8);
+    thr = v;
+  }
+  // ---- buffers: candidates, refinement list, counters, histogram
+  const unsigned rcap = 1u << 22;
+  char* buf = (char*)ws_get(ctx, WS_PAIR_CAND, (size_t)cap * 12 + (size_t)rcap * 8 + 64 + 8 * (size_t)nbins + 64);
+  float* cval = (float*)buf;
+  int* ci = (int*)(cval + cap);
+  int* cj = ci + cap;
+  int* ri = cj + cap;
+  int* rj = ri + rcap;
+  unsigned* counters = (unsigned*)(rj + rcap);  // ncand, nref, err
+  unsigned long long* hist = (unsigned long long*)round_up((long)(uintptr_t)(counters + 4), 16);
+
+  const int nj = ops.NBpad / TN, ni = ops.NApad / TM;
+  const int grid_max = ctx->sm_count;
+  int njc = 1;
+  while ((long)ni * njc < 8L * grid_max && njc < nj) njc *= 2;
+  const int jchunk = (nj + njc - 1) / njc;
+  njc = (nj + jchunk - 1) / jchunk;
+  PdParams prm;
+  prm.NA = NA;
+  prm.NB = NB;
+  prm.nj = nj;
+  prm.njc = njc;
+  prm.jchunk = jchunk;
+  prm.nitems = ni * njc;
+  prm.nkb = nkb;
+  prm.alpha = ops.alpha;
+  prm.beta = ops.beta;
+  prm.delta2 = (float)(delta * delta);
+  prm.nbins = nbins;
+  prm.lo = (float)lo;
+  prm.inv_width = (float)(nbins / (hi - lo));
+  prm.hist = hist;
+  prm.cap = cap;
+  prm.ncand = counters;
+  prm.cval = cval;
+  prm.ci = ci;
+  prm.cj = cj;
+  // left-out diagonal: |2 X4| <= 2 T 127^2 (quantised units); recompute pairs within 1e6 x that of zero
+  prm.refine_int = (long long)(2.0 * T * 127.0 * 127.0 * 1e6);
+  prm.rcap = rcap;
+  prm.nref = counters + 1;
+  prm.ri = ri;
+  prm.rj = rj;
+  prm.out = out;
+  prm.err = (int*)(counters + 2);
+  const size_t smem = smem_bytes(nkb, nbins);
+  set_max_smem((const void*)k_pairdiff_tc, smem);
+  const int grid = std::min(grid_max, prm.nitems);
+  // plain form: FP64 chi2 of row chunks, then histogram / candidates of each chunk
+  double* wd = nullptr;
+  const long rows_per_chunk = std::max<long>(1, std::min<long>(NA, (1L << 27) / NB));
+  double* chunk = nullptr;
+  if (method == 0) {
+    chunk = (double*)ws_get(ctx, WS_CONV_OUT, sizeof(double) * rows_per_chunk * NB);
+    wd = (double*)ctx->ws_ptr[WS_SMALL];  // sw, w, d from pairdiff_prepare
+  }
+  double W = 0.0;
+  for (int t = 0; t < T; t++) W += w_host[t];
+
+  for (int pass = 0; pass < 4; pass++) {
+    res.passes = pass + 1;
+    prm.thr = (float)std::min(thr, 3.0e38);
+    MLC_CUDA(cudaMemsetAsync(counters, 0, 16, ctx->stream));
+    MLC_CUDA(cudaMemsetAsync(hist, 0, 8 * (size_t)nbins, ctx->stream));
+    if (method == 1) {
+      MLC_KSCOPE(ctx, "pairdiff_tc");
+      k_pairdiff_tc<<<grid, NTHREADS, smem, ctx->stream>>>(tmA, tmB, prm);
+    } else {
+      for (long r0 = 0; r0 < NA; r0 += rows_per_chunk) {
+        const long nr = std::min<long>(rows_per_chunk, NA - r0);
+        pairdiff_plain(ctx, A + r0 * T, B, (int)nr, NB, T, wd + T, d_host ? wd + 2 * T : nullptr, W, offset, 0,
+                       nullptr, nullptr, chunk);
+        if (out) {
+          // matrix output of the plain form as FP32
+          std::vector<double> hc((size_t)nr * NB);
+          MLC_CUDA(cudaMemcpyAsync(hc.data(), chunk, sizeof(double) * hc.size(), cudaMemcpyDeviceToHost, ctx->stream));
+          MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+          std::vector<float> hf(hc.begin(), hc.end());
+          MLC_CUDA(cudaMemcpy(out + r0 * NB, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice));
+        }
+        const long n = nr * NB;
+        const size_t hsm = sizeof(uint32_t) * nbins;
+        set_max_smem((const void*)k_pd_hist_cand, hsm);
+        MLC_KSCOPE(ctx, "pd_hist_cand");
+        k_pd_hist_cand<<<(int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 8), 256, hsm, ctx->stream>>>(
+            chunk, n, r0 * NB, NB, nbins, lo, (hi - lo) / nbins, hist, prm.thr, cap, counters, cval, ci, cj);
+      }
+    }
+    MLC_CHECK_LAUNCH();
+    unsigned hc[4];
+    MLC_CUDA(cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+    MLC_REQUIRE(hc[2] == 0, MLC_ERR_TIMEOUT, "tensor-core pair kernel: a pipeline wait timed out");
+    MLC_REQUIRE(hc[1] <= rcap, MLC_ERR_LIMIT, "too many near-identical pairs to refine (> 4M)");
+    if (hc[1] > 0) {
+      MLC_KSCOPE(ctx, "pd_refine");
+      k_pd_refine<<<std::max(1u, std::min((hc[1] + 255) / 256, (unsigned)ctx->sm_count * 8)), 256, 0, ctx->stream>>>(
+          cen, NA, T, ri, rj, hc[1], nbins, lo, (hi - lo) / nbins, hist, prm.thr, cap, counters, cval, ci, cj, out, NB);
+    }
+    MLC_CHECK_LAUNCH();
+    MLC_CUDA(cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+    res.nrefined = hc[1];
+    res.ncand = hc[0];
+    res.thr = thr;
+    if (k == 0) break;
+    if (hc[0] > cap) {  // too many candidates: lower the threshold
+      thr *= 0.5;
+      continue;
+    }
+    if ((long long)hc[0] < std::min<long long>(k, P) && std::isfinite(thr)) {  // too few: raise it
+      thr = (hc[0] > 0 ? thr * 4.0 : thr * 16.0 + 1e-30);
+      if (pass == 2) thr = INFINITY;
+      continue;
+    }
+    break;
+  }
+  if (hist_host) MLC_CUDA(cudaMemcpy(hist_host, hist, 8 * (size_t)nbins, cudaMemcpyDeviceToHost));
+  // ---- top-k from the candidates: sort by value (stable by candidate order), then order
+  // ties by pair index on the host
+  if (k > 0) {
+    const unsigned nc = (unsigned)std::min<long long>(res.ncand, cap);
+    const unsigned m = (unsigned)std::min<long long>(nc, (long long)k + 1024);
+    const unsigned ncb = std::max(nc, 1u);
+    char* kb = (char*)ws_get(ctx, WS_LOC, (sizeof(uint64_t) + sizeof(uint32_t)) * (size_t)ncb + 12 * (size_t)ncb + 64);
+    uint64_t* keys = (uint64_t*)kb;
+    uint32_t* vals = (uint32_t*)(keys + ncb);
+    float* gv = (float*)(vals + ncb);
+    int* gi = (int*)(gv + ncb);
+    int* gj = gi + ncb;
+    if (nc > 0) {
+      {
+        MLC_KSCOPE(ctx, "pd_topk_keys");
+        k_cand_keys<<<std::max(1u, std::min((nc + 255) / 256, (unsigned)ctx->sm_count * 8)), 256, 0, ctx->stream>>>(
+            cval, nc, keys, vals);
+      }
+      MLC_CHECK_LAUNCH();
+      radix_sort_u64_u32(ctx, nc, keys, vals);
+      {
+        MLC_KSCOPE(ctx, "pd_topk_gather");
+        k_cand_gather<<<std::max(1u, (m + 255) / 256), 256, 0, ctx->stream>>>(vals, m, cval, ci, cj, gv, gi, gj);
+      }
+      MLC_CHECK_LAUNCH();
+    }
+    // the first k + 1024 by value; order ties by pair index on the host
+    std::vector<float> hv(m);
+    std::vector<int> hi_(m), hj(m);
+    MLC_CUDA(cudaMemcpy(hv.data(), gv, 4 * (size_t)m, cudaMemcpyDeviceToHost));
+    MLC_CUDA(cudaMemcpy(hi_.data(), gi, 4 * (size_t)m, cudaMemcpyDeviceToHost));
+    MLC_CUDA(cudaMemcpy(hj.data(), gj, 4 * (size_t)m, cudaMemcpyDeviceToHost));
+    const unsigned ncand_used = m;
+    std::vector<uint32_t> idx(ncand_used);
+    for (unsigned q = 0; q < ncand_used; q++) idx[q] = q;
+    std::sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) {
+      if (hv[x] != hv[y]) return hv[x] < hv[y];
+      const long long px = (long long)hi_[x] * NB + hj[x], py = (long long)hi_[y] * NB + hj[y];
+      return px < py;
+    });
+    const int kk = (int)std::min<long long>(k, ncand_used);
+    for (int q = 0; q < kk; q++) {
+      tv[q] = hv[idx[q]];
+      ti[q] = hi_[idx[q]];
+      tj[q] = hj[idx[q]];
+    }
+    for (int q = kk; q < k; q++) {
+      tv[q] = INFINITY;
+      ti[q] = -1;
+      tj[q] = -1;
+    }
+  }
+}
+
+}  // namespace mlc
