@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--small", action="store_true", help="reduced sizes (debug only; not a bench number)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 form")
+    ap.add_argument("--no-pair", action="store_true", help="skip the pair-chi2/s workload")
     ap.add_argument("--n", type=int, default=None, help="map side (profiling cases only; not a bench number)")
     ap.add_argument("--tracks", type=int, default=None, help="track count (profiling cases only)")
     return ap.parse_args()
@@ -180,6 +181,113 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["bf16_tflops"]), "measured burst"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+# Pairwise chi2 workload: images A and B, 10^5 FP32 magnitude curves each, T = 128 shared
+# epochs, sigma ~ U(0.02, 0.1) mag, offset-minimised magnitude-difference chi2, 1000-bin
+# log10-chi2 histogram and the 10^4 smallest pairs.
+PAIR_N, PAIR_T, PAIR_BINS, PAIR_K = 100_000, 128, 1000, 10_000
+
+
+def pair_workload(args, ctx, convs, n, dev, world, rank, stream):
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    N = min(PAIR_N, args.tracks or PAIR_N) if args.small or args.tracks else PAIR_N
+    # curves: 2N straight tracks with 128 epochs over three seasons, sampled on two
+    # convolved maps (thin disc 16 px for image A, uniform 16 px for image B)
+    g = torch.Generator(device="cpu").manual_seed(7 + rank)
+    T = PAIR_T
+    ntr = 2 * N
+    season = torch.arange(T) * 3 // T
+    base_t = season.double() * (SEASON_LEN + GAP) + (torch.arange(T) % (T // 3 + 1)).double() * (SEASON_LEN / (T // 3 + 1))
+    t = base_t.repeat(ntr)
+    off = torch.arange(0, ntr + 1, dtype=torch.int64) * T
+    phi = torch.rand(ntr, generator=g, dtype=torch.float64) * 6.283185307179586
+    v = 0.05 + 0.45 * torch.rand(ntr, generator=g, dtype=torch.float64)
+    L = v * base_t[-1]
+    x0 = MARGIN + torch.clamp(-L * torch.cos(phi), min=0) + (n - 2 * MARGIN - L.abs()) * torch.rand(ntr, generator=g, dtype=torch.float64)
+    y0 = MARGIN + torch.clamp(-L * torch.sin(phi), min=0) + (n - 2 * MARGIN - L.abs()) * torch.rand(ntr, generator=g, dtype=torch.float64)
+    f = lambda a: a.to(device=dev, dtype=torch.float32)
+    mags = mlc.sample_tracks(ctx, [convs[len(RHALF_PX) + 3], convs[3]], n, n, f(x0), f(y0), f(phi), f(v),
+                             off.to(dev), f(t), mag=True)
+    A = mags[0, : N * T].reshape(N, T).contiguous()
+    B = mags[1, N * T:].reshape(N, T).contiguous()
+    rng = np.random.default_rng(11 + rank)
+    w = 1.0 / rng.uniform(0.02, 0.1, T) ** 2
+    d = np.zeros(T)
+
+    def pstep():
+        return mlc.pair_chi2_magdiff(ctx, A, B, w, d, True, method="tensor", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                                     k=PAIR_K)
+
+    for _ in range(max(args.warmup, 1)):
+        r = pstep()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    psteps = max(1, min(args.steps, 5))
+    if world > 1:
+        torch.distributed.barrier()
+    e0.record(stream)
+    for _ in range(psteps):
+        r = pstep()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / psteps
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    pairs = float(N) * N
+    value = world * pairs / (ms / 1000.0)
+    # per-kernel times of one step
+    ctx.set_timing(True)
+    pstep()
+    kt = ctx.kernel_times(reset=True)
+    ctx.set_timing(False)
+    tc_ms = kt.get("pairdiff_tc", (float("nan"), 1))[0]
+    Kp = ((T + 63) // 64) * 64
+    napad, nbpad = ((N + 127) // 128) * 128, ((N + 47) // 48) * 48
+    executed = 9 * 2.0 * Kp * napad * nbpad  # 9 bf16 slice products per epoch per pair
+    peak, pk = bf16_peak()
+    ach = executed / (tc_ms / 1000.0) / 1e12
+    # plain FP64 form on a subset of rows (same statistic, one launch per stage)
+    sub_rows = 1000
+    mlc.pair_chi2_magdiff(ctx, A[:sub_rows], B, w, d, True, method="plain", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                          k=min(PAIR_K, 1000))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    mlc.pair_chi2_magdiff(ctx, A[:sub_rows], B, w, d, True, method="plain", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                          k=min(PAIR_K, 1000))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    pms = e0.elapsed_time(e1)
+    plain_val = world * sub_rows * float(N) / (pms / 1000.0)
+    return {"metric": "pair-chi2/s", "value": value, "unit": "pair-chi2/s", "ms_per_step": ms, "steps": psteps,
+            "config": {"workload": f"images A, B: {N} x {N} FP32 magnitude curves, T={T} shared epochs, "
+                                   f"sigma~U(0.02,0.1), offset-minimised, {PAIR_BINS}-bin log10-chi2 histogram, "
+                                   f"top-{PAIR_K}", "pairs_per_step": pairs,
+                       "curves": "bilinear samples of two convolved maps of the bench map"},
+            "roofline": {"kernel": "pairdiff_tc", "bound": "tensor", "achieved": ach, "peak": peak,
+                         "unit": "TFLOP/s", "frac": ach / peak, "traffic": None,
+                         "flops_per_launch": executed, "launch_ms": tc_ms,
+                         "useful_tflops": 2.0 * T * pairs / (tc_ms / 1000.0) / 1e12,
+                         "peak_source": f"{pk} bf16 dense (MEASURED_PEAKS.json bf16_tflops)",
+                         "note": "executed = 9 bf16 slice products (exact 24-bit sliced integers) per epoch per pair"},
+            "kernels_ms": {k_: v_[0] for k_, v_ in kt.items()},
+            "stats": r["stats"],
+            "plain_fp64": {"value": plain_val, "unit": "pair-chi2/s", "ms": pms, "pairs": sub_rows * N,
+                           "batched_over_plain": value / plain_val}}
 
 
 def algorithmic_bytes(name, n, E, nprof, e=4):
@@ -448,6 +556,11 @@ def main():
                  "batched_over_plain": value / (world * lc_per_step / (pms / 1000.0))}
         del m64, convs64, tr64, out64
 
+    # ---- pair-chi2/s workload on the same device
+    pair = None
+    if not args.no_pair:
+        pair = pair_workload(args, ctx, convs, n, dev, world, rank, stream)
+
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -462,7 +575,7 @@ def main():
                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
                        "ms_per_step": e2e_ms},
                "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
-               "light_curves_per_step": lc_per_step, "epochs_per_step": E}
+               "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair}
         print(json.dumps(res), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

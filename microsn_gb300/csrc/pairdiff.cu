@@ -10,8 +10,8 @@
 //
 // This file holds the plain FP64 form (one thread per pair, CUDA cores) and the
 // preparation used by the tensor-core form (pairtc.cu): per-curve centring and
-// weighting in FP64, one global quantisation step, 24-bit integers split into three
-// signed 8-bit slices stored as bf16 (exact), and the exact squared norms.
+// weighting in FP64, a power-of-two quantisation step per curve, 24-bit integers split
+// into three signed 8-bit slices stored as bf16 (exact), and the exact squared norms.
 #include <cmath>
 #include <vector>
 
@@ -104,16 +104,26 @@ __device__ __forceinline__ uint16_t bf16_of_small_int(int v) {
   return (uint16_t)(__float_as_uint(f) >> 16);
 }
 
-// Quantise to integers q = rint(v / delta) (|q| <= QMAX), split q = s0*65536 + s1*256 + s2
-// with balanced digits in [-128, 127], write the slices into the operand row
-// [slice 0 | slice 1 | slice 2] (Kp = padded T each, zeros beyond T), and the exact
-// squared norm sum q^2.  Rows beyond N (padding up to the tile) are zero.
-__global__ void __launch_bounds__(256) k_pd_quantize(const double* __restrict__ v, int N, int Npad, int T, int Kp,
-                                                     double inv_delta, uint16_t* __restrict__ ops,
-                                                     long long* __restrict__ norm2, int* __restrict__ err) {
+// Per row: step exponent e = ceil(log2(rowmax / QMAX)) (clamped to [-100, 100]), integers
+// q = rint(v 2^-e) (|q| <= QMAX), split q = s0*65536 + s1*256 + s2 with balanced digits in
+// [-128, 127], slices written to the operand row [slice 0 | slice 1 | slice 2] (Kp = padded T
+// each, zeros beyond T), the exact squared norm sum q^2 and its float-float copy.  Rows
+// beyond N (padding up to the tile) are zero.
+__global__ void __launch_bounds__(256) k_pd_quantize(const double* __restrict__ v, const double* __restrict__ rowmax,
+                                                     int N, int Npad, int T, int Kp, uint16_t* __restrict__ ops,
+                                                     long long* __restrict__ norm2, float2* __restrict__ norm2_ff,
+                                                     int* __restrict__ exps, int* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const long r = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= Npad) return;
+  int e = PD_EMIN;
+  if (r < N && rowmax[r] > 0) {
+    e = (int)ceil(log2(rowmax[r] / (double)PD_QMAX));
+    if (rowmax[r] * exp2(-(double)e) > (double)PD_QMAX) e++;  // guard the rounding of log2
+    if (e > PD_EMAX) atomicExch(err, 2);
+    e = max(PD_EMIN, min(PD_EMAX, e));
+  }
+  const double inv_delta = exp2(-(double)e);
   uint16_t* row = ops + r * (3L * Kp);
   long long acc = 0;
   for (int t = lane; t < Kp; t += 32) {
@@ -133,7 +143,14 @@ __global__ void __launch_bounds__(256) k_pd_quantize(const double* __restrict__ 
     acc += (long long)q * q;
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (lane == 0) norm2[r] = acc;
+  if (lane == 0) {
+    norm2[r] = acc;
+    // |P|^2 in natural units, alpha 2^(2e), as a float-float pair (exact scaling in FP64)
+    const double v2 = (double)acc * exp2(2.0 * e);
+    const float hi = (float)v2;
+    norm2_ff[r] = make_float2(hi, (float)(v2 - (double)hi));
+    exps[r] = e;
+  }
 }
 
 // Builds both operand sides.  Returns delta (the quantisation step).
@@ -177,6 +194,7 @@ double pairdiff_prepare(mlc_ctx* ctx, const float* A, const float* B, int NA, in
                                                           cen + (size_t)NA * T, rowmax + NA);
   }
   MLC_CHECK_LAUNCH();
+  // the largest row maximum sets the reported step; rows keep their own steps
   unsigned long long* gmax = (unsigned long long*)ws_get(ctx, WS_SORT_HIST, 64);
   int* derr = (int*)(gmax + 1);
   MLC_CUDA(cudaMemsetAsync(gmax, 0, 16, ctx->stream));
@@ -191,30 +209,35 @@ double pairdiff_prepare(mlc_ctx* ctx, const float* A, const float* B, int NA, in
   MLC_CUDA(cudaStreamSynchronize(ctx->stream));
   double mx;
   memcpy(&mx, &hm, 8);
-  const double delta = mx > 0 ? mx / (double)PD_QMAX : 1.0;
+  const double delta = mx > 0 ? std::exp2(std::ceil(std::log2(mx / (double)PD_QMAX))) : 1.0;
   ops.delta = delta;
-  // operands and norms
+  // operands, norms, float-float norms and exponents
   const size_t rowsA = ops.NApad, rowsB = ops.NBpad;
   ops.a = (uint16_t*)ws_get(ctx, WS_PAIR_ACC, sizeof(uint16_t) * 3 * ops.Kp * (rowsA + rowsB) +
-                                                  sizeof(long long) * (rowsA + rowsB) + 256);
+                                                  (sizeof(long long) + sizeof(float2) + sizeof(int)) * (rowsA + rowsB) +
+                                                  512);
   ops.b = ops.a + 3 * (size_t)ops.Kp * rowsA;
-  ops.alpha = (long long*)(ops.b + 3 * (size_t)ops.Kp * rowsB);
-  ops.alpha = (long long*)round_up((long)(uintptr_t)ops.alpha, 16);
+  ops.alpha = (long long*)round_up((long)(uintptr_t)(ops.b + 3 * (size_t)ops.Kp * rowsB), 16);
   ops.beta = ops.alpha + rowsA;
+  ops.alpha_ff = (float2*)(ops.beta + rowsB);
+  ops.beta_ff = ops.alpha_ff + rowsA;
+  ops.ea = (int*)(ops.beta_ff + rowsB);
+  ops.eb = ops.ea + rowsA;
   {
     MLC_KSCOPE(ctx, "pd_quantize");
-    k_pd_quantize<<<ceil_div(ops.NApad, 8), 256, 0, ctx->stream>>>(cen, NA, ops.NApad, T, ops.Kp, 1.0 / delta, ops.a,
-                                                                   ops.alpha, derr);
+    k_pd_quantize<<<ceil_div(ops.NApad, 8), 256, 0, ctx->stream>>>(cen, rowmax, NA, ops.NApad, T, ops.Kp, ops.a,
+                                                                   ops.alpha, ops.alpha_ff, ops.ea, derr);
   }
   {
     MLC_KSCOPE(ctx, "pd_quantize");
-    k_pd_quantize<<<ceil_div(ops.NBpad, 8), 256, 0, ctx->stream>>>(cen + (size_t)NA * T, NB, ops.NBpad, T, ops.Kp,
-                                                                   1.0 / delta, ops.b, ops.beta, derr);
+    k_pd_quantize<<<ceil_div(ops.NBpad, 8), 256, 0, ctx->stream>>>(cen + (size_t)NA * T, rowmax + NA, NB, ops.NBpad, T,
+                                                                   ops.Kp, ops.b, ops.beta, ops.beta_ff, ops.eb, derr);
   }
   MLC_CHECK_LAUNCH();
   int herr = 0;
   MLC_CUDA(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  MLC_REQUIRE(herr != 2, MLC_ERR_LIMIT, "curve amplitudes beyond 2^20 * 8355711 (after weighting)");
   MLC_REQUIRE(herr == 0, MLC_ERR_ARG, "non-finite curve values");
   return delta;
 }

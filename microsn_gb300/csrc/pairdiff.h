@@ -10,16 +10,23 @@ namespace mlc {
 // Largest quantised magnitude: three balanced base-256 digits in [-127, 127].
 constexpr int PD_QMAX = 127 * (65536 + 256 + 1);  // 8355711
 constexpr int PD_TILE_M = 128;                    // A curves per tile (TMEM lanes)
-constexpr int PD_TILE_N = 64;                     // B curves per tile
+constexpr int PD_TILE_N = 48;                     // B curves per tile
+constexpr int PD_EMIN = -60, PD_EMAX = 20;        // range of the per-curve step exponents
 
 // Operands of the tensor-core form, built by pairdiff_prepare.
+// Each curve r is quantised with its own power-of-two step 2^e_r (the smallest that keeps
+// |q| <= PD_QMAX), so flat curves keep full relative precision.
 struct PdOperands {
   int NA = 0, NB = 0, NApad = 0, NBpad = 0, T = 0, Kp = 0;
-  double delta = 1.0;          // quantisation step: value = delta * q
+  double delta = 1.0;          // largest step 2^e over all curves (reported)
   uint16_t* a = nullptr;       // NApad rows of [s0 | s1 | s2], Kp bf16 each (device)
   uint16_t* b = nullptr;       // NBpad rows of [t0 | t1 | t2]
   long long* alpha = nullptr;  // sum q^2 per A row (device)
   long long* beta = nullptr;   // sum q^2 per B row
+  float2* alpha_ff = nullptr;  // |P_i|^2 = alpha 2^(2 e) in natural units, float-float (hi, lo)
+  float2* beta_ff = nullptr;
+  int* ea = nullptr;           // step exponent per A row
+  int* eb = nullptr;           // step exponent per B row
 };
 
 struct PdResult {

@@ -1,20 +1,23 @@
 // Tensor-core form of the pairwise magnitude-difference chi2 (see pairdiff.cu for the
-// statistic).  chi2_ij = |Q_j - P_i|^2 = alpha_i + beta_j - 2 P_i.Q_j on quantised curves
-// P = delta p, Q = delta q (p, q integers, |p|,|q| <= 8355711) held as three signed 8-bit
-// slices p = 65536 s0 + 256 s1 + s2 in bf16.  A slice product summed over T <= 128 epochs
-// stays below 2^24, so every FP32 tensor-core accumulation is exact; the cross term is
-// accumulated per diagonal d = a + b of slice exponents (four TMEM accumulators d = 0..3,
-// eight slice pairs) and assembled in int64:
-//     x = 2^32 X0 + 2^24 X1 + 2^16 X2 + 2^8 X3   (X4 = s2.t2 is left out: |2 X4| <= 2^22 T)
-// chi2 (in delta^2 units) = alpha + beta - 2 x.  Pairs whose value is within 1e6 times the
-// left-out bound of zero are recomputed in FP64 by k_pd_refine, so every reported chi2 is
-// within 1e-6 relative of the exact chi2 of the quantised curves.
+// statistic).  chi2_ij = |Q_j - P_i|^2 on quantised curves P_i = 2^ei p_i, Q_j = 2^ej q_j
+// (p, q integers, |p|,|q| <= 8355711, one power-of-two step per curve) held as three signed
+// 8-bit slices p = 65536 s0 + 256 s1 + s2 in bf16.  A slice product summed over T <= 128
+// epochs stays below 2^24, so every FP32 tensor-core accumulation is exact; the cross term
+// is accumulated per diagonal d = a + b of slice exponents (five TMEM accumulators
+// d = 0..4, all nine slice pairs), so
+//     x = p.q = 2^32 X0 + 2^24 X1 + 2^16 X2 + 2^8 X3 + X4   exactly,
+// and chi2 = |P|^2 + |Q|^2 - 2^(ei+ej+1) x is formed in float-float arithmetic from the
+// per-curve norms (natural units) and the five exactly scaled accumulators.  Top-k
+// candidates, pairs whose chi2 is below 1e-7 of |P|^2 + |Q|^2 (where the float-float
+// rounding could matter) and, with a matrix requested, every pair whose quantisation error
+// could exceed 1e-6 relative are recomputed in FP64 by k_pd_refine.
 //
 // Kernel layout (one persistent CTA per SM, 12 warps):
 //   warp 0      TMA producer: the work item's 128 A rows (3 slices x Kp, resident in shared
-//               memory) and, double-buffered, each 64-row B tile
-//   warp 1      MMA issuer (one thread): 8 slice pairs x Kp/16 tcgen05.mma per tile into one
-//               of two TMEM buffers (4 accumulators x 64 columns each, 512 columns total)
+//               memory) and, double-buffered, each 48-row B tile
+//   warp 1      MMA issuer (one thread): 9 slice pairs x Kp/16 tcgen05.mma per tile into one
+//               of two TMEM buffers (5 accumulators x 48 columns each; buffers at columns
+//               0 and 256 of the 512 allocated)
 //   warp 2      TMEM allocation / release
 //   warps 4-11  epilogue: TMEM -> registers, int64 assembly, log10-chi2 histogram in shared
 //               memory, top-k candidates below a threshold, refinement list, optional matrix
@@ -45,13 +48,17 @@ constexpr int TMEM_COLS = 512;
 constexpr int MAX_KP = 128;
 constexpr int MAX_BINS = 4096;
 constexpr int A_BOX = TM * 128;  // bytes of one 64-element K box of A (128 rows x 128 B)
-constexpr int B_BOX = TN * 128;
+constexpr int B_BOX = TN * 128;  // 6144 B: a multiple of the 1024-B swizzle atom
+constexpr int NACC = 5;
+constexpr int TBUF = 256;        // TMEM column stride between the two accumulator buffers
+static_assert(NACC * TN <= TBUF && B_BOX % 1024 == 0, "TMEM / smem layout");
 
 struct PdParams {
   int NA, NB, nj, njc, jchunk, nitems, nkb;
-  const long long* alpha;
-  const long long* beta;
-  float delta2;
+  const float2* alpha_ff;
+  const float2* beta_ff;
+  const int* ea;
+  const int* eb;
   int nbins;
   float lo, inv_width;
   unsigned long long* hist;
@@ -61,7 +68,7 @@ struct PdParams {
   float* cval;
   int* ci;
   int* cj;
-  long long refine_int;
+  float refine_f;  // matrix mode: quantisation bound factor
   unsigned int rcap;
   unsigned int* nref;
   int* ri;
@@ -72,6 +79,28 @@ struct PdParams {
 
 size_t smem_bytes(int nkb, int nbins) {
   return 1024 + (size_t)3 * nkb * A_BOX + (size_t)NSTAGE * 3 * nkb * B_BOX + 16 * 8 + 16 + sizeof(uint32_t) * nbins;
+}
+
+// 2^k for k in [-126, 127]; 0 below (the terms it scales are then negligible)
+__device__ __forceinline__ float pow2f(int k) { return k < -126 ? 0.f : __int_as_float((k + 127) << 23); }
+
+// Error-free sum s + e = a + b.
+__device__ __forceinline__ float two_sum(float a, float b, float& e) {
+  const float s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+  return s;
+}
+
+// chi2 = A + B - (u0 + ... + u4): A, B float-float, u_k exact floats (scaled
+// accumulators); the large, cancelling terms go through error-free two-sums.
+__device__ __forceinline__ float chi2_assemble(float2 A, float2 B, float u0, float u1, float u2, float u3,
+                                               float u4) {
+  float e1, e2, e3;
+  const float s = two_sum(A.x, B.x, e1);
+  const float t = two_sum(s, -u0, e2);
+  const float t2 = two_sum(t, -u1, e3);
+  return t2 + (((e1 + e2) + e3) + ((A.y + B.y) - ((u2 + u3) + u4)));
 }
 
 __device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" ::"r"(EPI_WARPS * 32) : "memory"); }
@@ -154,17 +183,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
           break;
         }
         tc::fence_after_sync();
-        const uint32_t dbase = tmem + tb * 256;
-        uint32_t first = 0xF;
+        const uint32_t dbase = tmem + tb * TBUF;
+        uint32_t first = 0x1F;
         for (int a = 0; a < 3; a++)
           for (int b = 0; b < 3; b++) {
             const int d = a + b;
-            if (d > 3) continue;
             for (int kk = 0; kk < ksteps; kk++) {
               const int kb = kk >> 2, ko = (kk & 3) * 32;
               const uint64_t ad = tc::desc_sw128(tc::smem_u32(A_s + (a * nkb + kb) * A_BOX) + ko);
               const uint64_t bd = tc::desc_sw128(tc::smem_u32(B_s + (s * 3 * nkb + b * nkb + kb) * B_BOX) + ko);
-              tc::mma_bf16(dbase + d * 64, ad, bd, idesc, (first >> d) & 1 ? 0u : 1u);
+              tc::mma_bf16(dbase + d * TN, ad, bd, idesc, (first >> d) & 1 ? 0u : 1u);
               first &= ~(1u << d);
             }
           }
@@ -185,7 +213,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
       const int j0 = jc * P.jchunk, j1 = min(P.nj, j0 + P.jchunk);
       const int i = itile * TM + 32 * q + lane;
       const bool irow = i < P.NA;
-      const long long al = irow ? P.alpha[i] : 0;
+      const float2 aff = irow ? P.alpha_ff[i] : make_float2(0.f, 0.f);
+      const int ei = irow ? P.ea[i] : PD_EMIN;
       for (int jt = j0; jt < j1; jt++, ct++) {
         const uint32_t tb = ct & 1, tu = ct >> 1;
         if (*abort_s) break;
@@ -194,25 +223,46 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
           break;
         }
         tc::fence_after_sync();
-        for (int ch = 0; ch < 4; ch++) {
-          const int col0 = h * 32 + ch * 8;
-          uint32_t r0[8], r1[8], r2[8], r3[8];
-          const uint32_t ta = tmem + tb * 256 + lane_addr + col0;
+        // this warp's 24 columns: lane c < 24 holds column h*24 + c (broadcast by shuffles)
+        const int jl = jt * TN + h * 24 + lane;
+        const bool lok = lane < 24 && jl < P.NB;
+        const float2 bl = lok ? __ldg(P.beta_ff + jl) : make_float2(0.f, 0.f);
+        const int el = lok ? __ldg(P.eb + jl) : PD_EMIN;
+        for (int ch = 0; ch < 3; ch++) {
+          const int col0 = h * 24 + ch * 8;
+          uint32_t r0[8], r1[8], r2[8], r3[8], r4[8];
+          const uint32_t ta = tmem + tb * TBUF + lane_addr + col0;
           tc::tmem_ld8(ta, r0);
-          tc::tmem_ld8(ta + 64, r1);
-          tc::tmem_ld8(ta + 128, r2);
-          tc::tmem_ld8(ta + 192, r3);
+          tc::tmem_ld8(ta + TN, r1);
+          tc::tmem_ld8(ta + 2 * TN, r2);
+          tc::tmem_ld8(ta + 3 * TN, r3);
+          tc::tmem_ld8(ta + 4 * TN, r4);
           tc::tmem_wait_ld();
 #pragma unroll
           for (int c = 0; c < 8; c++) {
+            const int src = ch * 8 + c;
+            const float2 bff = make_float2(__shfl_sync(0xffffffffu, bl.x, src), __shfl_sync(0xffffffffu, bl.y, src));
+            const int ej = __shfl_sync(0xffffffffu, el, src);
             const int j = jt * TN + col0 + c;
             if (!irow || j >= P.NB) continue;
-            const long long x = ((long long)__float2int_rn(__uint_as_float(r0[c])) << 32) +
-                                ((long long)__float2int_rn(__uint_as_float(r1[c])) << 24) +
-                                ((long long)__float2int_rn(__uint_as_float(r2[c])) << 16) +
-                                ((long long)__float2int_rn(__uint_as_float(r3[c])) << 8);
-            const long long c2 = al + __ldg(P.beta + j) - 2 * x;
-            if (c2 < P.refine_int) {
+            // 2 x 2^(ei+ej) = sum_d 2^(ei+ej+33-8d) X_d, each term an exact float
+            const float s0 = pow2f(ei + ej + 33);
+            const float u0 = __uint_as_float(r0[c]) * s0;
+            const float u1 = __uint_as_float(r1[c]) * (s0 * 0x1p-8f);
+            const float u2 = __uint_as_float(r2[c]) * (s0 * 0x1p-16f);
+            const float u3 = __uint_as_float(r3[c]) * (s0 * 0x1p-24f);
+            const float u4 = __uint_as_float(r4[c]) * (s0 * 0x1p-32f);
+            const float chi2 = chi2_assemble(aff, bff, u0, u1, u2, u3, u4);
+            // below this the float-float rounding (about 2^-40 of the norms) could exceed
+            // 1e-5 relative; matrix mode: the quantisation-error bound
+            float bound = 1e-7f * (aff.x + bff.x);
+            if (P.out) {
+              const float q = pow2f(ei) + pow2f(ej);
+              bound = fmaxf(bound, P.refine_f * q * q);
+            }
+            // top-k candidates and near-zero pairs go to the exact FP64 list (which also
+            // histograms them); every other pair is histogrammed here
+            if (chi2 < bound || chi2 < P.thr) {
               const unsigned k = atomicAdd(P.nref, 1u);
               if (k < P.rcap) {
                 P.ri[k] = i;
@@ -220,18 +270,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
               }
               continue;
             }
-            const float chi2 = (float)c2 * P.delta2;
             if (P.out) P.out[(long)i * P.NB + j] = chi2;
             const int bin = (int)floorf((__log2f(chi2) * 0.30102999566398120f - P.lo) * P.inv_width);
             if (bin >= 0 && bin < P.nbins) atomicAdd(hist_s + bin, 1u);
-            if (chi2 < P.thr) {
-              const unsigned k = atomicAdd(P.ncand, 1u);
-              if (k < P.cap) {
-                P.cval[k] = chi2;
-                P.ci[k] = i;
-                P.cj[k] = j;
-              }
-            }
           }
         }
         tc::fence_before_sync();
@@ -458,9 +499,10 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
   prm.jchunk = jchunk;
   prm.nitems = ni * njc;
   prm.nkb = nkb;
-  prm.alpha = ops.alpha;
-  prm.beta = ops.beta;
-  prm.delta2 = (float)(delta * delta);
+  prm.alpha_ff = ops.alpha_ff;
+  prm.beta_ff = ops.beta_ff;
+  prm.ea = ops.ea;
+  prm.eb = ops.eb;
   prm.nbins = nbins;
   prm.lo = (float)lo;
   prm.inv_width = (float)(nbins / (hi - lo));
@@ -470,8 +512,14 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
   prm.cval = cval;
   prm.ci = ci;
   prm.cj = cj;
-  // left-out diagonal: |2 X4| <= 2 T 127^2 (quantised units); recompute pairs within 1e6 x that of zero
-  prm.refine_int = (long long)(2.0 * T * 127.0 * 127.0 * 1e6);
+  // Pairs recomputed exactly besides the top-k candidates (bounds in units of 2^(2m), where
+  // the steps of both curves are <= 2^m).  With a matrix requested, every pair whose
+  // quantisation error (taken at 2 sqrt(T/6) 2^m sqrt(chi2) for independent uniform errors)
+  // could exceed 1e-6 relative; otherwise the pairs within 1e4 times the left-out-diagonal
+  // bound 2 T 127^2 of zero (whose sign or log10 bin that bound could change).
+  // Matrix mode: recompute every pair whose quantisation error, taken at
+  // 2 sqrt(T/6) (2^ei + 2^ej) sqrt(chi2) for independent uniform errors, could exceed 1e-6.
+  prm.refine_f = (float)(4.0 * (T / 6.0) * 1e12);
   prm.rcap = rcap;
   prm.nref = counters + 1;
   prm.ri = ri;
@@ -526,7 +574,12 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
     MLC_CUDA(cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, ctx->stream));
     MLC_CUDA(cudaStreamSynchronize(ctx->stream));
     MLC_REQUIRE(hc[2] == 0, MLC_ERR_TIMEOUT, "tensor-core pair kernel: a pipeline wait timed out");
-    MLC_REQUIRE(hc[1] <= rcap, MLC_ERR_LIMIT, "too many near-identical pairs to refine (> 4M)");
+    if (hc[1] > rcap) {  // the exact list overflowed: with a finite threshold lower it, else give up
+      MLC_REQUIRE(std::isfinite(thr) && k > 0 && pass < 3, MLC_ERR_LIMIT,
+                  "more than 4M pairs need the exact FP64 path (near-identical curves)");
+      thr *= 0.25;
+      continue;
+    }
     if (hc[1] > 0) {
       MLC_KSCOPE(ctx, "pd_refine");
       k_pd_refine<<<std::max(1u, std::min((hc[1] + 255) / 256, (unsigned)ctx->sm_count * 8)), 256, 0, ctx->stream>>>(
