@@ -12,15 +12,16 @@
 // rounding could matter) and, with a matrix requested, every pair whose quantisation error
 // could exceed 1e-6 relative are recomputed in FP64 by k_pd_refine.
 //
-// Kernel layout (one persistent CTA per SM, 12 warps):
+// Kernel layout (one persistent CTA per SM, 16 warps):
 //   warp 0      TMA producer: the work item's 128 A rows (3 slices x Kp, resident in shared
 //               memory) and, double-buffered, each 48-row B tile
 //   warp 1      MMA issuer (one thread): 9 slice pairs x Kp/16 tcgen05.mma per tile into one
 //               of two TMEM buffers (5 accumulators x 48 columns each; buffers at columns
 //               0 and 256 of the 512 allocated)
 //   warp 2      TMEM allocation / release
-//   warps 4-11  epilogue: TMEM -> registers, int64 assembly, log10-chi2 histogram in shared
-//               memory, top-k candidates below a threshold, refinement list, optional matrix
+//   warps 4-15  epilogue (three warps per TMEM lane quadrant, 16 columns each): TMEM ->
+//               registers, chi2 assembly, log10-chi2 histogram in shared memory, top-k
+//               candidates below a threshold, refinement list, optional matrix
 // Every barrier wait is bounded; a timeout sets the error flag and all roles unwind.
 #include <cuda.h>
 
@@ -42,7 +43,7 @@ namespace {
 
 constexpr int TM = PD_TILE_M, TN = PD_TILE_N;
 constexpr int NSTAGE = 2;
-constexpr int EPI_WARPS = 8;
+constexpr int EPI_WARPS = 12;  // three per SM sub-partition, 16 columns each
 constexpr int NTHREADS = (4 + EPI_WARPS) * 32;
 constexpr int TMEM_COLS = 512;
 constexpr int MAX_KP = 128;
@@ -105,11 +106,12 @@ __device__ __forceinline__ float chi2_assemble(float2 A, float2 B, float u0, flo
 
 __device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" ::"r"(EPI_WARPS * 32) : "memory"); }
 
+template <int NKB>  // 64-element K boxes per slice (Kp / 64)
 __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_constant__ CUtensorMap tmA,
                                                              const __grid_constant__ CUtensorMap tmB, PdParams P) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const int nkb = P.nkb;
+  constexpr int nkb = NKB;
   unsigned char* A_s = sm;
   unsigned char* B_s = A_s + 3 * nkb * A_BOX;
   uint64_t* bars = (uint64_t*)(B_s + NSTAGE * 3 * nkb * B_BOX);
@@ -171,7 +173,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
     // ------------------------------------------------ MMA issuer
     const uint32_t idesc = tc::idesc_bf16(TM, TN);
     uint32_t cB = 0, ct = 0, n = 0;
-    const int ksteps = nkb * 4;  // 16-element K steps per slice
+    // Descriptors of the box starts: the start-address field holds (address >> 4) in its low
+    // 14 bits and shared-memory addresses stay below 2^18, so a descriptor for
+    // base + offset is the base descriptor plus offset >> 4 (no carry).
+    const uint64_t dA = tc::desc_sw128(tc::smem_u32(A_s));
+    const uint64_t dB0 = tc::desc_sw128(tc::smem_u32(B_s)), dB1 = tc::desc_sw128(tc::smem_u32(B_s + 3 * nkb * B_BOX));
     for (int it = blockIdx.x; it < P.nitems && !*abort_s; it += gridDim.x, n++) {
       const int jc = it % P.njc;
       const int j0 = jc * P.jchunk, j1 = min(P.nj, j0 + P.jchunk);
@@ -184,16 +190,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
         }
         tc::fence_after_sync();
         const uint32_t dbase = tmem + tb * TBUF;
-        uint32_t first = 0x1F;
+        const uint64_t dBs = s ? dB1 : dB0;
+        // slice pairs ordered so that each accumulator's first MMA clears it
+#pragma unroll
         for (int a = 0; a < 3; a++)
+#pragma unroll
           for (int b = 0; b < 3; b++) {
             const int d = a + b;
-            for (int kk = 0; kk < ksteps; kk++) {
+            const bool first_of_d = (a == 0) || (b == 2);  // (0,b) opens d <= 2; (a,2) opens d = 3, 4
+#pragma unroll
+            for (int kk = 0; kk < nkb * 4; kk++) {
               const int kb = kk >> 2, ko = (kk & 3) * 32;
-              const uint64_t ad = tc::desc_sw128(tc::smem_u32(A_s + (a * nkb + kb) * A_BOX) + ko);
-              const uint64_t bd = tc::desc_sw128(tc::smem_u32(B_s + (s * 3 * nkb + b * nkb + kb) * B_BOX) + ko);
-              tc::mma_bf16(dbase + d * TN, ad, bd, idesc, (first >> d) & 1 ? 0u : 1u);
-              first &= ~(1u << d);
+              const uint64_t ad = dA + (uint64_t)((((a * nkb + kb) * A_BOX) + ko) >> 4);
+              const uint64_t bd = dBs + (uint64_t)((((b * nkb + kb) * B_BOX) + ko) >> 4);
+              tc::mma_bf16(dbase + d * TN, ad, bd, idesc, (first_of_d && kk == 0) ? 0u : 1u);
             }
           }
         tc::mma_commit(b_empty + s);
@@ -203,7 +213,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
     }
   } else if (warp >= 4) {
     // ------------------------------------------------ epilogue
-    const int q = warp & 3, h = (warp - 4) >> 2;
+    const int q = warp & 3, h = (warp - 4) >> 2;  // lane quadrant, column third
     const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
     // Every epilogue warp walks the same items and reaches the two named-barrier syncs per
     // item the same number of times; after an abort it only skips the work.
@@ -215,6 +225,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
       const bool irow = i < P.NA;
       const float2 aff = irow ? P.alpha_ff[i] : make_float2(0.f, 0.f);
       const int ei = irow ? P.ea[i] : PD_EMIN;
+      const float pa = pow2f(ei);  // 2^ei
       for (int jt = j0; jt < j1; jt++, ct++) {
         const uint32_t tb = ct & 1, tu = ct >> 1;
         if (*abort_s) break;
@@ -223,13 +234,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
           break;
         }
         tc::fence_after_sync();
-        // this warp's 24 columns: lane c < 24 holds column h*24 + c (broadcast by shuffles)
-        const int jl = jt * TN + h * 24 + lane;
-        const bool lok = lane < 24 && jl < P.NB;
+        // this warp's 16 columns: lane c < 16 holds column h*16 + c (broadcast by shuffles)
+        const int jl = jt * TN + h * 16 + lane;
+        const bool lok = lane < 16 && jl < P.NB;
         const float2 bl = lok ? __ldg(P.beta_ff + jl) : make_float2(0.f, 0.f);
         const int el = lok ? __ldg(P.eb + jl) : PD_EMIN;
-        for (int ch = 0; ch < 3; ch++) {
-          const int col0 = h * 24 + ch * 8;
+        const float pl = pow2f(el + 33);  // 2^(ej+33): 2 x 2^(ei+ej) x 2^32 for the top diagonal
+        for (int ch = 0; ch < 2; ch++) {
+          const int col0 = h * 16 + ch * 8;
           uint32_t r0[8], r1[8], r2[8], r3[8], r4[8];
           const uint32_t ta = tmem + tb * TBUF + lane_addr + col0;
           tc::tmem_ld8(ta, r0);
@@ -242,27 +254,34 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
           for (int c = 0; c < 8; c++) {
             const int src = ch * 8 + c;
             const float2 bff = make_float2(__shfl_sync(0xffffffffu, bl.x, src), __shfl_sync(0xffffffffu, bl.y, src));
-            const int ej = __shfl_sync(0xffffffffu, el, src);
+            const float pb = __shfl_sync(0xffffffffu, pl, src);
             const int j = jt * TN + col0 + c;
             if (!irow || j >= P.NB) continue;
-            // 2 x 2^(ei+ej) = sum_d 2^(ei+ej+33-8d) X_d, each term an exact float
-            const float s0 = pow2f(ei + ej + 33);
-            const float u0 = __uint_as_float(r0[c]) * s0;
-            const float u1 = __uint_as_float(r1[c]) * (s0 * 0x1p-8f);
-            const float u2 = __uint_as_float(r2[c]) * (s0 * 0x1p-16f);
-            const float u3 = __uint_as_float(r3[c]) * (s0 * 0x1p-24f);
-            const float u4 = __uint_as_float(r4[c]) * (s0 * 0x1p-32f);
-            const float chi2 = chi2_assemble(aff, bff, u0, u1, u2, u3, u4);
-            // below this the float-float rounding (about 2^-40 of the norms) could exceed
-            // 1e-5 relative; matrix mode: the quantisation-error bound
-            float bound = 1e-7f * (aff.x + bff.x);
+            // 2 x 2^(ei+ej) = sum_d 2^(ei+ej+33-8d) X_d; s0 = 2^(ei+ej+33) is an exact product
+            const float s0 = pa * pb;
+            const float ab = aff.x + bff.x;
+            const float X0 = __uint_as_float(r0[c]), X1 = __uint_as_float(r1[c]);
+            const float X2 = __uint_as_float(r2[c]), X3 = __uint_as_float(r3[c]);
+            // fast FP32 assembly (rounding below 2^-22 (|P|^2+|Q|^2); the left-out X4 term
+            // below 2^-30 of it): within 1e-6 of chi2 whenever chi2 >= (|P|^2+|Q|^2)/4,
+            // otherwise the float-float form
+            const float v = fmaf(X1, 0x1p-8f, X0);
+            const float w = fmaf(X3, 0x1p-24f, X2 * 0x1p-16f);
+            float chi2 = fmaf(-v, s0, ab) + fmaf(-w, s0, aff.y + bff.y);
+            if (chi2 < 0.25f * ab) {
+              chi2 = chi2_assemble(aff, bff, X0 * s0, X1 * (s0 * 0x1p-8f), X2 * (s0 * 0x1p-16f),
+                                   X3 * (s0 * 0x1p-24f), __uint_as_float(r4[c]) * (s0 * 0x1p-32f));
+            }
+            // below 1e-7 (|P|^2+|Q|^2) the float-float rounding (about 2^-40 of it) could
+            // exceed 1e-5 relative; matrix mode adds the quantisation-error bound
+            float bound = fmaxf(1e-7f * ab, P.thr);
             if (P.out) {
-              const float q = pow2f(ei) + pow2f(ej);
+              const float q = pa + pb * 0x1p-33f;
               bound = fmaxf(bound, P.refine_f * q * q);
             }
             // top-k candidates and near-zero pairs go to the exact FP64 list (which also
             // histograms them); every other pair is histogrammed here
-            if (chi2 < bound || chi2 < P.thr) {
+            if (chi2 < bound) {
               const unsigned k = atomicAdd(P.nref, 1u);
               if (k < P.rcap) {
                 P.ri[k] = i;
@@ -281,7 +300,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
       }
       // flush this item's histogram (per item, so the 32-bit shared counters cannot overflow)
       epi_sync();
-      for (int b = threadIdx.x - 128; b < P.nbins; b += EPI_WARPS * 32) {
+      for (int b = (int)threadIdx.x - 128; b < P.nbins; b += EPI_WARPS * 32) {
         const uint32_t v = hist_s[b];
         if (v) {
           atomicAdd(P.hist + b, (unsigned long long)v);
@@ -455,8 +474,8 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
 
   // ---- top-k threshold from a sample of pairs
   const unsigned cap = (unsigned)std::min<long long>(P, 8LL * k + (1LL << 20));
-  double thr = INFINITY;
-  if (k > 0 && P > (long long)cap) {
+  double thr = -1.0;  // no candidates unless k > 0
+  if (k > 0) {
     const long S = 1L << 22;
     uint64_t* sk = (uint64_t*)ws_get(ctx, WS_LOC, (sizeof(uint64_t) + sizeof(uint32_t)) * S);
     uint32_t* sv = (uint32_t*)(sk + S);
@@ -527,7 +546,9 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
   prm.out = out;
   prm.err = (int*)(counters + 2);
   const size_t smem = smem_bytes(nkb, nbins);
-  set_max_smem((const void*)k_pairdiff_tc, smem);
+  MLC_REQUIRE(nkb == 1 || nkb == 2, MLC_ERR_LIMIT, "tensor-core pair chi2 supports T <= 128 epochs");
+  auto kern = nkb == 1 ? k_pairdiff_tc<1> : k_pairdiff_tc<2>;
+  set_max_smem((const void*)kern, smem);
   const int grid = std::min(grid_max, prm.nitems);
   // plain form: FP64 chi2 of row chunks, then histogram / candidates of each chunk
   double* wd = nullptr;
@@ -542,12 +563,12 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
 
   for (int pass = 0; pass < 4; pass++) {
     res.passes = pass + 1;
-    prm.thr = (float)std::min(thr, 3.0e38);
+    prm.thr = (float)std::min(thr, 3.0e38);  // -1: no candidates
     MLC_CUDA(cudaMemsetAsync(counters, 0, 16, ctx->stream));
     MLC_CUDA(cudaMemsetAsync(hist, 0, 8 * (size_t)nbins, ctx->stream));
     if (method == 1) {
       MLC_KSCOPE(ctx, "pairdiff_tc");
-      k_pairdiff_tc<<<grid, NTHREADS, smem, ctx->stream>>>(tmA, tmB, prm);
+      kern<<<grid, NTHREADS, smem, ctx->stream>>>(tmA, tmB, prm);
     } else {
       for (long r0 = 0; r0 < NA; r0 += rows_per_chunk) {
         const long nr = std::min<long>(rows_per_chunk, NA - r0);
@@ -597,7 +618,7 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
       continue;
     }
     if ((long long)hc[0] < std::min<long long>(k, P) && std::isfinite(thr)) {  // too few: raise it
-      thr = (hc[0] > 0 ? thr * 4.0 : thr * 16.0 + 1e-30);
+      thr = thr > 0 ? thr * (hc[0] > 0 ? 4.0 : 16.0) : 1e-30;
       if (pass == 2) thr = INFINITY;
       continue;
     }
