@@ -134,11 +134,13 @@ __device__ __forceinline__ void stockham_stage(const C2<T>* __restrict__ src, C2
 #pragma unroll
     for (int i = 0; i < R; i++) v[i] = src[(j + i * Lr) * CW + c];
     if (Ns > 1) {
-      const int kt = k * twstep;
+      // one table load per butterfly: W^k; the higher powers W^(ik) by multiplication
+      const C2<T> w1 = ldc(tw + k * twstep);
+      C2<T> w = w1;
 #pragma unroll
       for (int i = 1; i < R; i++) {
-        C2<T> w = ldc(tw + i * kt);
         v[i] = INV ? cmulc(v[i], w) : cmul(v[i], w);
+        if (i + 1 < R) w = cmul(w, w1);
       }
     }
     Dft<T, R, INV>::run(v);
