@@ -174,6 +174,57 @@ int mlc_sample_tracks_interleaved(mlc_ctx* ctx, const void* imap, int stride, in
                                   int precision, int ntracks, const void* x0, const void* y0, const void* phi,
                                   const void* v, const int64_t* off, const void* t, int mag, void* out);
 
+/* ======================================================================= whole step, one call */
+
+/* Straight tracks as in mlc_sample_tracks: start x0, y0 (pixels), angle phi (radians),
+ * speed v (pixels per day), epoch offsets off[ntracks + 1] (off[0] = 0) and epochs
+ * t[nepochs] (days, nepochs = off[ntracks]).  x0, y0, phi, v and t have the map's
+ * precision. */
+typedef struct {
+  int ntracks;
+  int64_t nepochs;
+  const void* x0;
+  const void* y0;
+  const void* phi;
+  const void* v;
+  const int64_t* off;
+  const void* t;
+} mlc_tracks;
+
+#define MLC_IO_HOST 1 /* pixels, the track arrays and out are host memory */
+#define MLC_ASYNC 2   /* return once queued (see below) */
+
+/* The light-curve step of one lensed image in one call -- expanding_source
+ * (gpu_functions.cu:82-225) with straight tracks in place of fixed locations:
+ *   pixels (Ny x Nx, the map's precision; NULL keeps the map's current pixels and cached
+ *   spectrum) -> forward spectrum -> convolution with each of the nprof profiles
+ *   (mode MLC_CONV_*) -> bilinear sampling of every track at its epochs ->
+ *   out[q * nepochs + e] (q < nprof), magnitudes -2.5 log10(mu) when mag != 0.
+ * Without MLC_IO_HOST every array is device memory and everything runs on the context's
+ * stream.  With MLC_IO_HOST the uploads run on an internal host-to-device stream and the
+ * light curves come back in chunks of tracks on an internal device-to-host stream, each
+ * chunk's copy overlapping the sampling of the next; host buffers should be page-locked
+ * (cudaHostAlloc / cudaHostRegister) for the copies to overlap.
+ * The call returns when out holds the result, unless MLC_ASYNC is given: then it returns
+ * once the work is queued, the caller keeps pixels, the tracks and out untouched until
+ * mlc_ctx_synchronize (or mlc_ctx_join + a sync of its stream), and the next call's
+ * uploads and convolutions overlap this call's copies back.  Device memory held: the
+ * group's convolved maps and their interleaved copy (2 x min(nprof,16) maps), two track
+ * buffers and an output ring of about twice one call's light curves (4 to 64 chunks). */
+int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof,
+                               const mlc_profile* profiles_host, const mlc_tracks* tracks, int mode,
+                               int mag, void* out, int flags);
+
+/* Makes the context's stream wait (on the device, without blocking the host) for all
+ * copies queued by MLC_IO_HOST calls, so that an event recorded on the stream afterwards
+ * covers them. */
+int mlc_ctx_join(mlc_ctx* ctx);
+
+/* Bytes of one output chunk of MLC_IO_HOST calls (default 256 MiB; 4 to 64 chunks are held
+ * on the device).  Smaller chunks start the download sooner; every track's light curves
+ * (min(nprof,16) x its epochs) must fit in one.  Waits for the context's queued work. */
+int mlc_ctx_set_chunk_bytes(mlc_ctx* ctx, size_t bytes);
+
 /* ======================================================================= chi2 vs one observed curve */
 
 /* Offset-minimised chi2 of ncurves magnitude curves of T epochs (m, row-major, the

@@ -24,6 +24,14 @@ class MlcProfile(C.Structure):
                 ("u", C.c_double)]
 
 
+class MlcTracks(C.Structure):
+    _fields_ = [("ntracks", C.c_int), ("nepochs", C.c_int64), ("x0", C.c_void_p), ("y0", C.c_void_p),
+                ("phi", C.c_void_p), ("v", C.c_void_p), ("off", C.c_void_p), ("t", C.c_void_p)]
+
+
+MLC_IO_HOST, MLC_ASYNC = 1, 2
+
+
 class MlcPairStats(C.Structure):
     _fields_ = [("delta", C.c_double), ("threshold", C.c_double), ("refined", C.c_longlong),
                 ("candidates", C.c_longlong), ("passes", C.c_int)]
@@ -67,6 +75,10 @@ SIGNATURES = {
     "mlc_sample_tracks": (i32, [vp, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
     "mlc_chi2_offset": (i32, [vp, i32, i32, i32, vp, vp, vp, vp, vp]),
     "mlc_interleave_maps": (i32, [vp, vp, i32, i32, i32, i32, i32, vp]),
+    "mlc_convolve_sample_tracks": (i32, [vp, vp, vp, i32, C.POINTER(MlcProfile), C.POINTER(MlcTracks), i32, i32, vp,
+                                         i32]),
+    "mlc_ctx_join": (i32, [vp]),
+    "mlc_ctx_set_chunk_bytes": (i32, [vp, C.c_size_t]),
     "mlc_sample_tracks_interleaved": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
     "mlc_pair_setup": (i32, [vp, i32, i32, vp, vp, i32, vp, vp, vp, vp]),
     "mlc_pair_chi2_ratio": (i32, [vp, i32, vp, vp, vp, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]),

@@ -62,6 +62,14 @@ class Context:
     def synchronize(self):
         self.check(self.L.mlc_ctx_synchronize(self.h))
 
+    def join(self):
+        """Make the context's stream wait (on the device) for the copies of host-buffer calls."""
+        self.check(self.L.mlc_ctx_join(self.h))
+
+    def set_chunk_bytes(self, nbytes: int):
+        """Output chunk size of host-buffer convolve_sample_tracks calls."""
+        self.check(self.L.mlc_ctx_set_chunk_bytes(self.h, int(nbytes)))
+
     def workspace_bytes(self) -> int:
         return int(self.L.mlc_ctx_workspace_bytes(self.h))
 
@@ -241,6 +249,59 @@ def sample_tracks_interleaved(ctx: Context, imap: torch.Tensor, nmaps: int, x0, 
     ctx.check(ctx.L.mlc_sample_tracks_interleaved(ctx.h, _ptr(imap), stride, nmaps, Nx, Ny, _PREC[dt], x0.numel(),
                                                   _ptr(x0), _ptr(y0), _ptr(phi), _ptr(v), _ptr(off), _ptr(t),
                                                   int(mag), _ptr(out)))
+    return out
+
+
+TRACK_KEYS = ("x0", "y0", "phi", "v", "off", "t")
+
+
+def convolve_sample_tracks(ctx: Context, m: Map, profiles, tracks: dict, mag=True, pixels=None, out=None,
+                           mode="fused", async_=False):
+    """The light-curve step of one image in one library call (mlc_convolve_sample_tracks).
+
+    tracks: dict of x0, y0, phi, v (map precision), off (int64, ntracks + 1) and t (map
+    precision), either all CUDA tensors (device buffers, everything on the context's
+    stream) or all CPU tensors / numpy arrays (host buffers: copies overlap the kernels;
+    page-locked tensors let them run asynchronously).  pixels: new map pixels (same
+    location as the tracks) or None to keep the map's.  Returns out[nprof, nepochs].
+    With async_=True the call returns once queued; host results are valid after
+    ctx.synchronize().
+    """
+    tr = {k: tracks[k] for k in TRACK_KEYS}
+    first = tr["x0"]
+    host = not (isinstance(first, torch.Tensor) and first.is_cuda)
+    for k, a in tr.items():
+        is_dev = isinstance(a, torch.Tensor) and a.is_cuda
+        if is_dev == host:
+            raise ValueError("track arrays must all be on the device or all on the host")
+        want = np.int64 if k == "off" else (np.float64 if m.prec == MLC_F64 else np.float32)
+        dt = torch.int64 if k == "off" else m.dtype
+        if isinstance(a, torch.Tensor):
+            if a.dtype != dt or not a.is_contiguous():
+                raise ValueError(f"tracks[{k!r}] must be a contiguous {dt} tensor")
+        elif isinstance(a, np.ndarray):
+            if a.dtype != want or not a.flags.c_contiguous:
+                raise ValueError(f"tracks[{k!r}] must be a contiguous {want} array")
+        else:
+            raise TypeError(type(a))
+    off = tr["off"]
+    ntr = int(off.shape[0]) - 1
+    if host:
+        E = int(off[-1])
+    else:
+        E = int(tr["t"].shape[0])
+    nprof = len(profiles)
+    if out is None:
+        if host:
+            out = torch.empty((nprof, E), dtype=m.dtype, pin_memory=torch.cuda.is_available())
+        else:
+            out = torch.empty((nprof, E), dtype=m.dtype, device=first.device)
+    flags = (_lib.MLC_IO_HOST if host else 0) | (_lib.MLC_ASYNC if async_ else 0)
+    T = _lib.MlcTracks(ntr, E, *[_ptr(tr[k]) for k in TRACK_KEYS])
+    P = (_lib.MlcProfile * nprof)(*profiles)
+    md = _MODES[mode]
+    ctx.check(ctx.L.mlc_convolve_sample_tracks(ctx.h, m.h, _ptr(pixels), nprof, P, C.byref(T), md, int(mag),
+                                               _ptr(out), flags))
     return out
 
 

@@ -12,10 +12,6 @@ namespace mlc {
 void sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx, int Ny, int prec,
                    int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
                    const int64_t* off, const void* t, int mag, void* out, long E);
-void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out);
-void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
-                      const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
-                      const void* t, int mag, void* out, long E);
 void chi2_offset(mlc_ctx* ctx, int prec, int ncurves, int T_, const void* m, const double* obs_dev,
                  const double* w_dev, double W, double* chi2, double* dm);
 void pair_setup(mlc_ctx* ctx, int Nloc, int Nprof, const double* LCA, const double* LCB, int Nbins,
@@ -114,6 +110,7 @@ int mlc_ctx_destroy(mlc_ctx* ctx) {
     cudaGetDevice(&prev);
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    batch_release(ctx);
     for (int i = 0; i < WS_NSLOTS; i++)
       if (ctx->ws_ptr[i]) cudaFree(ctx->ws_ptr[i]);
     ctx->plans.clear();
@@ -175,7 +172,10 @@ int mlc_ctx_set_stream(mlc_ctx* ctx, void* stream) {
 }
 
 int mlc_ctx_synchronize(mlc_ctx* ctx) {
-  return guarded(ctx, [&] { MLC_CUDA(cudaStreamSynchronize(ctx->stream)); });
+  return guarded(ctx, [&] {
+    MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+    batch_synchronize(ctx);
+  });
 }
 
 const char* mlc_ctx_last_error(const mlc_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
@@ -383,6 +383,31 @@ int mlc_interleave_maps(mlc_ctx* ctx, const void* const* maps_host, int nmaps, i
   return guarded(ctx, [&] { interleave(ctx, maps_host, nmaps, (long)Nx * Ny, precision, stride, out); });
 }
 
+int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof,
+                               const mlc_profile* profiles_host, const mlc_tracks* tracks, int mode, int mag, void* out,
+                               int flags) {
+  if (!ctx || !map || !profiles_host || !tracks) return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (nprof < 1) return fail(ctx, MLC_ERR_ARG, "need at least one profile");
+  if (mode != MLC_CONV_FUSED && mode != MLC_CONV_PLAIN) return fail(ctx, MLC_ERR_ARG, "unknown convolution mode");
+  if (flags & ~(MLC_IO_HOST | MLC_ASYNC)) return fail(ctx, MLC_ERR_ARG, "unknown flags");
+  const mlc_tracks& tr = *tracks;
+  if (tr.ntracks < 0 || tr.nepochs < 0) return fail(ctx, MLC_ERR_ARG, "negative track or epoch count");
+  if (tr.ntracks > 0 && (!tr.x0 || !tr.y0 || !tr.phi || !tr.v || !tr.off || (tr.nepochs > 0 && !tr.t) || !out))
+    return fail(ctx, MLC_ERR_ARG, "null track array or output");
+  if (map->device != ctx->device) return fail(ctx, MLC_ERR_ARG, "map lives on another device");
+  return guarded(ctx, [&] { convolve_sample_tracks(ctx, map, pixels, nprof, profiles_host, tr, mode, mag, out, flags); });
+}
+
+int mlc_ctx_join(mlc_ctx* ctx) {
+  return guarded(ctx, [&] { ctx_join(ctx); });
+}
+
+int mlc_ctx_set_chunk_bytes(mlc_ctx* ctx, size_t bytes) {
+  if (!ctx) return MLC_ERR_ARG;
+  if (bytes < 4096) return fail(ctx, MLC_ERR_ARG, "chunk must hold at least 4096 bytes");
+  return guarded(ctx, [&] { set_chunk_bytes(ctx, bytes); });
+}
+
 int mlc_sample_tracks_interleaved(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny,
                                   int precision, int ntracks, const void* x0, const void* y0, const void* phi,
                                   const void* v, const int64_t* off, const void* t, int mag, void* out) {
@@ -396,7 +421,8 @@ int mlc_sample_tracks_interleaved(mlc_ctx* ctx, const void* imap, int stride, in
       MLC_CUDA(cudaMemcpyAsync(&E, off + ntracks, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
       MLC_CUDA(cudaStreamSynchronize(ctx->stream));
     }
-    sample_tracks_il(ctx, imap, stride, nmaps, Nx, Ny, precision, ntracks, x0, y0, phi, v, off, t, mag, out, (long)E);
+    sample_tracks_il(ctx, imap, stride, nmaps, Nx, Ny, precision, ntracks, x0, y0, phi, v, off, t, mag, out, (long)E,
+                     0);
   });
 }
 

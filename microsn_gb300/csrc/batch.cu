@@ -1,0 +1,339 @@
+// The light-curve step of one lensed image through one call (mlc_convolve_sample_tracks):
+// map upload, forward spectrum, convolution with every profile, interleave, track
+// sampling and the download of the light curves.
+//
+// Replaces expanding_source (simulating_lcurves/src/gpu_functions.cu:82-225), which per
+// profile builds the kernel on the host, uploads it, transforms, multiplies, transforms
+// back, samples and synchronises.  Here every kernel runs on the context's stream and,
+// with host buffers, the copies run on two internal streams:
+//
+//   h2d stream   pixels of call i+1 (once call i's forward transform has read the
+//                map), tracks of call i+1 (double-buffered by call parity)
+//   compute      profiles upload, forward spectrum, convolutions, interleave, sampling
+//                of one chunk of tracks at a time into a ring of output slots
+//   d2h stream   each filled slot back to the caller's buffer while the next chunk is
+//                sampled; the slot is reused once its copy has run
+//
+// so that, with MLC_ASYNC, one call's download overlaps the next call's convolutions.
+#include <algorithm>
+#include <atomic>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+#include "mlc_internal.h"
+
+namespace mlc {
+
+struct BatchIO {
+  // Output ring: enough slots for about two calls' light curves (4 to 64 slots), so that
+  // the sampling of one call never waits for its own downloads and the next call's
+  // kernels start while this call's chunks are still being copied back.
+  static constexpr int NRING = 64;
+  int nring = 4;                     // slots in use (grow-only)
+  size_t slot_bytes = 256ull << 20;  // one output chunk
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t pix_free = nullptr;  // compute: the forward transform has read the map pixels
+  cudaEvent_t pix_in = nullptr;    // h2d: pixels uploaded
+  cudaEvent_t h2d_last = nullptr, d2h_last = nullptr;
+  void* ring[NRING] = {};
+  size_t ring_cap[NRING] = {};
+  cudaEvent_t ring_full[NRING] = {}, ring_free[NRING] = {};
+  int ring_pos = 0;
+  void* trk[2] = {};
+  size_t trk_cap[2] = {};
+  cudaEvent_t trk_in[2] = {}, trk_free[2] = {};
+  double* prof_host[2] = {};
+  size_t prof_cap[2] = {};
+  cudaEvent_t prof_sent[2] = {};
+  int parity = 0;
+};
+
+static void ev_create(cudaEvent_t* e) { MLC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming)); }
+
+static BatchIO* batch_get(mlc_ctx* ctx) {
+  if (ctx->batch) return ctx->batch;
+  BatchIO* b = new BatchIO();
+  ctx->batch = b;  // released by batch_release even if a creation below fails
+  MLC_CUDA(cudaStreamCreateWithFlags(&b->h2d, cudaStreamNonBlocking));
+  MLC_CUDA(cudaStreamCreateWithFlags(&b->d2h, cudaStreamNonBlocking));
+  ev_create(&b->pix_free);
+  ev_create(&b->pix_in);
+  ev_create(&b->h2d_last);
+  ev_create(&b->d2h_last);
+  for (int i = 0; i < BatchIO::NRING; i++) {
+    ev_create(&b->ring_full[i]);
+    ev_create(&b->ring_free[i]);
+  }
+  for (int i = 0; i < 2; i++) {
+    ev_create(&b->trk_in[i]);
+    ev_create(&b->trk_free[i]);
+    ev_create(&b->prof_sent[i]);
+  }
+  return b;
+}
+
+static void sync_all(mlc_ctx* ctx, BatchIO* b) {
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(b->h2d));
+  MLC_CUDA(cudaStreamSynchronize(b->d2h));
+}
+
+void batch_synchronize(mlc_ctx* ctx) {
+  BatchIO* b = ctx->batch;
+  if (!b) return;
+  if (b->h2d) MLC_CUDA(cudaStreamSynchronize(b->h2d));
+  if (b->d2h) MLC_CUDA(cudaStreamSynchronize(b->d2h));
+}
+
+void batch_release(mlc_ctx* ctx) {
+  BatchIO* b = ctx->batch;
+  if (!b) return;
+  if (b->h2d) cudaStreamSynchronize(b->h2d);
+  if (b->d2h) cudaStreamSynchronize(b->d2h);
+  for (int i = 0; i < BatchIO::NRING; i++) {
+    if (b->ring[i]) cudaFree(b->ring[i]);
+    if (b->ring_full[i]) cudaEventDestroy(b->ring_full[i]);
+    if (b->ring_free[i]) cudaEventDestroy(b->ring_free[i]);
+  }
+  for (int i = 0; i < 2; i++) {
+    if (b->trk[i]) cudaFree(b->trk[i]);
+    if (b->prof_host[i]) cudaFreeHost(b->prof_host[i]);
+    for (cudaEvent_t e : {b->trk_in[i], b->trk_free[i], b->prof_sent[i]})
+      if (e) cudaEventDestroy(e);
+  }
+  for (cudaEvent_t e : {b->pix_free, b->pix_in, b->h2d_last, b->d2h_last})
+    if (e) cudaEventDestroy(e);
+  if (b->h2d) cudaStreamDestroy(b->h2d);
+  if (b->d2h) cudaStreamDestroy(b->d2h);
+  delete b;
+  ctx->batch = nullptr;
+}
+
+// Device buffer that may still be in use by queued work on any of the three streams.
+static void* grow_dev(mlc_ctx* ctx, BatchIO* b, void*& p, size_t& cap, size_t need) {
+  if (cap >= need) return p;
+  sync_all(ctx, b);
+  if (p) MLC_CUDA(cudaFree(p));
+  p = nullptr;
+  cap = 0;
+  const size_t sz = (size_t)round_up((long)need, 1 << 20);
+  MLC_CUDA(cudaMalloc(&p, sz));
+  cap = sz;
+  return p;
+}
+
+static int pow2_at_least(int n) {
+  int s = 1;
+  while (s < n) s <<= 1;
+  return s;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+template <typename T>
+static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const mlc_profile* profs,
+                const mlc_tracks& tr, int mode, int mag, void* out, int flags) {
+  const bool host = (flags & MLC_IO_HOST) != 0;
+  const size_t es = sizeof(T);
+  const int Nx = map->Nx, Ny = map->Ny;
+  const long npix = (long)Nx * Ny;
+  FftPlan2D* p = plan_get(ctx, Nx, Ny, map->prec);
+  BatchIO* b = batch_get(ctx);
+  const int par = b->parity;
+  b->parity ^= 1;
+  const int ntr = tr.ntracks;
+  const int64_t E = tr.nepochs;
+
+  // ---- profiles: all rasters into page-locked staging, one upload on the compute stream
+  std::vector<int> pN(nprof);
+  std::vector<size_t> poff(nprof + 1, 0);
+  for (int k = 0; k < nprof; k++) {
+    pN[k] = profile_dims(profs[k]);
+    MLC_REQUIRE(pN[k] > 0, MLC_ERR_ARG, "invalid profile parameters");
+    MLC_REQUIRE(pN[k] <= Nx && pN[k] <= Ny, MLC_ERR_LIMIT, "profile raster larger than the map");
+    poff[k + 1] = poff[k] + (size_t)pN[k] * pN[k];
+  }
+  const size_t pbytes = poff[nprof] * sizeof(double);
+  MLC_CUDA(cudaEventSynchronize(b->prof_sent[par]));  // the last upload from this staging buffer has run
+  if (b->prof_cap[par] < pbytes) {
+    if (b->prof_host[par]) MLC_CUDA(cudaFreeHost(b->prof_host[par]));
+    b->prof_host[par] = nullptr;
+    b->prof_cap[par] = 0;
+    MLC_CUDA(cudaMallocHost((void**)&b->prof_host[par], pbytes));
+    b->prof_cap[par] = pbytes;
+  }
+  {
+    // rasters on host threads, largest first (they take milliseconds each, and the
+    // previous call's kernels are still running meanwhile)
+    std::vector<int> order(nprof);
+    std::iota(order.begin(), order.end(), 0);
+    std::sort(order.begin(), order.end(), [&](int a, int c) { return pN[a] > pN[c]; });
+    std::atomic<int> next{0}, bad{0};
+    auto work = [&] {
+      for (int i = next++; i < nprof; i = next++) {
+        const int k = order[i];
+        if (profile_raster(profs[k], b->prof_host[par] + poff[k], (long)(poff[k + 1] - poff[k])) != pN[k]) bad = 1;
+      }
+    };
+    const int nth = std::max(1, std::min<int>(nprof, (int)std::thread::hardware_concurrency()) - 1);
+    std::vector<std::thread> pool;
+    for (int i = 0; i < nth; i++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    MLC_REQUIRE(!bad, MLC_ERR_ARG, "profile raster failed");
+  }
+  double* dprof = (double*)ws_get(ctx, WS_PROFILE, pbytes);
+  MLC_CUDA(cudaMemcpyAsync(dprof, b->prof_host[par], pbytes, cudaMemcpyHostToDevice, ctx->stream));
+  MLC_CUDA(cudaEventRecord(b->prof_sent[par], ctx->stream));
+
+  // ---- map pixels and forward spectrum
+  if (pixels) {
+    if (host) {
+      MLC_CUDA(cudaStreamWaitEvent(b->h2d, b->pix_free, 0));
+      MLC_CUDA(cudaMemcpyAsync(map->data, pixels, npix * es, cudaMemcpyHostToDevice, b->h2d));
+      MLC_CUDA(cudaEventRecord(b->pix_in, b->h2d));
+      MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->pix_in, 0));
+    } else if (pixels != map->data) {
+      MLC_CUDA(cudaMemcpyAsync(map->data, pixels, npix * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    map->spec_valid = false;
+  }
+  if (!map->spec_valid) {
+    if (!map->spec) MLC_CUDA(cudaMalloc(&map->spec, p->spec_bytes()));
+    fft2_forward(ctx, *p, map->data, map->prec, map->spec);
+    map->spec_valid = true;
+  }
+  MLC_CUDA(cudaEventRecord(b->pix_free, ctx->stream));
+
+  // ---- tracks
+  const char* x0 = (const char*)tr.x0;
+  const char* y0 = (const char*)tr.y0;
+  const char* phi = (const char*)tr.phi;
+  const char* v = (const char*)tr.v;
+  const int64_t* off = tr.off;  // host offsets with MLC_IO_HOST, else device
+  const int64_t* doff = tr.off;  // device offsets
+  const char* t = (const char*)tr.t;
+  std::vector<std::pair<int, int>> chunks;  // track ranges of the output chunks (host IO)
+  const int nm_max = std::min(nprof, 16);
+  if (host && ntr > 0) {
+    MLC_REQUIRE(off[0] == 0 && off[ntr] == E, MLC_ERR_ARG, "track offsets must run from 0 to nepochs");
+    const size_t sp = align256(ntr * es), so = align256((ntr + 1) * sizeof(int64_t)), st = align256(E * es);
+    char* d = (char*)grow_dev(ctx, b, b->trk[par], b->trk_cap[par], 4 * sp + so + st);
+    // the buffer of this parity is free once the sampling two calls back has finished
+    MLC_CUDA(cudaStreamWaitEvent(b->h2d, b->trk_free[par], 0));
+    MLC_CUDA(cudaMemcpyAsync(d, x0, ntr * es, cudaMemcpyHostToDevice, b->h2d));
+    MLC_CUDA(cudaMemcpyAsync(d + sp, y0, ntr * es, cudaMemcpyHostToDevice, b->h2d));
+    MLC_CUDA(cudaMemcpyAsync(d + 2 * sp, phi, ntr * es, cudaMemcpyHostToDevice, b->h2d));
+    MLC_CUDA(cudaMemcpyAsync(d + 3 * sp, v, ntr * es, cudaMemcpyHostToDevice, b->h2d));
+    MLC_CUDA(cudaMemcpyAsync(d + 4 * sp, off, (ntr + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, b->h2d));
+    MLC_CUDA(cudaMemcpyAsync(d + 4 * sp + so, t, E * es, cudaMemcpyHostToDevice, b->h2d));
+    MLC_CUDA(cudaEventRecord(b->trk_in[par], b->h2d));
+    // chunks of whole tracks whose light curves fill at most one ring slot
+    const int64_t cap_e = (int64_t)(b->slot_bytes / ((size_t)nm_max * es));
+    for (int t0 = 0; t0 < ntr;) {
+      MLC_REQUIRE(off[t0 + 1] - off[t0] <= cap_e, MLC_ERR_LIMIT, "one track has more epochs than an output chunk holds");
+      const int64_t* lim = std::upper_bound(off + t0 + 1, off + ntr + 1, off[t0] + cap_e);
+      const int t1 = (int)(lim - off) - 1;  // last offset within the cap
+      chunks.emplace_back(t0, t1);
+      t0 = t1;
+    }
+    const size_t call_bytes = (size_t)nprof * E * es;
+    const long want = 2 * (long)((call_bytes + b->slot_bytes - 1) / b->slot_bytes);
+    const int nring = (int)std::max<long>(b->nring, std::min<long>(BatchIO::NRING, std::max(4L, want)));
+    if (nring != b->nring) {
+      sync_all(ctx, b);
+      b->nring = nring;
+      b->ring_pos = 0;
+    }
+    for (int i = 0; i < b->nring; i++) grow_dev(ctx, b, b->ring[i], b->ring_cap[i], b->slot_bytes);
+    x0 = d;
+    y0 = d + sp;
+    phi = d + 2 * sp;
+    v = d + 3 * sp;
+    doff = (const int64_t*)(d + 4 * sp);
+    t = d + 4 * sp + so;
+  }
+
+  // ---- profile groups of up to 16: convolve, interleave, sample
+  char* maps = (char*)ws_get(ctx, WS_BATCH_MAPS, (size_t)nm_max * npix * es);
+  void* imap = ntr > 0 ? ws_get(ctx, WS_BATCH_IMAP, (size_t)pow2_at_least(nm_max) * npix * es) : nullptr;
+  bool tracks_ready = false;
+  for (int g0 = 0; g0 < nprof; g0 += 16) {
+    const int nm = std::min(16, nprof - g0);
+    const int stride = pow2_at_least(nm);
+    const void* mp[16];
+    for (int q = 0; q < nm; q++) {
+      mp[q] = maps + (size_t)q * npix * es;
+      const double* pr = dprof + poff[g0 + q];
+      if (mode == MLC_CONV_FUSED) conv_fused(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+      else conv_plain(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+    }
+    if (ntr == 0) continue;
+    interleave(ctx, mp, nm, npix, map->prec, stride, imap);
+    if (!host) {
+      sample_tracks_il(ctx, imap, stride, nm, Nx, Ny, map->prec, ntr, x0, y0, phi, v, off, t, mag,
+                       (char*)out + (size_t)g0 * E * es, (long)E, 0);
+      continue;
+    }
+    if (!tracks_ready) {
+      MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->trk_in[par], 0));
+      tracks_ready = true;
+    }
+    for (const auto& c : chunks) {
+      const int t0 = c.first, t1 = c.second;
+      const int64_t e0 = off[t0], Ec = off[t1] - off[t0];
+      if (Ec == 0) continue;
+      const int s = b->ring_pos++ % b->nring;
+      MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->ring_free[s], 0));
+      sample_tracks_il(ctx, imap, stride, nm, Nx, Ny, map->prec, t1 - t0, x0 + t0 * es, y0 + t0 * es,
+                       phi + t0 * es, v + t0 * es, doff + t0, t, mag, b->ring[s], (long)Ec, e0);
+      MLC_CUDA(cudaEventRecord(b->ring_full[s], ctx->stream));
+      MLC_CUDA(cudaStreamWaitEvent(b->d2h, b->ring_full[s], 0));
+      char* dst = (char*)out + ((size_t)g0 * E + e0) * es;
+      if ((size_t)E * es < (1ull << 30)) {
+        MLC_CUDA(cudaMemcpy2DAsync(dst, E * es, b->ring[s], Ec * es, Ec * es, nm, cudaMemcpyDeviceToHost, b->d2h));
+      } else {
+        for (int q = 0; q < nm; q++)
+          MLC_CUDA(cudaMemcpyAsync(dst + (size_t)q * E * es, (const char*)b->ring[s] + (size_t)q * Ec * es, Ec * es,
+                                   cudaMemcpyDeviceToHost, b->d2h));
+      }
+      MLC_CUDA(cudaEventRecord(b->ring_free[s], b->d2h));
+    }
+  }
+  if (host) {
+    if (ntr > 0) MLC_CUDA(cudaEventRecord(b->trk_free[par], ctx->stream));
+    MLC_CUDA(cudaEventRecord(b->h2d_last, b->h2d));
+    MLC_CUDA(cudaEventRecord(b->d2h_last, b->d2h));
+  }
+  if (!(flags & MLC_ASYNC)) sync_all(ctx, b);
+}
+
+void convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const mlc_profile* profs,
+                            const mlc_tracks& tr, int mode, int mag, void* out, int flags) {
+  if (map->prec == MLC_F64) run<double>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags);
+  else run<float>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags);
+}
+
+void ctx_join(mlc_ctx* ctx) {
+  BatchIO* b = ctx->batch;
+  if (!b) return;
+  MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->h2d_last, 0));
+  MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->d2h_last, 0));
+}
+
+void set_chunk_bytes(mlc_ctx* ctx, size_t bytes) {
+  BatchIO* b = batch_get(ctx);
+  if (b->slot_bytes == bytes) return;
+  sync_all(ctx, b);
+  for (int i = 0; i < BatchIO::NRING; i++) {
+    if (b->ring[i]) MLC_CUDA(cudaFree(b->ring[i]));
+    b->ring[i] = nullptr;
+    b->ring_cap[i] = 0;
+  }
+  b->slot_bytes = bytes;
+  b->nring = 4;
+  b->ring_pos = 0;
+}
+
+}  // namespace mlc

@@ -44,9 +44,21 @@ enum WsSlot {
   WS_SMALL,
   WS_LOC,
   WS_PAIR_CAND,  // pair-stage candidates, refinement list, counters, histogram
+  WS_BATCH_MAPS,  // convolved maps of one profile group (mlc_convolve_sample_tracks)
+  WS_BATCH_IMAP,  // their profile-interleaved copy
   WS_NSLOTS
 };
 
+}  // namespace mlc
+
+namespace mlc {
+struct BatchIO;  // copy streams, ring and staging buffers of the whole-step entry (batch.cu)
+void batch_release(mlc_ctx* ctx);
+void batch_synchronize(mlc_ctx* ctx);
+void convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const mlc_profile* profs,
+                            const mlc_tracks& tr, int mode, int mag, void* out, int flags);
+void ctx_join(mlc_ctx* ctx);
+void set_chunk_bytes(mlc_ctx* ctx, size_t bytes);
 }  // namespace mlc
 
 struct mlc_ctx {
@@ -66,6 +78,7 @@ struct mlc_ctx {
   void* ws_ptr[mlc::WS_NSLOTS] = {};
   size_t ws_size[mlc::WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int>, std::unique_ptr<mlc::FftPlan2D>> plans;
+  mlc::BatchIO* batch = nullptr;
 };
 
 struct mlc_map {
@@ -133,6 +146,12 @@ int profile_dims(const mlc_profile& p);
 int profile_raster(const mlc_profile& p, double* out, long cap);
 
 // Sampling (sample.cu)
+void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out);
+// Interleaved-map track sampler: out[q * E + (e - ebase)] for the epochs e of the given
+// tracks (off holds global epoch indices; ebase lets a chunk of tracks fill its own buffer).
+void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
+                      const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
+                      const void* t, int mag, void* out, long E, int64_t ebase);
 void sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int Nprof, int Nloc, const int* lx,
                     const int* ly, double* LC, double* DLC);
 

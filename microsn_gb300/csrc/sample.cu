@@ -211,7 +211,8 @@ __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ 
                                                           const T* __restrict__ x0, const T* __restrict__ y0,
                                                           const T* __restrict__ phi, const T* __restrict__ v,
                                                           const int64_t* __restrict__ off, const T* __restrict__ t,
-                                                          int mag, T* __restrict__ out, long E, int nm_out) {
+                                                          int mag, T* __restrict__ out, long E, int nm_out,
+                                                          int64_t ebase) {
   const int lane = threadIdx.x & 31;
   const long track = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (track >= ntracks) return;
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ 
     }
 #pragma unroll
     for (int q = 0; q < NM; q++)
-      if (q < nm_out) out[(long)q * E + e] = mag ? (T)-2.5 * mlc_log10(acc[q]) : acc[q];
+      if (q < nm_out) out[(long)q * E + (e - ebase)] = mag ? (T)-2.5 * mlc_log10(acc[q]) : acc[q];
   }
 }
 
@@ -279,9 +280,9 @@ void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix
 template <typename T>
 static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int ntracks,
                            const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
-                           const void* t, int mag, void* out, long E) {
+                           const void* t, int mag, void* out, long E, int64_t ebase) {
   const int grid = ceil_div(ntracks, 8);
-#define MLC_IL_LAUNCH(NMV)                                                                                    k_sample_tracks_il<T, NMV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, Nx, Ny, ntracks, (const T*)x0,                                                              (const T*)y0, (const T*)phi, (const T*)v, off,                                                              (const T*)t, mag, (T*)out, E, nmaps)
+#define MLC_IL_LAUNCH(NMV)                                                                                    k_sample_tracks_il<T, NMV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, Nx, Ny, ntracks, (const T*)x0,                                                              (const T*)y0, (const T*)phi, (const T*)v, off,                                                              (const T*)t, mag, (T*)out, E, nmaps, ebase)
   MLC_KSCOPE(ctx, "sample_tracks_il");
   switch (stride) {
     case 1: MLC_IL_LAUNCH(1); break;
@@ -295,12 +296,12 @@ static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps
 
 void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
                       const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
-                      const void* t, int mag, void* out, long E) {
+                      const void* t, int mag, void* out, long E, int64_t ebase) {
   if (ntracks <= 0) return;
   if (prec == MLC_F64)
-    sample_il_impl<double>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E);
+    sample_il_impl<double>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E, ebase);
   else
-    sample_il_impl<float>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E);
+    sample_il_impl<float>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E, ebase);
   MLC_CHECK_LAUNCH();
 }
 

@@ -1,0 +1,195 @@
+"""The whole light-curve step in one call (mlc_convolve_sample_tracks) on the GPU.
+
+The call chains kernels that the other GPU tests check against the oracle (fused
+convolution, interleave, interleaved track sampler), so its output must equal, bit for
+bit, the same kernels called one at a time; host-buffer calls (chunked downloads, copy
+streams, asynchronous calls back to back) must equal device-buffer calls.  One FP64 case
+is also checked against the oracle directly.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from microsn_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda:0"
+
+
+def _profiles(n, pix=1.0):
+    import microsn_gb300 as mlc
+    shapes = ["uniform", "exponential", "gaussian", "limb_darkened"]
+    rh = [1.5, 3.0, 5.0, 8.0, 12.0]
+    out = []
+    for i in range(n):
+        out.append(mlc.profile(shapes[i % 4], rh[(i // 4) % 5] * pix, pix, ref_compat=False, u=0.6))
+    return out
+
+
+def _host_tracks(n, N, seed, dtype, epochs=(0, 40)):
+    x0, y0, phi, v, off, t = synth.tracks(n, N, 3.0, seed, epochs=epochs, v_range=(0.01, 0.3))
+    c = lambda a: np.ascontiguousarray(a, dtype)
+    return {"x0": c(x0), "y0": c(y0), "phi": c(phi), "v": c(v), "off": np.ascontiguousarray(off, np.int64),
+            "t": c(t)}
+
+
+def _pinned(tr):
+    out = {}
+    for k, a in tr.items():
+        x = torch.empty(a.shape, dtype=torch.from_numpy(a).dtype, pin_memory=True)
+        x.copy_(torch.from_numpy(a))
+        out[k] = x
+    return out
+
+
+def _device(tr):
+    return {k: torch.as_tensor(a, device=DEV) for k, a in tr.items()}
+
+
+@pytest.fixture(scope="module")
+def bctx(lib_built):
+    import microsn_gb300 as mlc
+    c = mlc.Context(0)
+    yield c
+    c.close()
+
+
+def _separate(ctx, m, profs, trd, mag):
+    """The same step with one library call per stage (planar sampler)."""
+    import microsn_gb300 as mlc
+    outs = []
+    for p in profs:
+        c = mlc.convolve(ctx, m, p, "fused")
+        o = mlc.sample_tracks(ctx, [c], m.Nx, m.Ny, trd["x0"], trd["y0"], trd["phi"], trd["v"], trd["off"],
+                              trd["t"], mag=mag)
+        outs.append(o[0])
+    return torch.stack(outs)
+
+
+@pytest.mark.parametrize("nprof", [1, 5, 20])
+def test_device_io_equals_separate_calls(bctx, nprof):
+    import microsn_gb300 as mlc
+    N = 360
+    mp = synth.lognormal_map(N, seed=21).astype(np.float32)
+    m = mlc.Map(bctx, mp, "f32")
+    profs = _profiles(nprof)
+    trd = _device(_host_tracks(700, N, 22, np.float32))
+    got = mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=True)
+    ref = _separate(bctx, m, profs, trd, True)
+    assert got.shape == ref.shape
+    assert torch.equal(got, ref)
+    m.close()
+
+
+def test_host_io_chunked_equals_device_io(bctx):
+    import microsn_gb300 as mlc
+    N = 300
+    mp = synth.lognormal_map(N, seed=31).astype(np.float32)
+    m = mlc.Map(bctx, mp, "f32")
+    profs = _profiles(18)  # two profile groups (16 + 2)
+    trh = _host_tracks(900, N, 32, np.float32)
+    ref = mlc.convolve_sample_tracks(bctx, m, profs, _device(trh), mag=True).cpu()
+    bctx.set_chunk_bytes(64 * 1024)  # 64 KiB: 1024 epochs of 16 profiles per chunk -> many chunks
+    try:
+        got_pinned = mlc.convolve_sample_tracks(bctx, m, profs, _pinned(trh), mag=True)
+        got_pageable = mlc.convolve_sample_tracks(bctx, m, profs, trh, mag=True,
+                                                  out=torch.empty(ref.shape, dtype=torch.float32))
+    finally:
+        bctx.set_chunk_bytes(256 << 20)
+    assert torch.equal(got_pinned, ref)
+    assert torch.equal(got_pageable, ref)
+    m.close()
+
+
+def test_host_io_async_back_to_back(bctx):
+    """Three asynchronous calls with new pixels each: every output matches its own map."""
+    import microsn_gb300 as mlc
+    N = 240
+    base = synth.lognormal_map(N, seed=41).astype(np.float32)
+    m = mlc.Map(bctx, base, "f32")
+    profs = _profiles(6)
+    trh = _host_tracks(800, N, 42, np.float32)
+    scales = [1.0, 2.0, 0.5]
+    pix = []
+    for s in scales:
+        h = torch.empty((N, N), dtype=torch.float32, pin_memory=True)
+        h.copy_(torch.from_numpy(base * np.float32(s)))
+        pix.append(h)
+    trp = _pinned(trh)
+    bctx.set_chunk_bytes(128 * 1024)
+    try:
+        outs = [mlc.convolve_sample_tracks(bctx, m, profs, trp, mag=False, pixels=pix[i], async_=True)
+                for i in range(3)]
+        bctx.synchronize()
+    finally:
+        bctx.set_chunk_bytes(256 << 20)
+    trd = _device(trh)
+    for i, s in enumerate(scales):
+        ref = mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=False,
+                                         pixels=torch.as_tensor(base * np.float32(s), device=DEV)).cpu()
+        assert torch.equal(outs[i], ref), i
+    m.close()
+
+
+def test_join_orders_copies_on_the_stream(bctx):
+    import microsn_gb300 as mlc
+    N = 200
+    mp = synth.lognormal_map(N, seed=51).astype(np.float32)
+    m = mlc.Map(bctx, mp, "f32")
+    profs = _profiles(3)
+    trp = _pinned(_host_tracks(400, N, 52, np.float32))
+    out = mlc.convolve_sample_tracks(bctx, m, profs, trp, mag=True, async_=True)
+    bctx.join()
+    ev = torch.cuda.Event()
+    ev.record(bctx.stream)
+    ev.synchronize()  # the copies back are done once the stream passes the join
+    ref = mlc.convolve_sample_tracks(bctx, m, profs, _device(_pinned(_host_tracks(400, N, 52, np.float32))),
+                                     mag=True).cpu()
+    assert torch.equal(out, ref)
+    m.close()
+
+
+def test_f64_matches_oracle(bctx):
+    import microsn_gb300 as mlc
+    N = 128
+    mp = synth.lognormal_map(N, seed=61)
+    m = mlc.Map(bctx, mp, "f64")
+    profs = _profiles(3)
+    trh = _host_tracks(200, N, 62, np.float64, epochs=(1, 30))
+    got = mlc.convolve_sample_tracks(bctx, m, profs, trh, mag=True,
+                                     out=torch.empty((3, int(trh["off"][-1])), dtype=torch.float64)).numpy()
+    for q, p in enumerate(profs):
+        conv = oracle.conv_fft(mp, mlc.profile_raster(p))
+        ref = oracle.sample_tracks(conv, trh["x0"], trh["y0"], trh["phi"], trh["v"], trh["off"], trh["t"], mag=True)
+        assert np.max(np.abs(got[q] - ref)) < 1e-9, (q, np.max(np.abs(got[q] - ref)))
+    m.close()
+
+
+def test_no_tracks_and_errors(bctx):
+    import microsn_gb300 as mlc
+    N = 120
+    m = mlc.Map(bctx, synth.lognormal_map(N, seed=71).astype(np.float32), "f32")
+    profs = _profiles(2)
+    empty = {"x0": np.zeros(0, np.float32), "y0": np.zeros(0, np.float32), "phi": np.zeros(0, np.float32),
+             "v": np.zeros(0, np.float32), "off": np.zeros(1, np.int64), "t": np.zeros(0, np.float32)}
+    out = mlc.convolve_sample_tracks(bctx, m, profs, empty)
+    assert tuple(out.shape) == (2, 0)
+    # one track longer than an output chunk is refused with MLC_ERR_LIMIT
+    trh = _host_tracks(10, N, 72, np.float32, epochs=(30, 40))
+    bctx.set_chunk_bytes(4096)
+    try:
+        # 4096 B / (2 profiles x 4 B) = 512 epochs per chunk: every track fits
+        mlc.convolve_sample_tracks(bctx, m, profs, trh)
+        # 4096 B / (16 profiles x 4 B) = 64 epochs per chunk: tracks of 70..80 epochs do not
+        with pytest.raises(mlc.MlcError) as e:
+            mlc.convolve_sample_tracks(bctx, m, _profiles(16), _host_tracks(10, N, 73, np.float32, epochs=(70, 80)))
+        assert e.value.code == 6
+    finally:
+        bctx.set_chunk_bytes(256 << 20)
+    with pytest.raises(ValueError):
+        mixed = dict(trh)
+        mixed["t"] = torch.as_tensor(trh["t"], device=DEV)
+        mlc.convolve_sample_tracks(bctx, m, profs, mixed)
+    m.close()
