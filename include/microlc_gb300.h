@@ -5,8 +5,8 @@
  * functions over host structs that own device buffers
  * (simulating_lcurves/include/gpu_functions.hpp:11-18, cpu_functions.hpp:12-15,
  * chi2/chi2_functions.cuh:93).  This header replaces them with plain-pointer C entry
- * points that a cgo / ctypes / C++ caller can bind; the C++ shim in
- * microsn_gb300/csrc/microlc_compat.hpp rebuilds the reference's own signatures on top.
+ * points that a cgo / ctypes / C++ caller can bind; the header-only C++ layer
+ * include/microlc_compat.hpp rebuilds the reference's own classes and signatures on top.
  *
  * Conventions
  *  - Every entry returns an int status: MLC_OK (0) or one of MLC_ERR_*; the text of
@@ -225,6 +225,25 @@ int mlc_ctx_join(mlc_ctx* ctx);
  * (min(nprof,16) x its epochs) must fit in one.  Waits for the context's queued work. */
 int mlc_ctx_set_chunk_bytes(mlc_ctx* ctx, size_t bytes);
 
+/* ======================================================================= map MPDs */
+
+/* MagnificationMap::getBinnedMpd (magnification_map_gpu.cu:45-87) of the map's pixels,
+ * in one pass instead of a sort of the whole map.  bins_host[i] = Mpd log edges
+ * pow(10, log10(min) + (i+1) dl) (mpd.cpp:8-13); counts_host[i] = the fraction of the
+ * Nx*Ny pixels v with min <= v < max and edge[i-1] < v <= edge[i] (a value above the last
+ * edge is dropped), 1/(Nx*Ny) for an empty bin.  Exact for FP64 maps; an FP32 map is
+ * binned by its FP32 values.  1 <= Nbins <= 16000. */
+int mlc_map_binned_mpd(mlc_ctx* ctx, mlc_map* map, int Nbins, double min, double max, double* bins_host,
+                       double* counts_host);
+
+/* Mpd::divide_by (mpd.cpp:71-107), A.divide_by(B, R): for each ratio edge z = binsR[i],
+ * countsR[i] = trapezium over B's bins of muB * pA(z muB) * pB(muB), pA interpolated
+ * linearly between A's edges (1e-8 outside them).  Bit-identical to the reference's
+ * host arithmetic. */
+int mlc_mpd_divide(mlc_ctx* ctx, int NA, const double* binsA_host, const double* countsA_host, int NB,
+                   const double* binsB_host, const double* countsB_host, int NR, const double* binsR_host,
+                   double* countsR_host);
+
 /* ======================================================================= chi2 vs one observed curve */
 
 /* Offset-minimised chi2 of ncurves magnitude curves of T epochs (m, row-major, the
@@ -343,6 +362,11 @@ int mlc_setup_chi2(double MA, double MB, double V0, double Dfac, int Nd, const d
                    const double* t_host, const double* s_host, int Nprof, const double* x_host, int ref_compat,
                    int* Njp_out, int* indA, int* indB, double* facA, double* facB, double* d_out, double* s_out,
                    double* const_term);
+
+/* find_indices (cpu_functions.cpp:28-45): for each of the Nd ascending times t_host the
+ * profile-size index j with x[j] <= t < x[j+1] (x_host: Nprof ascending sizes), -1 where
+ * the reference leaves the entry unset (a time above the last size or before the first). */
+int mlc_find_indices(const double* t_host, const double* x_host, int Nd, int Nprof, int* ind_host);
 
 /* locations_on_grid / locations_random (locations.cpp:6-25); host arrays of Nside^2 / Nloc. */
 int mlc_locations_grid(int Nside, int Nmap, int Noff, int* x_host, int* y_host);

@@ -78,6 +78,9 @@ SIGNATURES = {
     "mlc_convolve_sample_tracks": (i32, [vp, vp, vp, i32, C.POINTER(MlcProfile), C.POINTER(MlcTracks), i32, i32, vp,
                                          i32]),
     "mlc_ctx_join": (i32, [vp]),
+    "mlc_find_indices": (i32, [vp, vp, i32, i32, vp]),
+    "mlc_map_binned_mpd": (i32, [vp, vp, i32, f64, f64, vp, vp]),
+    "mlc_mpd_divide": (i32, [vp, i32, vp, vp, i32, vp, vp, i32, vp, vp]),
     "mlc_ctx_set_chunk_bytes": (i32, [vp, C.c_size_t]),
     "mlc_sample_tracks_interleaved": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
     "mlc_pair_setup": (i32, [vp, i32, i32, vp, vp, i32, vp, vp, vp, vp]),

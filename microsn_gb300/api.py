@@ -252,6 +252,32 @@ def sample_tracks_interleaved(ctx: Context, imap: torch.Tensor, nmaps: int, x0, 
     return out
 
 
+def map_binned_mpd(ctx: Context, m: Map, nbins: int, mn: float = 0.02, mx: float = 200.0):
+    """MagnificationMap::getBinnedMpd: (bins, counts) of the map's pixels in log bins."""
+    bins = np.zeros(nbins); counts = np.zeros(nbins)
+    ctx.check(ctx.L.mlc_map_binned_mpd(ctx.h, m.h, nbins, mn, mx, _ptr(bins), _ptr(counts)))
+    return bins, counts
+
+
+def mpd_normalize(bins, counts) -> np.ndarray:
+    """Mpd::normalize (mpd.cpp:64-69): counts / trapezium integral over the bins."""
+    b = np.asarray(bins, np.float64); c = np.array(counts, np.float64)
+    s = 0.0
+    for i in range(1, len(c)):
+        s += (c[i] + c[i - 1]) * (b[i] - b[i - 1]) / 2.0
+    return c / s
+
+
+def mpd_divide(ctx: Context, binsA, countsA, binsB, countsB, binsR) -> np.ndarray:
+    """Mpd::divide_by: A.divide_by(B, R) -> R's counts."""
+    c = lambda a: np.ascontiguousarray(a, np.float64)
+    bA, cA, bB, cB, bR = c(binsA), c(countsA), c(binsB), c(countsB), c(binsR)
+    out = np.zeros(len(bR))
+    ctx.check(ctx.L.mlc_mpd_divide(ctx.h, len(bA), _ptr(bA), _ptr(cA), len(bB), _ptr(bB), _ptr(cB), len(bR),
+                                   _ptr(bR), _ptr(out)))
+    return out
+
+
 TRACK_KEYS = ("x0", "y0", "phi", "v", "off", "t")
 
 

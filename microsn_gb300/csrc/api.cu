@@ -398,6 +398,23 @@ int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, i
   return guarded(ctx, [&] { convolve_sample_tracks(ctx, map, pixels, nprof, profiles_host, tr, mode, mag, out, flags); });
 }
 
+int mlc_map_binned_mpd(mlc_ctx* ctx, mlc_map* map, int Nbins, double min, double max, double* bins_host,
+                       double* counts_host) {
+  if (!ctx || !map || !bins_host || !counts_host) return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (map->device != ctx->device) return fail(ctx, MLC_ERR_ARG, "map lives on another device");
+  return guarded(ctx, [&] { map_binned_mpd(ctx, map, Nbins, min, max, bins_host, counts_host); });
+}
+
+int mlc_mpd_divide(mlc_ctx* ctx, int NA, const double* binsA_host, const double* countsA_host, int NB,
+                   const double* binsB_host, const double* countsB_host, int NR, const double* binsR_host,
+                   double* countsR_host) {
+  if (!ctx || !binsA_host || !countsA_host || !binsB_host || !countsB_host || !binsR_host || !countsR_host)
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  return guarded(ctx, [&] {
+    mpd_divide(ctx, NA, binsA_host, countsA_host, NB, binsB_host, countsB_host, NR, binsR_host, countsR_host);
+  });
+}
+
 int mlc_ctx_join(mlc_ctx* ctx) {
   return guarded(ctx, [&] { ctx_join(ctx); });
 }

@@ -132,6 +132,12 @@ double mlc_trapezium(int N, const double* f1, const double* f2, const double* x)
 // dir/mapmeta.dat holds "avgmu avgN / Nx / width / k g s"; dir/map.bin holds Nx*Nx int32
 // ray counts; pixels = counts * |avgmu/avgN| / |1/((1-k)^2 - g^2)|.  Call with out_host
 // NULL to read the size only.
+int mlc_find_indices(const double* t_host, const double* x_host, int Nd, int Nprof, int* ind_host) {
+  if (Nd < 0 || Nprof < 1 || (Nd > 0 && (!t_host || !x_host || !ind_host))) return MLC_ERR_ARG;
+  find_indices(t_host, x_host, Nd, Nprof, ind_host);
+  return MLC_OK;
+}
+
 int mlc_read_gerlumph(const char* dir, int* Nx, double* width, double* meta6, double* out_host, long cap) {
   if (!dir || !Nx || !width) return MLC_ERR_ARG;
   std::string d(dir);

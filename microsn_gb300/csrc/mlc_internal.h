@@ -145,6 +145,12 @@ void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double
 int profile_dims(const mlc_profile& p);
 int profile_raster(const mlc_profile& p, double* out, long cap);
 
+// Map MPDs (mpd.cu)
+void map_binned_mpd(mlc_ctx* ctx, const mlc_map* map, int nb, double mn, double mx, double* bins_host,
+                    double* counts_host);
+void mpd_divide(mlc_ctx* ctx, int NA, const double* bA, const double* cA, int NB, const double* bB,
+                const double* cB, int NR, const double* bR, double* cR);
+
 // Sampling (sample.cu)
 void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out);
 // Interleaved-map track sampler: out[q * E + (e - ebase)] for the epochs e of the given

@@ -75,6 +75,9 @@ def lib():
         L.orc_find_indices.argtypes = [_dp, _dp, C.c_int, C.c_int, _ip]
         L.orc_setup_chi2.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp,
                                      _dp, C.c_int, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
+        L.orc_binned_mpd.argtypes = [_dp, C.c_long, C.c_int, C.c_double, C.c_double, _dp, _dp]
+        L.orc_mpd_divide.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp, C.c_int, _dp, _dp]
+        L.orc_mpd_normalize.argtypes = [C.c_int, _dp, _dp]
         L.orc_pair_rank.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_int, _dp, _up, _up, _up]
         L.orc_pair_chi2_ratio.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, C.c_int, C.c_int,
                                           _dp, _dp, _dp, _dp, C.c_void_p, _dp]
@@ -118,6 +121,9 @@ def ref():
         R.ref_mpd_edges.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp]
         R.ref_trapezium.argtypes = [C.c_int, _dp, _dp, _dp]
         R.ref_trapezium.restype = C.c_double
+        R.ref_binned_mpd.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _dp, _dp]
+        R.ref_mpd_divide.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp, C.c_int, _dp, _dp]
+        R.ref_mpd_normalize.argtypes = [C.c_int, _dp, _dp]
         R.ref_read_map.argtypes = [C.c_char_p, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                    C.POINTER(C.c_double), C.c_void_p, C.c_long]
         _ref = R
@@ -263,6 +269,29 @@ def bin_chi2(lower, nper, chi2_sorted):
 def mpd_edges(Nbins, mn, mx, log=True):
     out = np.zeros(Nbins)
     lib().orc_mpd_edges(Nbins, mn, mx, int(log), out)
+    return out
+
+
+def binned_mpd(data, Nbins, mn, mx):
+    """getBinnedMpd: (edges, counts) of the map's pixels in log bins (see orc_binned_mpd)."""
+    d = np.ascontiguousarray(data, np.float64).ravel()
+    edges = mpd_edges(Nbins, mn, mx, True)
+    counts = np.zeros(Nbins)
+    lib().orc_binned_mpd(d, d.size, Nbins, mn, mx, edges, counts)
+    return edges, counts
+
+
+def mpd_normalize(bins, counts):
+    c = np.array(counts, np.float64)
+    lib().orc_mpd_normalize(len(c), np.ascontiguousarray(bins, np.float64), c)
+    return c
+
+
+def mpd_divide(bA, cA, bB, cB, bR):
+    """Mpd::divide_by: A.divide_by(B, R) -> R's counts."""
+    c = lambda a: np.ascontiguousarray(a, np.float64)
+    out = np.zeros(len(bR))
+    lib().orc_mpd_divide(len(bA), c(bA), c(cA), len(bB), c(bB), c(cB), len(bR), c(bR), out)
     return out
 
 

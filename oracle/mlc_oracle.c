@@ -389,6 +389,72 @@ void orc_mpd_edges(int Nbins, double mn, double mx, int logscale, double* out) {
   }
 }
 
+/* MagnificationMap::getBinnedMpd (magnification_map_gpu.cu:45-87), restated without the
+ * sort: the reference sorts the pixels, keeps those in [lower_bound(min), lower_bound(max))
+ * -- min <= v < max -- and counts, for every right edge, the kept values <= edge
+ * (upper_bound) and differences neighbours.  So a kept value lands in the first bin whose
+ * edge is >= v, and is dropped when it lies above the last edge.  counts are divided by
+ * npix, an empty bin gets 1/npix. */
+void orc_binned_mpd(const double* data, long npix, int Nbins, double mn, double mx, const double* edges,
+                    double* counts) {
+  long* c = (long*)calloc(Nbins, sizeof(long));
+  for (long p = 0; p < npix; p++) {
+    const double v = data[p];
+    if (!(v >= mn) || !(v < mx)) continue;
+    int lo = 0, hi = Nbins; /* first edge >= v */
+    while (lo < hi) {
+      const int mid = (lo + hi) / 2;
+      if (edges[mid] < v) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo < Nbins) c[lo]++;
+  }
+  for (int i = 0; i < Nbins; i++)
+    counts[i] = c[i] < 1 ? 1.0 / (double)npix : (double)c[i] / (double)npix;
+  free(c);
+}
+
+/* Mpd::divide_by (mpd.cpp:71-107): ratio[i] = trapezium over b of
+ * muB pA(z_i muB) pB(muB), pA linearly interpolated in A's bins (1e-8 outside the open
+ * range of A's edges); the interval is located by binary search (the reference scans
+ * linearly for the first edge above z muB -- the same interval). */
+void orc_mpd_divide(int NA, const double* bA, const double* cA, int NB, const double* bB, const double* cB,
+                    int NR, const double* bR, double* cR) {
+  double* terms = (double*)malloc(sizeof(double) * (NB > 0 ? NB : 1));
+  for (int i = 0; i < NR; i++) {
+    const double z = bR[i];
+    for (int b = 0; b < NB; b++) {
+      const double muB = bB[b];
+      const double prod = z * muB;
+      double pA;
+      if (prod <= bA[0] || prod >= bA[NA - 1]) {
+        pA = 1e-8;
+      } else {
+        int lo = 0, hi = NA; /* first edge > prod */
+        while (lo < hi) {
+          const int mid = (lo + hi) / 2;
+          if (bA[mid] <= prod) lo = mid + 1;
+          else hi = mid;
+        }
+        const int k = lo;
+        pA = cA[k - 1] + (cA[k] - cA[k - 1]) * (prod - bA[k - 1]) / (bA[k] - bA[k - 1]);
+      }
+      terms[b] = muB * pA * cB[b];
+    }
+    double s = 0.0;
+    for (int b = 1; b < NB; b++) s += (terms[b - 1] + terms[b]) * (bB[b] - bB[b - 1]) / 2.0;
+    cR[i] = s;
+  }
+  free(terms);
+}
+
+/* Mpd::integrate / normalize (mpd.cpp:48-69). */
+void orc_mpd_normalize(int N, const double* bins, double* counts) {
+  double s = 0.0;
+  for (int i = 1; i < N; i++) s += (counts[i] + counts[i - 1]) * (bins[i] - bins[i - 1]) / 2.0;
+  for (int i = 0; i < N; i++) counts[i] /= s;
+}
+
 /* trapezium (integration.cpp:3-9). */
 double orc_trapezium(int N, const double* f1, const double* f2, const double* x) {
   double s = 0.0;

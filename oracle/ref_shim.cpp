@@ -190,4 +190,42 @@ int ref_read_map(const char* dir, double Rein, int* Nx, double* width, double* p
   return (out && cap < n) ? 2 : 0;
 }
 
+// MagnificationMap::getBinnedMpd (magnification_map_gpu.cu:45-87) on given pixels, built
+// for thrust's sequential host backend.
+int ref_binned_mpd(const double* data, int Nx, int Ny, int Nbins, double mn, double mx, double* bins,
+                   double* counts) {
+  MagnificationMap m;
+  m.Nx = Nx;
+  m.Ny = Ny;
+  m.data = (double*)malloc(sizeof(double) * (size_t)Nx * Ny);  // freed by ~Image
+  memcpy(m.data, data, sizeof(double) * (size_t)Nx * Ny);
+  Mpd r = m.getBinnedMpd(Nbins, mn, mx);
+  memcpy(bins, r.bins, sizeof(double) * Nbins);
+  memcpy(counts, r.counts, sizeof(double) * Nbins);
+  return 0;
+}
+
+// Mpd::normalize then Mpd::divide_by (mpd.cpp:64-107): A.divide_by(B, ratio).
+int ref_mpd_divide(int NA, const double* binsA, const double* countsA, int NB, const double* binsB,
+                   const double* countsB, int NR, const double* binsR, double* countsR) {
+  Mpd A(NA), B(NB), R(NR);
+  memcpy(A.bins, binsA, sizeof(double) * NA);
+  memcpy(A.counts, countsA, sizeof(double) * NA);
+  memcpy(B.bins, binsB, sizeof(double) * NB);
+  memcpy(B.counts, countsB, sizeof(double) * NB);
+  memcpy(R.bins, binsR, sizeof(double) * NR);
+  A.divide_by(&B, &R);
+  memcpy(countsR, R.counts, sizeof(double) * NR);
+  return 0;
+}
+
+int ref_mpd_normalize(int N, const double* bins, double* counts) {
+  Mpd A(N);
+  memcpy(A.bins, bins, sizeof(double) * N);
+  memcpy(A.counts, counts, sizeof(double) * N);
+  A.normalize();
+  memcpy(counts, A.counts, sizeof(double) * N);
+  return 0;
+}
+
 }  // extern "C"

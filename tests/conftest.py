@@ -10,6 +10,9 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs an sm_103 GPU (GB300); calls the CUDA library through the C ABI")
+    # temporary files of the tests stay inside the repository (git-ignored)
+    if not config.option.basetemp:
+        config.option.basetemp = os.path.join(ROOT, "tests", ".tmp")
 
 
 @pytest.fixture(scope="session")

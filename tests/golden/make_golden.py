@@ -116,6 +116,32 @@ def main():
     f1 = rng.random(20); f2 = rng.random(20); xx = np.cumsum(rng.random(20))
     out.update(trap_f1=f1, trap_f2=f2, trap_x=xx, trap_val=np.array(R.ref_trapezium(20, f1, f2, xx)))
 
+    # map magnification-probability distributions: getBinnedMpd of a small heavy-tailed map
+    # (values placed exactly on edges, at min and max, and between the last edge and max),
+    # normalize, and divide_by into a ratio Mpd -- driver.cpp:173-180
+    mp = np.exp(rng.normal(0.0, 1.2, (64, 64)))
+    e50 = np.zeros(50)
+    R.ref_mpd_edges(50, 0.02, 200.0, 1, e50)
+    flat = mp.ravel()
+    flat[:10] = e50[[0, 1, 5, 5, 20, 33, 48, 49, 49, 12]]
+    flat[10:13] = [0.02, 200.0, np.nextafter(200.0, 0.0)]
+    flat[13:16] = [0.0, 1e-3, 1e4]
+    bins = np.zeros(50); counts = np.zeros(50)
+    R.ref_binned_mpd(flat.copy(), 64, 64, 50, 0.02, 200.0, bins, counts)
+    cn = counts.copy()
+    R.ref_mpd_normalize(50, bins, cn)
+    mpB = np.exp(rng.normal(0.2, 0.9, (64, 64))).ravel()
+    binsB = np.zeros(50); countsB = np.zeros(50)
+    R.ref_binned_mpd(mpB.copy(), 64, 64, 50, 0.02, 200.0, binsB, countsB)
+    R.ref_mpd_normalize(50, binsB, countsB)
+    eR = np.zeros(30)
+    R.ref_mpd_edges(30, 0.05, 20.0, 1, eR)
+    cR = np.zeros(30)
+    R.ref_mpd_divide(50, bins, cn, 50, binsB, countsB, 30, eR, cR)
+    out.update(mpd_map=flat.reshape(64, 64), mpd_bins=bins, mpd_counts=counts, mpd_counts_norm=cn,
+               mpd_mapB=mpB.reshape(64, 64), mpd_binsB=binsB, mpd_countsB_norm=countsB, mpd_ratio_bins=eR,
+               mpd_ratio_counts=cR)
+
     np.savez_compressed(os.path.join(HERE, "reference_cpu.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_cpu.npz"), len(out), "arrays")
 

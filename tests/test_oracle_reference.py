@@ -112,3 +112,41 @@ def test_pair_stage_random_live():
     R.ref_setup_integral_cpu(Nloc, Nprof, LCA.ravel().copy(), LCB.ravel().copy(), rank_ref)
     rank, _, _ = oracle.pair_rank(LCA, LCB)
     assert np.array_equal(rank, rank_ref)
+
+
+def test_mpd_match_golden(golden):
+    """getBinnedMpd, normalize and divide_by (driver.cpp:173-180) against the reference's output."""
+    b, c = oracle.binned_mpd(golden["mpd_map"], 50, 0.02, 200.0)
+    assert np.array_equal(b, golden["mpd_bins"])
+    assert np.array_equal(c, golden["mpd_counts"])
+    assert np.array_equal(oracle.mpd_normalize(b, c), golden["mpd_counts_norm"])
+    cR = oracle.mpd_divide(golden["mpd_bins"], golden["mpd_counts_norm"], golden["mpd_binsB"],
+                           golden["mpd_countsB_norm"], golden["mpd_ratio_bins"])
+    assert np.array_equal(cR, golden["mpd_ratio_counts"])
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_mpd_random_live(seed):
+    R = oracle.ref()
+    rng = np.random.default_rng(seed)
+    n = 300
+    # ray-shooting-like maps: integer counts times a factor, many exact ties
+    mp = rng.poisson(rng.lognormal(1.0, 1.0, (n, n))).astype(np.float64) * 0.37
+    nb = int(rng.integers(20, 400))
+    lo, hi = 10 ** rng.uniform(-3, -1), 10 ** rng.uniform(1, 3)
+    bins = np.zeros(nb); counts = np.zeros(nb)
+    R.ref_binned_mpd(mp.ravel().copy(), n, n, nb, lo, hi, bins, counts)
+    b, c = oracle.binned_mpd(mp, nb, lo, hi)
+    assert np.array_equal(b, bins) and np.array_equal(c, counts)
+    cn = counts.copy(); R.ref_mpd_normalize(nb, bins, cn)
+    assert np.array_equal(oracle.mpd_normalize(b, c), cn)
+    mpB = rng.poisson(rng.lognormal(0.5, 1.2, (n, n))).astype(np.float64) * 0.61
+    bB = np.zeros(nb); cB = np.zeros(nb)
+    R.ref_binned_mpd(mpB.ravel().copy(), n, n, nb, lo, hi, bB, cB)
+    R.ref_mpd_normalize(nb, bB, cB)
+    nr = int(rng.integers(10, 300))
+    eR = oracle.mpd_edges(nr, 0.01, 50.0, True)
+    cR = np.zeros(nr)
+    R.ref_mpd_divide(nb, bins, cn, nb, bB, cB, nr, eR, cR)
+    assert np.array_equal(oracle.mpd_divide(bins, cn, bB, cB, eR), cR)
