@@ -198,6 +198,40 @@ def bf16_peak():
 PAIR_N, PAIR_T, PAIR_BINS, PAIR_K = 100_000, 128, 1000, 10_000
 
 
+# Multi-filter flux-ratio likelihood at the reference chi2 driver's size
+# (chi2/chi2_driver.cu: N = 10^4 locations per image, F = 7 filters, T = 10 epochs).
+FR_N, FR_F, FR_T = 10_000, 7, 10
+
+
+def flux_ratio_workload(args, ctx, dev, rank):
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    rng = np.random.default_rng(13 + rank)
+    fo = rng.uniform(0.8, 1.2, (FR_F, FR_T)).astype(np.float32)
+    dfo = rng.uniform(0.05, 0.2, (FR_F, FR_T)).astype(np.float32)
+    m1 = torch.as_tensor(rng.lognormal(0.0, 0.3, (FR_N, FR_F, FR_T)).astype(np.float32), device=dev)
+    m2 = torch.as_tensor(rng.lognormal(0.0, 0.3, (FR_N, FR_F, FR_T)).astype(np.float32), device=dev)
+    for _ in range(max(args.warmup, 1)):
+        mlc.flux_ratio_chi2(ctx, fo, dfo, m1, m2)
+    torch.cuda.synchronize()
+    ctx.set_timing(True)
+    steps = max(1, min(args.steps, 10))
+    for _ in range(steps):
+        like = mlc.flux_ratio_chi2(ctx, fo, dfo, m1, m2)
+    kt = ctx.kernel_times(reset=True)
+    ctx.set_timing(False)
+    ms = sum(v[0] for v in kt.values()) / steps
+    pairs = FR_N * FR_N
+    k_ms = kt["flux_ratio_chi2"][0] / kt["flux_ratio_chi2"][1]
+    flops = 3.0 * FR_F * FR_T * pairs  # one FMA + one multiply + one FMA per pair and (filter, epoch)
+    return {"metric": "flux-ratio pair likelihood terms/s", "value": pairs / (ms / 1000.0), "unit": "pairs/s",
+            "ms_per_call": ms, "config": {"N": FR_N, "F": FR_F, "T": FR_T, "data": "synthetic lognormal fluxes"},
+            "likelihood": like, "kernel_ms": k_ms, "fp32_tflops": flops / (k_ms / 1000.0) / 1e12,
+            "bound": "FP32 pipe (3 FP32 operations per pair and (filter, epoch))"}
+
+
 def pair_workload(args, ctx, m, profs, n, dev, world, rank, stream):
     import numpy as np
     import torch
@@ -558,6 +592,9 @@ def main():
     pair = None
     if not args.no_pair:
         pair = pair_workload(args, ctx, m, profs, n, dev, world, rank, stream)
+    flux = None
+    if not args.no_pair:
+        flux = flux_ratio_workload(args, ctx, dev, rank)
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -573,7 +610,8 @@ def main():
                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
                        "ms_per_step": e2e_ms},
                "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
-               "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair}
+               "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair,
+               "flux_ratio": flux}
         print(json.dumps(res), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

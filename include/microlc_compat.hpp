@@ -12,6 +12,7 @@
 //   integration.hpp    trapezium
 //   locations.hpp      locations_on_grid, locations_random
 //   util.hpp           get_total_gpu_mem, get_free_gpu_mem, get_used_gpu_mem
+//   chi2/chi2_functions.cuh  getChi2GPU (multi-filter flux-ratio likelihood)
 // This header declares the same names with the same members, argument meaning and
 // ownership (the classes allocate their device halves with cudaMalloc in their
 // constructors, as data_structs.cu:39-125 does), so such a driver compiles unchanged
@@ -543,6 +544,25 @@ inline std::size_t get_used_gpu_mem() {
   std::size_t f = 0, t = 0;
   cudaMemGetInfo(&f, &t);
   return (t - f) / (1024 * 1024);
+}
+
+// ============================================================================ chi2/chi2_functions.cuh
+
+// Adds sum over location pairs of exp(-chi2) to *likelihood, chi2 the multi-filter
+// flux-ratio chi2 (chi2_functions.cuh:93-146) with mu2 taken at the second location (the
+// reference's kernel reads it at the first).  f_obs, df_obs must be host-readable and mu1,
+// mu2 device-readable (the reference's driver passes managed memory, which is both).
+// Prints the reason and returns false on failure, like the reference.
+inline bool getChi2GPU(float* f_obs, float* df_obs, float* mu1, float* mu2, int N, int F, int T, float* likelihood) {
+  double like = 0.0;
+  mlc_ctx* ctx = microlc_compat::context();
+  const int st = mlc_flux_ratio_chi2(ctx, f_obs, df_obs, mu1, mu2, N, F, T, nullptr, &like);
+  if (st != MLC_OK) {
+    std::fprintf(stderr, "microlc: getChi2GPU failed (status %d): %s\n", st, mlc_ctx_last_error(ctx));
+    return false;
+  }
+  *likelihood += (float)like;
+  return true;
 }
 
 #endif  // MICROLC_COMPAT_HPP

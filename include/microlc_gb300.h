@@ -225,6 +225,19 @@ int mlc_ctx_join(mlc_ctx* ctx);
  * (min(nprof,16) x its epochs) must fit in one.  Waits for the context's queued work. */
 int mlc_ctx_set_chunk_bytes(mlc_ctx* ctx, size_t bytes);
 
+/* ======================================================================= multi-filter flux ratios */
+
+/* getChi2GPU / getChi2CPU (chi2/chi2_functions.cuh:93-190): for every location pair
+ * (x of image 1, y of image 2)
+ *   chi2[x,y] = 1/2 sum_f sum_t ((f_obs[f,t] - mu1[x,f,t] / mu2[y,f,t]) / df_obs[f,t])^2
+ * -- the CPU twin's indexing; the reference's kernel reads mu2 at x, so its chi2 ignores
+ * y -- and *likelihood_host = sum over pairs of exp(-chi2), accumulated in FP64 in a
+ * fixed order.  f_obs_host, df_obs_host: F*T floats (filter-major) on the host; mu1, mu2:
+ * N*F*T device floats (location, filter, time).  chi2: device N*N floats stored as the
+ * reference's chi2_all[y*N + x], or NULL to skip.  FP32 arithmetic per term. */
+int mlc_flux_ratio_chi2(mlc_ctx* ctx, const float* f_obs_host, const float* df_obs_host, const float* mu1,
+                        const float* mu2, int N, int F, int T, float* chi2, double* likelihood_host);
+
 /* ======================================================================= map MPDs */
 
 /* MagnificationMap::getBinnedMpd (magnification_map_gpu.cu:45-87) of the map's pixels,

@@ -252,6 +252,24 @@ def sample_tracks_interleaved(ctx: Context, imap: torch.Tensor, nmaps: int, x0, 
     return out
 
 
+def flux_ratio_chi2(ctx: Context, f_obs, df_obs, mu1: torch.Tensor, mu2: torch.Tensor, want_chi2=False):
+    """getChi2GPU: likelihood = sum over location pairs of exp(-chi2) (FP64), and the
+    N x N chi2 (chi2[y, x], FP32) when want_chi2.  f_obs, df_obs: (F, T); mu1, mu2:
+    (N, F, T) FP32 CUDA tensors."""
+    fo = np.ascontiguousarray(f_obs, np.float32); dfo = np.ascontiguousarray(df_obs, np.float32)
+    F, T = fo.shape
+    N = mu1.shape[0]
+    if mu1.dtype != torch.float32 or mu2.dtype != torch.float32 or tuple(mu1.shape) != (N, F, T) \
+            or tuple(mu2.shape) != (N, F, T):
+        raise ValueError("mu1 and mu2 must be (N, F, T) float32 tensors")
+    mu1 = mu1.contiguous(); mu2 = mu2.contiguous()
+    chi2 = torch.empty((N, N), dtype=torch.float32, device=mu1.device) if want_chi2 else None
+    like = C.c_double()
+    ctx.check(ctx.L.mlc_flux_ratio_chi2(ctx.h, _ptr(fo), _ptr(dfo), _ptr(mu1), _ptr(mu2), N, F, T, _ptr(chi2),
+                                        C.byref(like)))
+    return (like.value, chi2) if want_chi2 else like.value
+
+
 def map_binned_mpd(ctx: Context, m: Map, nbins: int, mn: float = 0.02, mx: float = 200.0):
     """MagnificationMap::getBinnedMpd: (bins, counts) of the map's pixels in log bins."""
     bins = np.zeros(nbins); counts = np.zeros(nbins)

@@ -398,6 +398,13 @@ int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, i
   return guarded(ctx, [&] { convolve_sample_tracks(ctx, map, pixels, nprof, profiles_host, tr, mode, mag, out, flags); });
 }
 
+int mlc_flux_ratio_chi2(mlc_ctx* ctx, const float* f_obs_host, const float* df_obs_host, const float* mu1,
+                        const float* mu2, int N, int F, int T, float* chi2, double* likelihood_host) {
+  if (!ctx || !f_obs_host || !df_obs_host || !mu1 || !mu2 || !likelihood_host)
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  return guarded(ctx, [&] { flux_ratio_chi2(ctx, f_obs_host, df_obs_host, mu1, mu2, N, F, T, chi2, likelihood_host); });
+}
+
 int mlc_map_binned_mpd(mlc_ctx* ctx, mlc_map* map, int Nbins, double min, double max, double* bins_host,
                        double* counts_host) {
   if (!ctx || !map || !bins_host || !counts_host) return fail(ctx, MLC_ERR_ARG, "null argument");

@@ -145,6 +145,10 @@ void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double
 int profile_dims(const mlc_profile& p);
 int profile_raster(const mlc_profile& p, double* out, long cap);
 
+// Multi-filter flux-ratio likelihood (fluxratio.cu)
+void flux_ratio_chi2(mlc_ctx* ctx, const float* f_obs_host, const float* df_obs_host, const float* mu1,
+                     const float* mu2, int N, int F, int T, float* chi2, double* likelihood_host);
+
 // Map MPDs (mpd.cu)
 void map_binned_mpd(mlc_ctx* ctx, const mlc_map* map, int nb, double mn, double mx, double* bins_host,
                     double* counts_host);

@@ -75,6 +75,10 @@ def lib():
         L.orc_find_indices.argtypes = [_dp, _dp, C.c_int, C.c_int, _ip]
         L.orc_setup_chi2.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, _dp, _dp,
                                      _dp, C.c_int, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp, _dp]
+        L.orc_flux_ratio.argtypes = [_fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.orc_flux_ratio.restype = C.c_double
+        L.orc_flux_ratio_f32.argtypes = [_fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_int]
+        L.orc_flux_ratio_f32.restype = C.c_float
         L.orc_binned_mpd.argtypes = [_dp, C.c_long, C.c_int, C.c_double, C.c_double, _dp, _dp]
         L.orc_mpd_divide.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp, C.c_int, _dp, _dp]
         L.orc_mpd_normalize.argtypes = [C.c_int, _dp, _dp]
@@ -121,6 +125,9 @@ def ref():
         R.ref_mpd_edges.argtypes = [C.c_int, C.c_double, C.c_double, C.c_int, _dp]
         R.ref_trapezium.argtypes = [C.c_int, _dp, _dp, _dp]
         R.ref_trapezium.restype = C.c_double
+        R.chi2 = C.CDLL(os.path.join(HERE, "_ref", "libmlcref_chi2.so"))
+        R.chi2.ref_chi2_cpu.argtypes = [_fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_int]
+        R.chi2.ref_chi2_cpu.restype = C.c_float
         R.ref_binned_mpd.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, _dp, _dp]
         R.ref_mpd_divide.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp, C.c_int, _dp, _dp]
         R.ref_mpd_normalize.argtypes = [C.c_int, _dp, _dp]
@@ -293,6 +300,25 @@ def mpd_divide(bA, cA, bB, cB, bR):
     out = np.zeros(len(bR))
     lib().orc_mpd_divide(len(bA), c(bA), c(cA), len(bB), c(bB), c(cB), len(bR), c(bR), out)
     return out
+
+
+def flux_ratio(f_obs, df_obs, mu1, mu2, want_chi2=False):
+    """getChi2CPU in FP64: (likelihood, chi2[y, x] if want_chi2)."""
+    fo = np.ascontiguousarray(f_obs, np.float32).ravel(); dfo = np.ascontiguousarray(df_obs, np.float32).ravel()
+    m1 = np.ascontiguousarray(mu1, np.float32); m2 = np.ascontiguousarray(mu2, np.float32)
+    N, F, T = m1.shape
+    chi2 = np.zeros((N, N)) if want_chi2 else None
+    like = lib().orc_flux_ratio(fo, dfo, m1.ravel(), m2.ravel(), N, F, T,
+                                None if chi2 is None else chi2.ctypes.data_as(C.c_void_p))
+    return (like, chi2) if want_chi2 else like
+
+
+def flux_ratio_f32(f_obs, df_obs, mu1, mu2):
+    """getChi2CPU in the reference's own FP32 arithmetic (float likelihood)."""
+    fo = np.ascontiguousarray(f_obs, np.float32).ravel(); dfo = np.ascontiguousarray(df_obs, np.float32).ravel()
+    m1 = np.ascontiguousarray(mu1, np.float32); m2 = np.ascontiguousarray(mu2, np.float32)
+    N, F, T = m1.shape
+    return lib().orc_flux_ratio_f32(fo, dfo, m1.ravel(), m2.ravel(), N, F, T)
 
 
 def trapezium(f1, f2, x):

@@ -455,6 +455,42 @@ void orc_mpd_normalize(int N, const double* bins, double* counts) {
   for (int i = 0; i < N; i++) counts[i] /= s;
 }
 
+/* getChi2CPU (chi2/chi2_functions.cuh:150-190) restated in FP64: chi2[y*N + x] =
+ * 1/2 sum_{f,t} ((fo - m1[x]/m2[y]) / df)^2 and the likelihood sum of exp(-chi2). */
+double orc_flux_ratio(const float* fo, const float* dfo, const float* m1, const float* m2, int N, int F, int T,
+                      double* chi2) {
+  const long K = (long)F * T;
+  double like = 0.0;
+  for (int x = 0; x < N; x++)
+    for (int y = 0; y < N; y++) {
+      double c = 0.0;
+      for (long k = 0; k < K; k++) {
+        const double tmp = ((double)fo[k] - (double)m1[x * K + k] / (double)m2[y * K + k]) / (double)dfo[k];
+        c += tmp * tmp / 2;
+      }
+      if (chi2) chi2[(long)y * N + x] = c;
+      like += exp(-c);
+    }
+  return like;
+}
+
+/* The same in the reference CPU twin's own FP32 arithmetic and order (float chi2 and
+ * float likelihood accumulators, chi2_functions.cuh:165-183). */
+float orc_flux_ratio_f32(const float* fo, const float* dfo, const float* m1, const float* m2, int N, int F, int T) {
+  float like = 0.0f;
+  for (int x = 0; x < N; x++)
+    for (int y = 0; y < N; y++) {
+      float c = 0.0f;
+      for (int f = 0; f < F; f++)
+        for (int t = 0; t < T; t++) {
+          const float tmp = (fo[f * T + t] - m1[x * F * T + f * T + t] / m2[y * F * T + f * T + t]) / dfo[f * T + t];
+          c += tmp * tmp / 2;
+        }
+      like += expf(-c);
+    }
+  return like;
+}
+
 /* trapezium (integration.cpp:3-9). */
 double orc_trapezium(int N, const double* f1, const double* f2, const double* x) {
   double s = 0.0;

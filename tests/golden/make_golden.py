@@ -142,6 +142,15 @@ def main():
                mpd_mapB=mpB.reshape(64, 64), mpd_binsB=binsB, mpd_countsB_norm=countsB, mpd_ratio_bins=eR,
                mpd_ratio_counts=cR)
 
+    # multi-filter flux-ratio likelihood: getChi2CPU (chi2/chi2_functions.cuh:150-190)
+    N, F, T = 40, 3, 7
+    fo = rng.uniform(0.6, 1.4, (F, T)).astype(np.float32)
+    dfo = rng.uniform(0.05, 0.3, (F, T)).astype(np.float32)
+    m1 = rng.uniform(0.5, 2.0, (N, F, T)).astype(np.float32)
+    m2 = rng.uniform(0.5, 2.0, (N, F, T)).astype(np.float32)
+    like = R.chi2.ref_chi2_cpu(fo.ravel(), dfo.ravel(), m1.ravel(), m2.ravel(), N, F, T)
+    out.update(fr_fobs=fo, fr_dfobs=dfo, fr_mu1=m1, fr_mu2=m2, fr_like=np.array(like, np.float32))
+
     np.savez_compressed(os.path.join(HERE, "reference_cpu.npz"), **out)
     print("wrote", os.path.join(HERE, "reference_cpu.npz"), len(out), "arrays")
 

@@ -150,3 +150,25 @@ def test_mpd_random_live(seed):
     cR = np.zeros(nr)
     R.ref_mpd_divide(nb, bins, cn, nb, bB, cB, nr, eR, cR)
     assert np.array_equal(oracle.mpd_divide(bins, cn, bB, cB, eR), cR)
+
+
+def test_flux_ratio_match_golden(golden):
+    """getChi2CPU: the FP32 emulation is bit-identical, the FP64 restatement within 1e-5."""
+    args = (golden["fr_fobs"], golden["fr_dfobs"], golden["fr_mu1"], golden["fr_mu2"])
+    ref = float(golden["fr_like"])
+    assert np.float32(oracle.flux_ratio_f32(*args)) == np.float32(ref)
+    assert abs(oracle.flux_ratio(*args) - ref) <= 1e-5 * abs(ref)
+
+
+@needs_ref
+@pytest.mark.parametrize("N,F,T,seed", [(25, 7, 10, 1), (60, 2, 3, 2), (1, 1, 1, 3)])
+def test_flux_ratio_random_live(N, F, T, seed):
+    R = oracle.ref()
+    rng = np.random.default_rng(seed)
+    fo = rng.uniform(0.6, 1.4, (F, T)).astype(np.float32)
+    dfo = rng.uniform(0.2, 0.6, (F, T)).astype(np.float32)
+    m1 = rng.uniform(0.5, 2.0, (N, F, T)).astype(np.float32)
+    m2 = rng.uniform(0.5, 2.0, (N, F, T)).astype(np.float32)
+    ref = R.chi2.ref_chi2_cpu(fo.ravel(), dfo.ravel(), m1.ravel(), m2.ravel(), N, F, T)
+    assert np.float32(oracle.flux_ratio_f32(fo, dfo, m1, m2)) == np.float32(ref)
+    assert abs(oracle.flux_ratio(fo, dfo, m1, m2) - ref) <= 1e-5 * abs(ref)
