@@ -225,6 +225,43 @@ int mlc_ctx_join(mlc_ctx* ctx);
  * (min(nprof,16) x its epochs) must fit in one.  Waits for the context's queued work. */
 int mlc_ctx_set_chunk_bytes(mlc_ctx* ctx, size_t bytes);
 
+/* ======================================================================= differentiable track fit */
+/* No reference counterpart.  Gradients of the chi2 of model light curves with respect to
+ * every track's parameters theta = (x0, y0, phi, v, R_half, dm), for gradient-based fits. */
+
+#define MLC_FIT_MAX_RADII 32
+
+/* Smooth thin-disc raster on a fixed N x N grid (N even): the thin-disc law of
+ * profile.cpp:402-446, I = min(I_core, 1 / (exp((r/sigma)^(3/4)) - 1)), sigma = 0.4106
+ * rhalf, without the truncation at 2 rhalf, normalised to unit sum, and the rasters of its
+ * analytic derivatives at the same offsets: dP/dx and dP/dy per pixel of offset (x along
+ * a row), dP/d(rhalf) with the normalisation included.  Derivative outputs may be NULL.
+ * Host FP64. */
+int mlc_fit_raster(double rhalf, double pix, int N, double* P_host, double* dPdx_host, double* dPdy_host,
+                   double* dPdR_host);
+
+/* Radius stack of a map for mlc_track_fit: for each radius radii_host[k] (K of them,
+ * increasing, 2 <= K <= MLC_FIT_MAX_RADII, in the units of pix) the map convolved with
+ * P(R_k), dP/dx, dP/dy and dP/dR (mlc_fit_raster, N x N) -- the values and first
+ * derivatives of the continuous convolution at every pixel node -- interleaved per pixel
+ * into stack (device, Ny*Nx*K*4 values of the map's precision):
+ * stack[((y*Nx + x)*K + k)*4 + {0: M, 1: dM/dx, 2: dM/dy, 3: dM/dR}]. */
+int mlc_radius_stack(mlc_ctx* ctx, mlc_map* map, int K, const double* radii_host, double pix, int N, void* stack);
+
+/* chi2 of ntracks model curves and its gradient.  theta: ntracks x 6 (x0, y0 in pixels,
+ * phi in radians, v in pixels per unit of t, R_half in the stack's radius units, dm in
+ * magnitudes); off: ntracks+1 epoch offsets; t, obs, w: epochs, observed magnitudes and
+ * weights (1/sigma^2).  Model: m(t) = -2.5 log10 M(x0 + v t cos phi, y0 + v t sin phi; R)
+ * + dm, M the tensor-product cubic Hermite interpolant in (x, y, R) of the stack's node
+ * values and derivatives (nodes at pixel centres j + 1/2; C1, so finite differences
+ * converge to the gradient everywhere); chi2[i] = sum_e w (obs - m)^2; grad[i*6 + j] = dchi2_i/dtheta_ij (NULL to skip);
+ * model[e] = m(t_e) (NULL to skip; NaN where the position leaves the map).  All arrays on
+ * the device in `precision`.  Only queues one kernel: no allocation, no synchronisation,
+ * so the call can be captured into a CUDA graph. */
+int mlc_track_fit(mlc_ctx* ctx, const void* stack, int Nx, int Ny, int precision, int K, const double* radii_host,
+                  int ntracks, const void* theta, const int64_t* off, const void* t, const void* obs, const void* w,
+                  void* chi2, void* grad, void* model);
+
 /* ======================================================================= multi-filter flux ratios */
 
 /* getChi2GPU / getChi2CPU (chi2/chi2_functions.cuh:93-190): for every location pair

@@ -252,6 +252,79 @@ def sample_tracks_interleaved(ctx: Context, imap: torch.Tensor, nmaps: int, x0, 
     return out
 
 
+# ----------------------------------------------------------------------------- differentiable track fit
+
+FIT_PARAMS = ("x0", "y0", "phi", "v", "R_half", "dm")
+
+
+def fit_raster(rhalf: float, pix: float, N: int):
+    """Smooth thin-disc raster P (N x N) and its derivative rasters dP/dx, dP/dy (per pixel
+    of offset) and dP/d(rhalf), as used by the radius stack."""
+    out = [np.zeros(N * N) for _ in range(4)]
+    st = _lib.load().mlc_fit_raster(rhalf, pix, N, *[_ptr(a) for a in out])
+    if st:
+        raise MlcError(st, "fit raster: rhalf, pix > 0 and an even N are required")
+    return tuple(a.reshape(N, N) for a in out)
+
+
+def radius_stack(ctx: Context, m: Map, radii, N: int | None = None, pix: float = 1.0) -> torch.Tensor:
+    """The map convolved with P(R_k), dP/dx, dP/dy and dP/dR for each radius: (Ny, Nx, K, 4)
+    tensor in the map's precision.  N defaults to a raster of 2.2 R_max on each side."""
+    r = np.ascontiguousarray(radii, np.float64)
+    if N is None:
+        N = int(np.ceil(4.4 * r[-1] / pix)) // 2 * 2 + 2
+    out = torch.empty((m.Ny, m.Nx, len(r), 4), dtype=m.dtype, device=f"cuda:{ctx.device}")
+    ctx.check(ctx.L.mlc_radius_stack(ctx.h, m.h, len(r), _ptr(r), pix, int(N), _ptr(out)))
+    return out
+
+
+def track_fit(ctx: Context, stack: torch.Tensor, radii, theta: torch.Tensor, off: torch.Tensor, t: torch.Tensor,
+              obs: torch.Tensor, w: torch.Tensor, grad: bool = True, model: bool = False, out_chi2=None,
+              out_grad=None, out_model=None):
+    """chi2 (n,), d chi2 / d theta (n, 6) and optionally the model magnitudes of n tracks
+    with parameters theta = (x0, y0, phi, v, R_half, dm) against observed curves (obs, w
+    per epoch).  One kernel launch, no allocation inside the library (pass out_* to make
+    the call capturable in a CUDA graph)."""
+    Ny, Nx, K, four = stack.shape
+    assert four == 4
+    dt = stack.dtype
+    prec = _PREC[dt]
+    n = theta.shape[0]
+    for name, a in (("theta", theta), ("t", t), ("obs", obs), ("w", w)):
+        if a.dtype != dt or not a.is_contiguous() or not a.is_cuda:
+            raise ValueError(f"{name} must be a contiguous CUDA {dt} tensor")
+    if off.dtype != torch.int64 or off.numel() != n + 1:
+        raise ValueError("off must be int64 with ntracks + 1 entries")
+    c2 = out_chi2 if out_chi2 is not None else torch.empty(n, dtype=dt, device=theta.device)
+    g = (out_grad if out_grad is not None else torch.empty((n, 6), dtype=dt, device=theta.device)) if grad else None
+    mo = (out_model if out_model is not None else torch.empty(t.shape[0], dtype=dt, device=theta.device)) \
+        if model else None
+    r = (C.c_double * K)(*[float(x) for x in radii])
+    ctx.check(ctx.L.mlc_track_fit(ctx.h, _ptr(stack), Nx, Ny, prec, K, r, n, _ptr(theta), _ptr(off), _ptr(t),
+                                  _ptr(obs), _ptr(w), _ptr(c2), _ptr(g), _ptr(mo)))
+    return c2, g, mo
+
+
+class TrackChi2(torch.autograd.Function):
+    """chi2 of every track as a differentiable function of theta (n, 6); the forward
+    kernel computes the gradient at the same time and backward scales it."""
+
+    @staticmethod
+    def forward(fctx, theta, ctx, stack, radii, off, t, obs, w):
+        c2, g, _ = track_fit(ctx, stack, radii, theta.detach().contiguous(), off, t, obs, w, grad=True)
+        fctx.save_for_backward(g)
+        return c2
+
+    @staticmethod
+    def backward(fctx, gout):
+        (g,) = fctx.saved_tensors
+        return gout[:, None] * g, None, None, None, None, None, None, None
+
+
+def track_chi2(ctx: Context, stack, radii, theta, off, t, obs, w) -> torch.Tensor:
+    return TrackChi2.apply(theta, ctx, stack, radii, off, t, obs, w)
+
+
 def flux_ratio_chi2(ctx: Context, f_obs, df_obs, mu1: torch.Tensor, mu2: torch.Tensor, want_chi2=False):
     """getChi2GPU: likelihood = sum over location pairs of exp(-chi2) (FP64), and the
     N x N chi2 (chi2[y, x], FP32) when want_chi2.  f_obs, df_obs: (F, T); mu1, mu2:

@@ -275,13 +275,15 @@ int mlc_map_data(mlc_map* map, void** dev_ptr) {
   return MLC_OK;
 }
 
-static void map_prepare(mlc_ctx* ctx, mlc_map* map) {
+extern "C++" {
+void mlc::map_prepare(mlc_ctx* ctx, mlc_map* map) {
   if (map->spec_valid) return;
   FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
   if (!map->spec) MLC_CUDA(cudaMalloc(&map->spec, p->spec_bytes()));
   fft2_forward(ctx, *p, map->data, map->prec, map->spec);
   map->spec_valid = true;
 }
+}  // extern "C++"
 
 int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map) {
   if (!map) return fail(ctx, MLC_ERR_ARG, "null map");
@@ -396,6 +398,31 @@ int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, i
     return fail(ctx, MLC_ERR_ARG, "null track array or output");
   if (map->device != ctx->device) return fail(ctx, MLC_ERR_ARG, "map lives on another device");
   return guarded(ctx, [&] { convolve_sample_tracks(ctx, map, pixels, nprof, profiles_host, tr, mode, mag, out, flags); });
+}
+
+int mlc_fit_raster(double rhalf, double pix, int N, double* P_host, double* dPdx_host, double* dPdy_host,
+                   double* dPdR_host) {
+  if (!P_host) return MLC_ERR_ARG;
+  return thin_disc_fit_raster(rhalf, pix, N, P_host, dPdx_host, dPdy_host, dPdR_host) == N ? MLC_OK : MLC_ERR_ARG;
+}
+
+int mlc_radius_stack(mlc_ctx* ctx, mlc_map* map, int K, const double* radii_host, double pix, int N, void* stack) {
+  if (!ctx || !map || !radii_host || !stack) return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (map->device != ctx->device) return fail(ctx, MLC_ERR_ARG, "map lives on another device");
+  if (!(pix > 0)) return fail(ctx, MLC_ERR_ARG, "pix must be positive");
+  return guarded(ctx, [&] { radius_stack(ctx, map, K, radii_host, pix, N, stack); });
+}
+
+int mlc_track_fit(mlc_ctx* ctx, const void* stack, int Nx, int Ny, int precision, int K, const double* radii_host,
+                  int ntracks, const void* theta, const int64_t* off, const void* t, const void* obs, const void* w,
+                  void* chi2, void* grad, void* model) {
+  if (!ctx || !stack || !radii_host || (ntracks > 0 && (!theta || !off || !t || !obs || !w)))
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (Nx < 2 || Ny < 2 || ntracks < 0 || (precision != MLC_F64 && precision != MLC_F32))
+    return fail(ctx, MLC_ERR_ARG, "bad sizes or precision");
+  return guarded(ctx, [&] {
+    track_fit(ctx, stack, Nx, Ny, precision, K, radii_host, ntracks, theta, off, t, obs, w, chi2, grad, model);
+  });
 }
 
 int mlc_flux_ratio_chi2(mlc_ctx* ctx, const float* f_obs_host, const float* df_obs_host, const float* mu1,

@@ -149,6 +149,16 @@ int profile_raster(const mlc_profile& p, double* out, long cap);
 void flux_ratio_chi2(mlc_ctx* ctx, const float* f_obs_host, const float* df_obs_host, const float* mu1,
                      const float* mu2, int N, int F, int T, float* chi2, double* likelihood_host);
 
+// Spectrum of the map's current pixels, computed once and cached (api.cu).
+void map_prepare(mlc_ctx* ctx, mlc_map* map);
+
+// Differentiable track fit (profile.cu, fit.cu)
+int thin_disc_fit_raster(double rhalf, double pix, int N, double* P, double* dPdx, double* dPdy, double* dPdR);
+void radius_stack(mlc_ctx* ctx, mlc_map* map, int K, const double* radii, double pix, int N, void* stack);
+void track_fit(mlc_ctx* ctx, const void* stack, int Nx, int Ny, int prec, int K, const double* radii, int ntracks,
+               const void* theta, const int64_t* off, const void* t, const void* obs, const void* w, void* chi2,
+               void* grad, void* model);
+
 // Map MPDs (mpd.cu)
 void map_binned_mpd(mlc_ctx* ctx, const mlc_map* map, int nb, double mn, double mx, double* bins_host,
                     double* counts_host);
@@ -157,6 +167,9 @@ void mpd_divide(mlc_ctx* ctx, int NA, const double* bA, const double* cA, int NB
 
 // Sampling (sample.cu)
 void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out);
+// out[p * S + off + q] = maps[q][p] for q < nmaps (<= 16); other slots untouched.
+void interleave_into(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int S, int off,
+                     void* out);
 // Interleaved-map track sampler: out[q * E + (e - ebase)] for the epochs e of the given
 // tracks (off holds global epoch indices; ebase lets a chunk of tracks fill its own buffer).
 void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,

@@ -152,4 +152,54 @@ int profile_raster(const mlc_profile& p, double* out, long cap) {
   return N;
 }
 
+// Thin-disc raster for differentiable fits: the reference's thin-disc law
+// (profile.cpp:402-446) I(r) = 1 / (exp((r/sigma)^(3/4)) - 1), sigma = 0.4106 R_half,
+// with its flat core (I <= I_core = 10 / (exp((R_half/sigma)^(3/4)) - 1), a constant), but
+// on a fixed N x N grid and without the truncation at r = 2 R_half, so that the normalised
+// raster P is smooth in R_half.  Pixel centres as in createGrid (profile.cpp:126-157):
+// (j - N/2) pix + pix/2.  Also returns the derivative rasters of the same continuous
+// profile at the same offsets: dPdx, dPdy per pixel of offset (x = column, y = row) and
+// dPdR per unit of R_half, dP/dR = (dI/dR) / S - P sum(dI/dR) / S with S = sum I.
+// Any of the derivative outputs may be null.
+int thin_disc_fit_raster(double rhalf, double pix, int N, double* P, double* dPdx, double* dPdy, double* dPdR) {
+  if (!(rhalf > 0) || !(pix > 0) || N < 2 || (N & 1)) return -1;
+  const double sigma = 0.4106 * rhalf;
+  const double v_core = 10.0 / (std::exp(std::pow(rhalf / sigma, 0.75)) - 1.0);
+  double S = 0.0, SdR = 0.0;
+  for (int i = 0; i < N; i++) {
+    const double y = (i - N / 2) * pix + pix / 2.0;
+    for (int j = 0; j < N; j++) {
+      const double x = (j - N / 2) * pix + pix / 2.0;
+      const double r = std::hypot(x, y);
+      const double u = r / sigma;
+      const double e = std::exp(std::pow(u, 0.75));
+      const double f = 1.0 / (e - 1.0);
+      double v, dx = 0.0, dy = 0.0, dR = 0.0;
+      if (f >= v_core) {  // core: constant, independent of position and R
+        v = v_core;
+      } else {
+        v = f;
+        const double fp = -0.75 * std::pow(u, -0.25) * e / ((e - 1.0) * (e - 1.0));  // dI/du
+        dx = fp * x / (r * sigma) * pix;
+        dy = fp * y / (r * sigma) * pix;
+        dR = -fp * u / rhalf;
+      }
+      const long q = (long)i * N + j;
+      P[q] = v;
+      if (dPdx) dPdx[q] = dx;
+      if (dPdy) dPdy[q] = dy;
+      if (dPdR) dPdR[q] = dR;
+      S += v;
+      SdR += dR;
+    }
+  }
+  for (long q = 0; q < (long)N * N; q++) {
+    P[q] /= S;
+    if (dPdx) dPdx[q] /= S;
+    if (dPdy) dPdy[q] /= S;
+    if (dPdR) dPdR[q] = dPdR[q] / S - P[q] * SdR / S;
+  }
+  return N;
+}
+
 }  // namespace mlc

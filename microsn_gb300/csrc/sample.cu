@@ -4,6 +4,7 @@
 // curve.
 #include <cmath>
 
+#include "bilinear.cuh"
 #include "mlc_internal.h"
 
 namespace mlc {
@@ -30,44 +31,6 @@ void sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int 
   MLC_CHECK_LAUNCH();
 }
 
-// Bilinear weights of RectGrid::interp2d_bilinear (rectGrid.cpp:349-378) on pixel
-// centres j + 1/2.  The position is split into an exact integer base (bx, by) and a
-// small offset (fx, fy) so that FP32 keeps sub-pixel precision far from the origin.
-template <typename T>
-struct Bilin {
-  int jl, jr, il, iu;
-  T w0, w1, w2, w3;  // (iu,jl) (iu,jr) (il,jl) (il,jr)
-  bool inside;
-};
-
-template <typename T>
-__device__ __forceinline__ Bilin<T> bilin_weights(long bx, T fx, long by, T fy, int Nx, int Ny) {
-  Bilin<T> B;
-  // absolute coordinate = b + f ; hull of centres is [0.5, N - 0.5]
-  const T flx = floor(fx), fly = floor(fy);
-  const long jx = bx + (long)flx, iy = by + (long)fly;  // pixel containing the point
-  const T rx = fx - flx, ry = fy - fly;                 // in [0, 1)
-  B.inside = !((jx < 0) || (jx == 0 && rx < (T)0.5) || (jx > Nx - 1) || (jx == Nx - 1 && rx > (T)0.5) ||
-               (iy < 0) || (iy == 0 && ry < (T)0.5) || (iy > Ny - 1) || (iy == Ny - 1 && ry > (T)0.5));
-  const T dx = rx - (T)0.5, dy = ry - (T)0.5;
-  const long jl = (dx < 0) ? jx - 1 : jx;
-  const long iu = (dy < 0) ? iy : iy + 1;
-  // a = x - centre(jl), b = centre(jl+1) - x, c = centre(iu) - y, d = y - centre(iu-1)
-  const T a = (dx < 0) ? rx + (T)0.5 : dx;
-  const T b = (T)1 - a;
-  const T d = (dy < 0) ? ry + (T)0.5 : dy;
-  const T c = (T)1 - d;
-  B.jl = (int)jl;
-  B.jr = (int)min(jl + 1, (long)Nx - 1);
-  B.iu = (int)min(iu, (long)Ny - 1);
-  B.il = (int)(iu - 1);
-  B.w0 = b * d;
-  B.w1 = a * d;
-  B.w2 = b * c;
-  B.w3 = a * c;
-  return B;
-}
-
 template <typename T>
 __device__ __forceinline__ T bilin_read(const T* __restrict__ m, const Bilin<T>& B, int Nx) {
   T z = B.w0 * __ldg(m + (long)B.iu * Nx + B.jl);
@@ -77,8 +40,6 @@ __device__ __forceinline__ T bilin_read(const T* __restrict__ m, const Bilin<T>&
   return z;
 }
 
-__device__ __forceinline__ double mlc_log10(double x) { return log10(x); }
-__device__ __forceinline__ float mlc_log10(float x) { return log10f(x); }
 
 template <typename T>
 struct MapList {
@@ -160,27 +121,30 @@ void sample_tracks(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int Nx
 // Interleaving the maps pixel by pixel ([y][x][stride], stride >= nm, a power of two)
 // makes a corner one contiguous 4*stride-byte read for all maps at once.
 
-// out[p*stride + q] = maps[q][p] (q < nm), 0 for nm <= q < stride.  A CTA moves a tile of
-// 256 pixels: coalesced loads of each map's 256 values into shared memory, then the tile's
-// 256*stride contiguous outputs are written with consecutive threads on consecutive words.
+// out[p*S + off + q] = maps[q][p] for q < width (0 for nm <= q < width).  A CTA moves a
+// tile of 256 pixels: coalesced loads of each map's 256 values into shared memory, then
+// the tile's width-long runs are written with consecutive threads on consecutive words
+// (a whole contiguous block when width == S).  wshift = log2(width) when width is a power
+// of two, else -1.
 template <typename T>
-__global__ void __launch_bounds__(256) k_interleave(MapList<T> maps, int nm, int stride, long npix,
-                                                   T* __restrict__ out) {
+__global__ void __launch_bounds__(256) k_interleave(MapList<T> maps, int nm, int width, int wshift, int S, int off,
+                                                   long npix, T* __restrict__ out) {
   __shared__ T tile[16][257];
   const long ntiles = (npix + 255) / 256;
   for (long tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
     const long p0 = tb * 256;
     const int np = (int)min(256L, npix - p0);
-    for (int q = 0; q < stride; q++) {
+    for (int q = 0; q < width; q++) {
       const long p = p0 + threadIdx.x;
       tile[q][threadIdx.x] = (q < nm && threadIdx.x < np) ? __ldg(maps.m[q] + p) : (T)0;
     }
     __syncthreads();
-    T* o = out + p0 * stride;
-    const int nout = np * stride;
+    T* o = out + p0 * S + off;
+    const int nout = np * width;
     for (int i = threadIdx.x; i < nout; i += blockDim.x) {
-      const int px = i / stride, q = i - px * stride;
-      o[i] = tile[q][px];
+      const int px = wshift >= 0 ? (i >> wshift) : i / width;
+      const int q = i - px * width;
+      o[(long)px * S + q] = tile[q][px];
     }
     __syncthreads();
   }
@@ -261,20 +225,33 @@ __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ 
   }
 }
 
-void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out) {
+static void interleave_impl(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int width, int S, int off,
+                            long npix, int prec, void* out) {
   const int grid = (int)std::min<long>((npix + 255) / 256, (long)ctx->sm_count * 16);
+  int wshift = -1;
+  for (int b = 0; b < 5; b++)
+    if (width == (1 << b)) wshift = b;
   if (prec == MLC_F64) {
     MapList<double> ml{};
     for (int q = 0; q < nmaps; q++) ml.m[q] = (const double*)maps_host[q];
     MLC_KSCOPE(ctx, "interleave");
-    k_interleave<double><<<grid, 256, 0, ctx->stream>>>(ml, nmaps, stride, npix, (double*)out);
+    k_interleave<double><<<grid, 256, 0, ctx->stream>>>(ml, nmaps, width, wshift, S, off, npix, (double*)out);
   } else {
     MapList<float> ml{};
     for (int q = 0; q < nmaps; q++) ml.m[q] = (const float*)maps_host[q];
     MLC_KSCOPE(ctx, "interleave");
-    k_interleave<float><<<grid, 256, 0, ctx->stream>>>(ml, nmaps, stride, npix, (float*)out);
+    k_interleave<float><<<grid, 256, 0, ctx->stream>>>(ml, nmaps, width, wshift, S, off, npix, (float*)out);
   }
   MLC_CHECK_LAUNCH();
+}
+
+void interleave(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int stride, void* out) {
+  interleave_impl(ctx, maps_host, nmaps, stride, stride, 0, npix, prec, out);
+}
+
+void interleave_into(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long npix, int prec, int S, int off,
+                     void* out) {
+  interleave_impl(ctx, maps_host, nmaps, nmaps, S, off, npix, prec, out);
 }
 
 template <typename T>

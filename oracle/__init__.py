@@ -79,6 +79,9 @@ def lib():
         L.orc_flux_ratio.restype = C.c_double
         L.orc_flux_ratio_f32.argtypes = [_fp, _fp, _fp, _fp, C.c_int, C.c_int, C.c_int]
         L.orc_flux_ratio_f32.restype = C.c_float
+        L.orc_fit_raster.argtypes = [C.c_double, C.c_double, C.c_int, _dp, _dp, _dp, _dp]
+        L.orc_track_fit.argtypes = [_dp, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _lp, _dp, _dp, _dp, _dp,
+                                    _dp, C.c_void_p]
         L.orc_binned_mpd.argtypes = [_dp, C.c_long, C.c_int, C.c_double, C.c_double, _dp, _dp]
         L.orc_mpd_divide.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp, C.c_int, _dp, _dp]
         L.orc_mpd_normalize.argtypes = [C.c_int, _dp, _dp]
@@ -319,6 +322,38 @@ def flux_ratio_f32(f_obs, df_obs, mu1, mu2):
     m1 = np.ascontiguousarray(mu1, np.float32); m2 = np.ascontiguousarray(mu2, np.float32)
     N, F, T = m1.shape
     return lib().orc_flux_ratio_f32(fo, dfo, m1.ravel(), m2.ravel(), N, F, T)
+
+
+def fit_raster(rhalf, pix, N):
+    """(P, dP/dx, dP/dy, dP/dR) N x N rasters of the smooth thin disc."""
+    out = [np.zeros(N * N) for _ in range(4)]
+    lib().orc_fit_raster(rhalf, pix, N, *out)
+    return tuple(a.reshape(N, N) for a in out)
+
+
+def radius_stack(mp, radii, pix, N):
+    """(Ny, Nx, K, 4) FP64: the map convolved with P, dP/dx, dP/dy, dP/dR for each radius."""
+    Ny, Nx = mp.shape
+    st = np.zeros((Ny, Nx, len(radii), 4))
+    for k, R in enumerate(radii):
+        for f, r in enumerate(fit_raster(R, pix, N)):
+            st[:, :, k, f] = conv_fft(mp, r)
+    return st
+
+
+def track_fit(stack, radii, theta, off, t, obs, w, model=False):
+    """FP64 chi2 (n,), gradient (n, 6) and optionally the model magnitudes."""
+    st = np.ascontiguousarray(stack, np.float64)
+    Ny, Nx, K, _ = st.shape
+    th = np.ascontiguousarray(theta, np.float64)
+    n = th.shape[0]
+    chi2 = np.zeros(n); grad = np.zeros((n, 6))
+    mod = np.zeros(len(t)) if model else None
+    lib().orc_track_fit(st.ravel(), Nx, Ny, K, np.ascontiguousarray(radii, np.float64), n, th.ravel(),
+                        np.ascontiguousarray(off, np.int64), np.ascontiguousarray(t, np.float64),
+                        np.ascontiguousarray(obs, np.float64), np.ascontiguousarray(w, np.float64), chi2, grad,
+                        None if mod is None else mod.ctypes.data_as(C.c_void_p))
+    return (chi2, grad, mod) if model else (chi2, grad)
 
 
 def trapezium(f1, f2, x):

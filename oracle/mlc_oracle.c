@@ -455,6 +455,129 @@ void orc_mpd_normalize(int N, const double* bins, double* counts) {
   for (int i = 0; i < N; i++) counts[i] /= s;
 }
 
+/* ---- differentiable track fit (no reference counterpart; restated from the model) ---- */
+
+/* Thin-disc law of profile.cpp:402-446 on a fixed N x N grid, flat core kept, no outer
+ * truncation; P normalised; Px, Py = dP/dx, dP/dy per pixel of offset, PR = dP/drhalf
+ * (quotient rule for the normalisation). */
+int orc_fit_raster(double rhalf, double pix, int N, double* P, double* Px, double* Py, double* PR) {
+  const double sig = 0.4106 * rhalf;
+  const double core = 10.0 / (exp(pow(1.0 / 0.4106, 0.75)) - 1.0);
+  double S = 0.0, T = 0.0;
+  for (int i = 0; i < N; i++)
+    for (int j = 0; j < N; j++) {
+      const double y = (i - N / 2) * pix + pix / 2.0, x = (j - N / 2) * pix + pix / 2.0;
+      const double r = sqrt(x * x + y * y), u = r / sig;
+      const double E = exp(pow(u, 0.75));
+      double v = 1.0 / (E - 1.0), gx = 0.0, gy = 0.0, gr = 0.0;
+      if (v >= core) {
+        v = core;
+      } else {
+        /* dv/du = -(3/4) u^(-1/4) E / (E-1)^2 ; du/dx = x / (r sig) ; du/dR = -u / R */
+        const double dvdu = -0.75 * pow(u, -0.25) * E / ((E - 1.0) * (E - 1.0));
+        gx = dvdu * x / (r * sig) * pix;
+        gy = dvdu * y / (r * sig) * pix;
+        gr = -dvdu * u / rhalf;
+      }
+      P[i * N + j] = v;
+      Px[i * N + j] = gx;
+      Py[i * N + j] = gy;
+      PR[i * N + j] = gr;
+      S += v;
+      T += gr;
+    }
+  for (int k = 0; k < N * N; k++) {
+    P[k] /= S;
+    Px[k] /= S;
+    Py[k] /= S;
+    PR[k] = PR[k] / S - P[k] * T / S;
+  }
+  return N;
+}
+
+/* Cubic Hermite basis on [0,1]: b[0..3] = h00, h01, h10, h11 and d[0..3] their derivatives. */
+static void orc_herm(double s, double* b, double* d) {
+  b[0] = 2 * s * s * s - 3 * s * s + 1;
+  b[1] = -2 * s * s * s + 3 * s * s;
+  b[2] = s * s * s - 2 * s * s + s;
+  b[3] = s * s * s - s * s;
+  d[0] = 6 * s * s - 6 * s;
+  d[1] = -6 * s * s + 6 * s;
+  d[2] = 3 * s * s - 4 * s + 1;
+  d[3] = 3 * s * s - 2 * s;
+}
+
+/* Model value and first derivatives at (x, y, R): tensor-product cubic Hermite in x, y
+ * (nodes at pixel centres, unit spacing) and R (nodes radii[k]) of the stack's node values
+ * M and derivatives Mx, My, MR, st[((i Nx + j) K + k) 4 + f], without cross-derivative
+ * terms.  Returns 0 outside the hull of pixel centres. */
+static int orc_fit_eval(const double* st, int Nx, int Ny, int K, const double* radii, double x, double y, double R,
+                        double* F, double* Fx, double* Fy, double* FR) {
+  if (x < 0.5 || x > Nx - 0.5 || y < 0.5 || y > Ny - 0.5) return 0;
+  int j0 = (int)floor(x - 0.5), i0 = (int)floor(y - 0.5);
+  if (j0 > Nx - 2) j0 = Nx - 2;
+  if (i0 > Ny - 2) i0 = Ny - 2;
+  const double sx = x - (j0 + 0.5), sy = y - (i0 + 0.5);
+  int k = 0;
+  while (k < K - 2 && R >= radii[k + 1]) k++;
+  const double h = radii[k + 1] - radii[k];
+  double sr = (R - radii[k]) / h;
+  int cl = 0;
+  if (sr < 0) { sr = 0; cl = 1; }
+  if (sr > 1) { sr = 1; cl = 1; }
+  double bx[4], dx[4], by[4], dy[4], br[4], dr[4];
+  orc_herm(sx, bx, dx);
+  orc_herm(sy, by, dy);
+  orc_herm(sr, br, dr);
+  *F = *Fx = *Fy = *FR = 0.0;
+  for (int b = 0; b < 2; b++)     /* y node */
+    for (int a = 0; a < 2; a++)   /* x node */
+      for (int c = 0; c < 2; c++) { /* radius node */
+        const double* q = st + (((long)(i0 + b) * Nx + (j0 + a)) * K + k + c) * 4;
+        const double vx = bx[a], tx = bx[2 + a], vy = by[b], ty = by[2 + b];
+        const double wr = br[c], ur = br[2 + c] * h;
+        const double dwr = cl ? 0 : dr[c] / h, dur = cl ? 0 : dr[2 + c];
+        *F += vx * vy * (wr * q[0] + ur * q[3]) + tx * vy * wr * q[1] + vx * ty * wr * q[2];
+        *Fx += dx[a] * vy * (wr * q[0] + ur * q[3]) + dx[2 + a] * vy * wr * q[1] + dx[a] * ty * wr * q[2];
+        *Fy += vx * dy[b] * (wr * q[0] + ur * q[3]) + tx * dy[b] * wr * q[1] + vx * dy[2 + b] * wr * q[2];
+        *FR += vx * vy * (dwr * q[0] + dur * q[3]) + tx * vy * dwr * q[1] + vx * ty * dwr * q[2];
+      }
+  return 1;
+}
+
+void orc_track_fit(const double* st, int Nx, int Ny, int K, const double* radii, int n, const double* theta,
+                   const long* off, const double* t, const double* obs, const double* w, double* chi2,
+                   double* grad, double* model) {
+  for (int i = 0; i < n; i++) {
+    const double* th = theta + 6 * i;
+    double c2 = 0, g[6] = {0, 0, 0, 0, 0, 0};
+    for (long e = off[i]; e < off[i + 1]; e++) {
+      const double vt = th[3] * t[e];
+      const double x = th[0] + vt * cos(th[2]), y = th[1] + vt * sin(th[2]);
+      double M, Mx, My, MR;
+      if (!orc_fit_eval(st, Nx, Ny, K, radii, x, y, th[4], &M, &Mx, &My, &MR) || !(M > 0)) {
+        if (model) model[e] = NAN;
+        continue;
+      }
+      const double m = -2.5 * log10(M) + th[5];
+      if (model) model[e] = m;
+      const double r = obs[e] - m;
+      c2 += w[e] * r * r;
+      const double gm = -2.0 * w[e] * r;
+      const double gM = gm * (-2.5 / log(10.0)) / M;
+      g[0] += gM * Mx;
+      g[1] += gM * My;
+      g[2] += gM * (-vt * sin(th[2]) * Mx + vt * cos(th[2]) * My);
+      g[3] += gM * (t[e] * cos(th[2]) * Mx + t[e] * sin(th[2]) * My);
+      g[4] += gM * MR;
+      g[5] += gm;
+    }
+    chi2[i] = c2;
+    if (grad)
+      for (int j = 0; j < 6; j++) grad[6 * i + j] = g[j];
+  }
+}
+
 /* getChi2CPU (chi2/chi2_functions.cuh:150-190) restated in FP64: chi2[y*N + x] =
  * 1/2 sum_{f,t} ((fo - m1[x]/m2[y]) / df)^2 and the likelihood sum of exp(-chi2). */
 double orc_flux_ratio(const float* fo, const float* dfo, const float* m1, const float* m2, int N, int F, int T,

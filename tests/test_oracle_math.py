@@ -69,3 +69,34 @@ def test_synthetic_map_statistics():
     mp, counts, meta = synth.rayshoot_numpy(64, 4.0, 0.4, 0.4, seed=0, rays_per_pixel=16)
     assert mp.shape == (64, 64) and counts.dtype == np.int32
     assert 0.7 < mp.mean() < 1.3 and (mp >= 0).all()
+
+
+def test_fit_raster_derivatives():
+    """The smooth thin-disc raster's derivative rasters equal central differences of the
+    same law evaluated at shifted offsets (x, y) and radii (library and oracle agree)."""
+    import microsn_gb300 as mlc
+    N, pix = 64, 1.0
+
+    def law(x, y, R):
+        sig = 0.4106 * R
+        core = 10.0 / (np.exp((1 / 0.4106) ** 0.75) - 1.0)
+        u = np.hypot(x, y) / sig
+        with np.errstate(divide="ignore"):
+            v = 1.0 / (np.exp(u ** 0.75) - 1.0)
+        return np.minimum(v, core)
+
+    for R in (3.3, 9.0, 14.5):
+        P, Px, Py, PR = mlc.fit_raster(R, pix, N)
+        for a, b in zip((P, Px, Py, PR), oracle.fit_raster(R, pix, N)):
+            assert np.max(np.abs(a - b)) <= 1e-15 * np.max(np.abs(a))
+        c = (np.arange(N) - N // 2) * pix + pix / 2.0
+        X, Y = np.meshgrid(c, c)
+        S = law(X, Y, R).sum()
+        h = 1e-5
+        fx = (law(X + h, Y, R) - law(X - h, Y, R)) / (2 * h) / S
+        fy = (law(X, Y + h, R) - law(X, Y - h, R)) / (2 * h) / S
+        assert np.max(np.abs(fx - Px)) <= 1e-6 * np.max(np.abs(Px))
+        assert np.max(np.abs(fy - Py)) <= 1e-6 * np.max(np.abs(Py))
+        Pp = mlc.fit_raster(R * (1 + 1e-6), pix, N)[0]
+        Pm = mlc.fit_raster(R * (1 - 1e-6), pix, N)[0]
+        assert np.max(np.abs((Pp - Pm) / (2e-6 * R) - PR)) <= 1e-6 * np.max(np.abs(PR))
