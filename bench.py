@@ -198,6 +198,205 @@ def bf16_peak():
 PAIR_N, PAIR_T, PAIR_BINS, PAIR_K = 100_000, 128, 1000, 10_000
 
 
+# configs[0], the small plain-FP64 end-to-end case: 2000^2 ray-shot map (kappa* = 0.4,
+# gamma = 0.4, width 20, seed 0) convolved with a Gaussian of sigma 10 px, 10^4 straight
+# tracks of 50 epochs at 5 px per epoch, offset chi2 against one noisy observed curve,
+# sort and a 100-bin histogram.
+C1_N, C1_TRACKS, C1_T = 2000, 10_000, 50
+
+
+def c1_workload(args, ctx, dev, rank):
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    from microsn_gb300 import synth
+    mp, _ = synth.rayshoot_gpu(ctx, C1_N, 20.0, 0.4, 0.4, seed=0 + rank, rays_per_pixel=4.0, dtype=torch.float64)
+    m = mlc.Map(ctx, mp, "f64")
+    prof = mlc.profile("gaussian", 1.18 * 10.0, 1.0, ref_compat=False)
+    rng = np.random.default_rng(1 + rank)
+    L = 5.0 * (C1_T - 1)
+    phi = rng.uniform(0, 2 * np.pi, C1_TRACKS)
+    lo = 40.0 + np.maximum(-L * np.cos(phi), 0), 40.0 + np.maximum(-L * np.sin(phi), 0)
+    x0 = lo[0] + rng.uniform(0, 1, C1_TRACKS) * (C1_N - 80.0 - np.abs(L * np.cos(phi)))
+    y0 = lo[1] + rng.uniform(0, 1, C1_TRACKS) * (C1_N - 80.0 - np.abs(L * np.sin(phi)))
+    D = lambda a: torch.as_tensor(a, dtype=torch.float64, device=dev)
+    tr = [D(x0), D(y0), D(phi), D(np.full(C1_TRACKS, 5.0))]
+    t = D(np.arange(C1_T, dtype=np.float64))
+    conv = mlc.convolve(ctx, m, prof, "fused")
+    off1 = torch.tensor([0, C1_T], dtype=torch.int64, device=dev)
+    lc0 = mlc.sample_tracks(ctx, [conv], C1_N, C1_N, tr[0][:1], tr[1][:1], tr[2][:1], tr[3][:1], off1, t, mag=True)
+    obs = D(lc0[0].cpu().numpy() + rng.normal(0, 0.05, C1_T))
+    w = D(np.full(C1_T, 1 / 0.05 ** 2))
+    chi2 = torch.empty((1, C1_TRACKS), dtype=torch.float64, device=dev)
+    idx = torch.empty(C1_TRACKS, dtype=torch.int32, device=dev)
+
+    def step(mode):
+        m.refresh()
+        mlc.convolve(ctx, m, prof, mode, out=conv)
+        mlc.track_chi2_offset(ctx, conv, 1, *tr, t, obs, w, out=chi2)
+        torch.arange(C1_TRACKS, dtype=torch.int32, device=dev, out=idx)
+        mlc.sort_f64_u32(ctx, chi2[0], idx)
+        return mlc.histogram_f64(ctx, chi2[0], 100, 0.0, 7.0, log=True)
+
+    def plain_step():
+        # one launch per stage, FP64: plain convolution, light curves to memory, offset chi2
+        m.refresh()
+        mlc.convolve(ctx, m, prof, "plain", out=conv)
+        offs = torch.arange(0, (C1_TRACKS + 1) * C1_T, C1_T, dtype=torch.int64, device=dev)
+        lc = mlc.sample_tracks(ctx, [conv], C1_N, C1_N, *tr, offs, t.repeat(C1_TRACKS), mag=True)
+        c2, _ = mlc.chi2_offset(ctx, lc[0].reshape(C1_TRACKS, C1_T), obs.cpu().numpy(), w.cpu().numpy())
+        torch.arange(C1_TRACKS, dtype=torch.int32, device=dev, out=idx)
+        mlc.sort_f64_u32(ctx, c2, idx)
+        return mlc.histogram_f64(ctx, c2, 100, 0.0, 7.0, log=True)
+
+    out = {}
+    for name, fn in (("fused", lambda: step("fused")), ("plain", plain_step)):
+        for _ in range(max(args.warmup, 1)):
+            h = fn()
+        torch.cuda.synchronize()
+        steps = max(1, min(args.steps, 10))
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            h = fn()
+        e1.record(); torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[name] = {"ms_per_step": ms, "light_curves_per_s": C1_TRACKS / (ms / 1000.0),
+                     "histogram_total": int(np.asarray(h).sum())}
+    # the same step on the host cores (oracle FP64: scipy FFT convolution + bilinear + offset chi2)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.build()
+        mph = mp.cpu().numpy()
+        P = mlc.profile_raster(prof)
+        t0 = time.perf_counter()
+        cm = oracle.conv_fft_workers(mph, P)
+        offs = np.arange(0, (C1_TRACKS + 1) * C1_T, C1_T, dtype=np.int64)
+        lc = oracle.sample_tracks(cm, x0, y0, phi, np.full(C1_TRACKS, 5.0), offs, np.tile(np.arange(C1_T, dtype=float),
+                                                                                          C1_TRACKS), mag=True)
+        c2, _ = oracle.chi2_offset(lc.reshape(C1_TRACKS, C1_T), obs.cpu().numpy(), w.cpu().numpy())
+        np.sort(c2)
+        np.histogram(np.log10(c2), bins=100, range=(0.0, 7.0))
+        dt_ = time.perf_counter() - t0
+        cpu = {"kind": "port", "cores": os.cpu_count(), "ms_per_step": dt_ * 1000.0,
+               "light_curves_per_s": C1_TRACKS / dt_}
+    m.close()
+    return {"workload": "configs[0]: 2000^2 FP64 ray-shot map, Gaussian sigma 10 px, 10^4 tracks x 50 epochs, "
+                        "offset chi2 vs one noisy curve, radix sort, 100-bin log10 chi2 histogram",
+            "fused": out["fused"], "plain_fp64": out["plain"],
+            "fused_over_plain": out["plain"]["ms_per_step"] / out["fused"]["ms_per_step"], "cpu": cpu,
+            "dtype": "f64"}
+
+
+# configs[3], the differentiable fit: 4000^2 FP32 map, thin-disc radius stack (16 radii,
+# 4..32 px), 4096 tracks = 64 targets x 64 perturbed starts, 80 uneven epochs each, fused
+# chi2 + gradient kernel with an Adam step, replayed from a CUDA graph.
+C4_N, C4_TARGETS, C4_STARTS, C4_T = 4000, 64, 64, 80
+
+
+def c4_workload(args, ctx, dev, rank):
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    from microsn_gb300 import synth
+    mp, _ = synth.rayshoot_gpu(ctx, C4_N, 20.0, 0.45, 0.35, seed=5 + rank, rays_per_pixel=4.0, dtype=torch.float32)
+    m = mlc.Map(ctx, mp, "f32")
+    radii = list(np.geomspace(4.0, 32.0, 16))
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    stack = mlc.radius_stack(ctx, m, radii)
+    e1.record(); torch.cuda.synchronize()
+    stack_ms = e0.elapsed_time(e1)
+    rng = np.random.default_rng(5 + rank)
+    n = C4_TARGETS * C4_STARTS
+    t1 = np.sort(rng.integers(0, 3, (C4_TARGETS, C4_T)) * 365.0 + rng.uniform(0, 150, (C4_TARGETS, C4_T)), axis=1)
+    v = rng.uniform(0.02, 0.08, C4_TARGETS); phi = rng.uniform(0, 2 * np.pi, C4_TARGETS)
+    span = v * t1[:, -1]
+    mg = 80.0
+    x0 = mg + np.maximum(-span * np.cos(phi), 0) + rng.uniform(0, 1, C4_TARGETS) * (C4_N - 2 * mg - np.abs(span * np.cos(phi)))
+    y0 = mg + np.maximum(-span * np.sin(phi), 0) + rng.uniform(0, 1, C4_TARGETS) * (C4_N - 2 * mg - np.abs(span * np.sin(phi)))
+    true = np.stack([x0, y0, phi, v, rng.uniform(8, 16, C4_TARGETS), rng.uniform(-0.3, 0.3, C4_TARGETS)], 1)
+    D = lambda a, dt=torch.float32: torch.as_tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    offT = np.arange(C4_TARGETS + 1, dtype=np.int64) * C4_T
+    _, _, model = mlc.track_fit(ctx, stack, radii, D(true), D(offT, torch.int64), D(t1.ravel()),
+                                D(np.zeros(C4_TARGETS * C4_T)), D(np.ones(C4_TARGETS * C4_T)), grad=False, model=True)
+    obs1 = model.cpu().numpy() + rng.normal(0, 0.02, C4_TARGETS * C4_T)
+    idx = np.repeat(np.arange(C4_TARGETS), C4_STARTS)
+    scale = np.array([2.0, 2.0, 0.02, 0.002, 1.5, 0.1])
+    th0 = true[idx] + rng.normal(0, 1, (n, 6)) * scale
+    th0[:, 4] = np.clip(th0[:, 4], radii[0], radii[-1])
+    sel = (idx[:, None] * C4_T + np.arange(C4_T)[None, :]).ravel()
+    off = D(np.arange(n + 1, dtype=np.int64) * C4_T, torch.int64)
+    t = D(t1.ravel()[sel]); obs = D(obs1[sel]); w = D(np.full(n * C4_T, 1 / 0.02 ** 2))
+    sc = D(scale)
+    u = D(th0 / scale)
+    th = torch.empty_like(u)
+    c2 = torch.empty(n, dtype=torch.float32, device=dev)
+    g = torch.empty((n, 6), dtype=torch.float32, device=dev)
+    m1 = torch.zeros_like(u); m2 = torch.zeros_like(u)
+    b1, b2, lr, eps = 0.9, 0.999, 0.05, 1e-8
+    bc = torch.ones(2, dtype=torch.float32, device=dev)  # running bias corrections
+    betas = torch.tensor([b1, b2], dtype=torch.float32, device=dev)
+
+    def it():
+        torch.mul(u, sc, out=th)
+        mlc.track_fit(ctx, stack, radii, th, off, t, obs, w, out_chi2=c2, out_grad=g)
+        gu = g * sc
+        m1.mul_(b1).add_(gu, alpha=1 - b1)
+        m2.mul_(b2).addcmul_(gu, gu, value=1 - b2)
+        bc.mul_(betas)
+        u.sub_(lr * (m1 / (1 - bc[0])) / ((m2 / (1 - bc[1])).sqrt() + eps))
+
+    # warm up on a side stream, capture one iteration, replay it
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    old = ctx.stream
+    with torch.cuda.stream(s):
+        ctx.set_stream(s)
+        u0 = u.clone()
+        for _ in range(3):
+            it()
+        u.copy_(u0); m1.zero_(); m2.zero_(); bc.fill_(1.0)
+    torch.cuda.current_stream().wait_stream(s)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        ctx.set_stream(torch.cuda.current_stream())
+        it()
+    ctx.set_stream(old)
+    iters = 300
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(iters):
+        graph.replay()
+    e1.record(); torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    # kernel-only throughput of the fused chi2 + gradient kernel
+    ctx.set_timing(True)
+    for _ in range(20):
+        mlc.track_fit(ctx, stack, radii, th, off, t, obs, w, out_chi2=c2, out_grad=g)
+    kt = ctx.kernel_times(reset=True)
+    ctx.set_timing(False)
+    k_ms = kt["track_fit"][0] / kt["track_fit"][1]
+    final = c2.cpu().numpy().reshape(C4_TARGETS, C4_STARTS)
+    torch.mul(u, sc, out=th)
+    mlc.track_fit(ctx, stack, radii, D(true), D(offT, torch.int64), D(t1.ravel()), D(obs1),
+                  D(np.full(C4_TARGETS * C4_T, 1 / 0.02 ** 2)), out_chi2=c2[:C4_TARGETS], out_grad=g[:C4_TARGETS])
+    true_c2 = c2[:C4_TARGETS].cpu().numpy()
+    recovered = float(np.mean(final.min(axis=1) <= 1.2 * true_c2 + 5.0))
+    m.close()
+    return {"workload": "configs[3]: 4000^2 FP32 map, 16-radius thin-disc stack, 4096 tracks (64 targets x 64 "
+                        "starts) x 80 uneven epochs, 6 parameters, Adam from a CUDA graph",
+            "stack_build_ms": stack_ms, "iteration_ms": ms / iters,
+            "gradient_evaluations_per_s": n / (ms / iters / 1000.0),
+            "kernel_ms": k_ms, "track_epochs_per_s_kernel": n * C4_T / (k_ms / 1000.0),
+            "iterations": iters, "targets_recovered_fraction": recovered,
+            "median_best_over_true_chi2": float(np.median(final.min(axis=1) / true_c2))}
+
+
 # Multi-filter flux-ratio likelihood at the reference chi2 driver's size
 # (chi2/chi2_driver.cu: N = 10^4 locations per image, F = 7 filters, T = 10 epochs).
 FR_N, FR_F, FR_T = 10_000, 7, 10
@@ -592,9 +791,11 @@ def main():
     pair = None
     if not args.no_pair:
         pair = pair_workload(args, ctx, m, profs, n, dev, world, rank, stream)
-    flux = None
+    flux = c1 = c4 = None
     if not args.no_pair:
         flux = flux_ratio_workload(args, ctx, dev, rank)
+        c1 = c1_workload(args, ctx, dev, rank)
+        c4 = c4_workload(args, ctx, dev, rank)
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -611,7 +812,7 @@ def main():
                        "ms_per_step": e2e_ms},
                "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
                "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair,
-               "flux_ratio": flux}
+               "flux_ratio": flux, "c1_small_fp64": c1, "c4_fit": c4}
         print(json.dumps(res), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

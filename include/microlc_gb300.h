@@ -296,6 +296,20 @@ int mlc_mpd_divide(mlc_ctx* ctx, int NA, const double* binsA_host, const double*
 
 /* ======================================================================= chi2 vs one observed curve */
 
+/* Fused sample -> magnitude -> offset-minimised chi2, no light curve written: for each of
+ * ntracks straight tracks (x0, y0, phi, v as in mlc_sample_tracks) sampled at the shared
+ * epochs t[Tn] on each of the nmaps maps of an interleaved map (mlc_interleave_maps,
+ * stride a power of two <= 16; stride 1 is a plain map), m = -2.5 log10(mu) and
+ *   dm = sum w (o - m) / sum w,  chi2 = sum w (o - m - dm)^2     (FP64 accumulation)
+ * against the observed curve obs[Tn] with weights w[Tn] (FP64).  chi2[q*ntracks + i],
+ * dm[q*ntracks + i] (dm may be NULL), FP64 device arrays.  A position outside the map makes
+ * that chi2 +inf.  One kernel, no allocation or synchronisation.  No reference
+ * counterpart (the reference has no offset solve). */
+int mlc_track_chi2_offset(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int precision,
+                          int ntracks, const void* x0, const void* y0, const void* phi, const void* v, int Tn,
+                          const void* t, const double* obs, const double* w, double* chi2, double* dm);
+
+
 /* Offset-minimised chi2 of ncurves magnitude curves of T epochs (m, row-major, the
  * given precision) against one observed curve obs_host / weights w_host (FP64, T):
  * dm = sum w (o - m) / sum w (FP64), chi2 = sum w (o - m - dm)^2.  No reference

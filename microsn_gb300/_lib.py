@@ -78,6 +78,7 @@ SIGNATURES = {
     "mlc_convolve_sample_tracks": (i32, [vp, vp, vp, i32, C.POINTER(MlcProfile), C.POINTER(MlcTracks), i32, i32, vp,
                                          i32]),
     "mlc_ctx_join": (i32, [vp]),
+    "mlc_track_chi2_offset": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp]),
     "mlc_fit_raster": (i32, [f64, f64, i32, vp, vp, vp, vp]),
     "mlc_radius_stack": (i32, [vp, vp, i32, vp, f64, i32, vp]),
     "mlc_track_fit": (i32, [vp, vp, i32, i32, i32, i32, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp]),

@@ -422,6 +422,25 @@ def convolve_sample_tracks(ctx: Context, m: Map, profiles, tracks: dict, mag=Tru
     return out
 
 
+def track_chi2_offset(ctx: Context, imap: torch.Tensor, nmaps: int, x0, y0, phi, v, t, obs, w, out=None):
+    """Fused sample -> magnitude -> offset-minimised chi2 of every track against one
+    observed curve on shared epochs t (T,).  imap: (Ny, Nx) map or (Ny, Nx, stride)
+    interleaved maps; obs, w: (T,) float64 CUDA tensors.  Returns (chi2, dm), each
+    (nmaps, ntracks) float64."""
+    if imap.dim() == 2:
+        Ny, Nx = imap.shape
+        stride = 1
+    else:
+        Ny, Nx, stride = imap.shape
+    n = x0.numel()
+    chi2 = out if out is not None else torch.empty((nmaps, n), dtype=torch.float64, device=x0.device)
+    dm = torch.empty((nmaps, n), dtype=torch.float64, device=x0.device)
+    ctx.check(ctx.L.mlc_track_chi2_offset(ctx.h, _ptr(imap), stride, nmaps, Nx, Ny, _PREC[imap.dtype], n, _ptr(x0),
+                                          _ptr(y0), _ptr(phi), _ptr(v), t.numel(), _ptr(t), _ptr(obs), _ptr(w),
+                                          _ptr(chi2), _ptr(dm)))
+    return chi2, dm
+
+
 def chi2_offset(ctx: Context, m: torch.Tensor, obs, w):
     """Offset-minimised chi2 of each row of m against obs with weights w."""
     n, T = m.shape

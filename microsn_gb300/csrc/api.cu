@@ -385,6 +385,19 @@ int mlc_interleave_maps(mlc_ctx* ctx, const void* const* maps_host, int nmaps, i
   return guarded(ctx, [&] { interleave(ctx, maps_host, nmaps, (long)Nx * Ny, precision, stride, out); });
 }
 
+int mlc_track_chi2_offset(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int precision,
+                          int ntracks, const void* x0, const void* y0, const void* phi, const void* v, int Tn,
+                          const void* t, const double* obs, const double* w, double* chi2, double* dm) {
+  if (!ctx || !imap || !x0 || !y0 || !phi || !v || !t || !obs || !w || !chi2)
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (nmaps < 1 || !pow2_le16(stride) || stride < nmaps || Nx < 2 || Ny < 2 || ntracks < 0 || Tn < 1 ||
+      (precision != MLC_F64 && precision != MLC_F32))
+    return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  return guarded(ctx, [&] {
+    track_chi2_offset(ctx, imap, stride, nmaps, Nx, Ny, precision, ntracks, x0, y0, phi, v, Tn, t, obs, w, chi2, dm);
+  });
+}
+
 int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof,
                                const mlc_profile* profiles_host, const mlc_tracks* tracks, int mode, int mag, void* out,
                                int flags) {

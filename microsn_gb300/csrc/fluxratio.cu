@@ -10,7 +10,8 @@
 // on one host core.  Here one CTA owns a 64 x 64 tile of pairs (each thread 4 x 4):
 // the K = F*T values of its 64 + 64 locations are staged through shared memory in
 // chunks of 32 with 1/mu2 and 1/df precomputed, so a pair costs 3 FP32 operations per
-// (filter, time); exp(-chi2) is summed in FP64 per CTA and the CTA sums are added in a
+// (filter, time); exp(-chi2) is summed per thread relative to its smallest chi2 (FP32
+// terms, one FP64-range exp per thread), per CTA in FP64, and the CTA sums are added in a
 // fixed order (deterministic).  chi2 is stored only when asked for.
 #include <vector>
 
@@ -74,7 +75,16 @@ __global__ void __launch_bounds__(256) k_flux_ratio(const float* __restrict__ mu
     __syncthreads();
   }
 
-  double lsum = 0.0;
+  // sum of exp(-chi2) over this thread's pairs as exp(-cmin) * sum expf(cmin - chi2): the
+  // FP32 terms are in (0, 1] and only those below e^-87 of the largest underflow, and
+  // one exp per thread takes the FP64 path when cmin is beyond the FP32 exp range
+  float cmin = INFINITY;
+#pragma unroll
+  for (int j = 0; j < 4; j++)
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+      if (x0 + tx * 4 + i < N && y0 + ty * 4 + j < N) cmin = fminf(cmin, 0.5f * acc[j][i]);
+  float esum = 0.f;
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     const int y = y0 + ty * 4 + j;
@@ -83,8 +93,7 @@ __global__ void __launch_bounds__(256) k_flux_ratio(const float* __restrict__ mu
     for (int i = 0; i < 4; i++) {
       c[i] = 0.5f * acc[j][i];
       const int x = x0 + tx * 4 + i;
-      // FP32 exp underflows beyond chi2 ~ 87: those terms take the FP64 exp
-      if (x < N && y < N) lsum += c[i] < 80.f ? (double)expf(-c[i]) : exp(-(double)c[i]);
+      if (x < N && y < N) esum += expf(cmin - c[i]);
     }
     if (chi2 && y < N) {
       const int x = x0 + tx * 4;
@@ -97,6 +106,8 @@ __global__ void __launch_bounds__(256) k_flux_ratio(const float* __restrict__ mu
       }
     }
   }
+  double lsum = 0.0;
+  if (esum > 0.f) lsum = (cmin < 80.f ? (double)expf(-cmin) : exp(-(double)cmin)) * (double)esum;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
   if ((tid & 31) == 0) red[tid >> 5] = lsum;

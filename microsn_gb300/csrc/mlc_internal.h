@@ -175,6 +175,10 @@ void interleave_into(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long
 void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
                       const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
                       const void* t, int mag, void* out, long E, int64_t ebase);
+// Fused sample -> magnitude -> offset-minimised chi2 against one curve on shared epochs.
+void track_chi2_offset(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
+                       const void* x0, const void* y0, const void* phi, const void* v, int Tn, const void* t,
+                       const double* obs, const double* w, double* chi2, double* dm);
 void sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int Nprof, int Nloc, const int* lx,
                     const int* ly, double* LC, double* DLC);
 

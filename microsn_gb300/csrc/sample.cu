@@ -282,6 +282,144 @@ void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int
   MLC_CHECK_LAUNCH();
 }
 
+// Fused sample -> magnitude -> offset-minimised chi2 of every track against one observed
+// curve on shared epochs t[T] (no light curve is written): one warp per track, lanes over
+// the epochs.  Pass 1 samples the NM interleaved maps and accumulates sum w (o - m) per
+// map (FP64) to get the offset dm = sum w (o - m) / W; pass 2 samples again (the same
+// addresses, now L1 hits) and accumulates sum w (o - m - dm)^2, so the chi2 never comes
+// from the cancellation-prone single-pass form.  An epoch outside the hull samples 0
+// (magnitude +inf) and makes that map's chi2 +inf, as the light curve would.
+template <typename T, int NM>
+__device__ __forceinline__ void sample_mags(const T* __restrict__ imap, int Nx, int Ny, long bx, T fx, long by, T fy,
+                                            T* m) {
+  const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
+  if (!B.inside) {
+#pragma unroll
+    for (int q = 0; q < NM; q++) m[q] = (T)INFINITY;
+    return;
+  }
+  T a[NM], b[NM], c[NM], d[NM];
+  load_pix<T, NM>(imap + ((long)B.iu * Nx + B.jl) * NM, a);
+  load_pix<T, NM>(imap + ((long)B.iu * Nx + B.jr) * NM, b);
+  load_pix<T, NM>(imap + ((long)B.il * Nx + B.jl) * NM, c);
+  load_pix<T, NM>(imap + ((long)B.il * Nx + B.jr) * NM, d);
+#pragma unroll
+  for (int q = 0; q < NM; q++) {
+    T z = B.w0 * a[q];
+    z += B.w1 * b[q];
+    z += B.w2 * c[q];
+    z += B.w3 * d[q];
+    m[q] = (T)-2.5 * mlc_log10(z);
+  }
+}
+
+template <typename T, int NM>
+__global__ void __launch_bounds__(256) k_track_chi2_offset(const T* __restrict__ imap, int nm_out, int Nx, int Ny,
+                                                           int ntracks, const T* __restrict__ x0,
+                                                           const T* __restrict__ y0, const T* __restrict__ phi,
+                                                           const T* __restrict__ v, int Tn, const T* __restrict__ t,
+                                                           const double* __restrict__ obs,
+                                                           const double* __restrict__ w,
+                                                           double* __restrict__ chi2, double* __restrict__ dm) {
+  const int lane = threadIdx.x & 31;
+  const long tr = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (tr >= ntracks) return;
+  const T X0 = x0[tr], Y0 = y0[tr], V = v[tr];
+  T sn, cs;
+  if (sizeof(T) == 8) {
+    double s_, c_;
+    sincos((double)phi[tr], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  } else {
+    float s_, c_;
+    sincosf((float)phi[tr], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  }
+  const long bx = (long)floor(X0), by = (long)floor(Y0);
+  const T fx0 = X0 - (T)bx, fy0 = Y0 - (T)by;
+  double s1[NM], s2[NM], W = 0.0;
+#pragma unroll
+  for (int q = 0; q < NM; q++) s1[q] = s2[q] = 0.0;
+  for (int e = lane; e < Tn; e += 32) {
+    const T vt = V * t[e];
+    T m[NM];
+    sample_mags<T, NM>(imap, Nx, Ny, bx, fx0 + vt * cs, by, fy0 + vt * sn, m);
+    const double we = __ldg(w + e), oe = __ldg(obs + e);
+    W += we;
+#pragma unroll
+    for (int q = 0; q < NM; q++) s1[q] += we * (oe - (double)m[q]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) W += __shfl_xor_sync(0xffffffffu, W, o);
+#pragma unroll
+  for (int q = 0; q < NM; q++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s1[q] += __shfl_xor_sync(0xffffffffu, s1[q], o);
+    s1[q] /= W;  // the offset
+  }
+  for (int e = lane; e < Tn; e += 32) {
+    const T vt = V * t[e];
+    T m[NM];
+    sample_mags<T, NM>(imap, Nx, Ny, bx, fx0 + vt * cs, by, fy0 + vt * sn, m);
+    const double we = __ldg(w + e), oe = __ldg(obs + e);
+#pragma unroll
+    for (int q = 0; q < NM; q++) {
+      const double r = oe - (double)m[q] - s1[q];
+      s2[q] += we * r * r;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NM; q++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s2[q] += __shfl_xor_sync(0xffffffffu, s2[q], o);
+  }
+  if (lane < NM && lane < nm_out) {
+    double c = 0.0, d = 0.0;
+#pragma unroll
+    for (int q = 0; q < NM; q++)
+      if (q == lane) {
+        c = s2[q];
+        d = s1[q];
+      }
+    chi2[(long)lane * ntracks + tr] = c;
+    if (dm) dm[(long)lane * ntracks + tr] = d;
+  }
+}
+
+template <typename T>
+static void track_chi2_offset_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny,
+                                   int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
+                                   int Tn, const void* t, const double* obs, const double* w, double* chi2,
+                                   double* dm) {
+  const int grid = ceil_div(ntracks, 8);
+#define MLC_TC_LAUNCH(NMV)                                                                                   \
+  k_track_chi2_offset<T, NMV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, nmaps, Nx, Ny, ntracks,          \
+                                                            (const T*)x0, (const T*)y0, (const T*)phi,      \
+                                                            (const T*)v, Tn, (const T*)t, obs, w, chi2, dm)
+  MLC_KSCOPE(ctx, "track_chi2_offset");
+  switch (stride) {
+    case 1: MLC_TC_LAUNCH(1); break;
+    case 2: MLC_TC_LAUNCH(2); break;
+    case 4: MLC_TC_LAUNCH(4); break;
+    case 8: MLC_TC_LAUNCH(8); break;
+    default: MLC_TC_LAUNCH(16); break;
+  }
+#undef MLC_TC_LAUNCH
+}
+
+void track_chi2_offset(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
+                       const void* x0, const void* y0, const void* phi, const void* v, int Tn, const void* t,
+                       const double* obs, const double* w, double* chi2, double* dm) {
+  if (ntracks <= 0) return;
+  if (prec == MLC_F64)
+    track_chi2_offset_impl<double>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, Tn, t, obs, w, chi2, dm);
+  else
+    track_chi2_offset_impl<float>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, Tn, t, obs, w, chi2, dm);
+  MLC_CHECK_LAUNCH();
+}
+
 // Offset-minimised chi2, one warp per curve, FP64 accumulation:
 // dm = sum w (o - m) / W ; chi2 = sum w (o - m - dm)^2 (two passes, no cancellation).
 template <typename T>

@@ -92,3 +92,30 @@ def test_interleaved_sampling_equals_planar(ctx, dtype, nm, stride):
         a = mlc.sample_tracks(ctx, maps, N, N, *dev, mag=mag)
         b = mlc.sample_tracks_interleaved(ctx, il, nm, *dev, mag=mag)
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("prec,nm,stride", [("f64", 1, 1), ("f64", 3, 4), ("f32", 16, 16), ("f32", 5, 8)])
+def test_fused_track_chi2_offset_matches_two_step(ctx, prec, nm, stride):
+    """Fused sample -> magnitude -> offset chi2 (no light curve in memory) equals sampling
+    the light curves and then running the offset chi2: FP64 1e-10, FP32 1e-5 relative."""
+    import microsn_gb300 as mlc
+    N, n, T = 240, 700, 50
+    dt = torch.float64 if prec == "f64" else torch.float32
+    maps = [torch.as_tensor(synth.lognormal_map(N, seed=40 + q), dtype=dt, device="cuda:0") for q in range(nm)]
+    imap = mlc.interleave_maps(ctx, maps, N, N, stride) if stride > 1 else maps[0]
+    rng = np.random.default_rng(9)
+    x0 = rng.uniform(30, 60, n); y0 = rng.uniform(30, 60, n); phi = rng.uniform(0, 2 * np.pi, n)
+    v = rng.uniform(0.5, 3.0, n)
+    t = np.arange(T, dtype=np.float64)
+    D = lambda a: torch.as_tensor(a, dtype=dt, device="cuda:0")
+    off = torch.arange(0, (n + 1) * T, T, dtype=torch.int64, device="cuda:0")
+    lc = mlc.sample_tracks(ctx, maps, N, N, D(x0), D(y0), D(phi), D(v), off, D(np.tile(t, n)), mag=True)
+    obs = lc[0, :T].double().cpu().numpy() + rng.normal(0, 0.05, T)
+    w = np.full(T, 1 / 0.05 ** 2)
+    c2, dm = mlc.track_chi2_offset(ctx, imap, nm, D(x0), D(y0), D(phi), D(v), D(t),
+                                   torch.as_tensor(obs, device="cuda:0"), torch.as_tensor(w, device="cuda:0"))
+    for q in range(nm):
+        ref, dref = oracle.chi2_offset(lc[q].double().cpu().numpy().reshape(n, T), obs, w)
+        tol = 1e-10 if prec == "f64" else 1e-5
+        np.testing.assert_allclose(c2[q].cpu().numpy(), ref, rtol=tol)
+        np.testing.assert_allclose(dm[q].cpu().numpy(), dref, rtol=tol, atol=tol)
