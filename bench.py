@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--small", action="store_true", help="reduced sizes (debug only; not a bench number)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 form")
-    ap.add_argument("--no-pair", action="store_true", help="skip the pair-chi2/s workload")
+    ap.add_argument("--no-pair", action="store_true", help="skip the pair-chi2/s, flux-ratio, C1 and C4 workloads")
+    ap.add_argument("--no-c5", action="store_true", help="skip the supernova multi-image workload")
     ap.add_argument("--n", type=int, default=None, help="map side (profiling cases only; not a bench number)")
     ap.add_argument("--tracks", type=int, default=None, help="track count (profiling cases only)")
     return ap.parse_args()
@@ -395,6 +396,109 @@ def c4_workload(args, ctx, dev, rank):
             "kernel_ms": k_ms, "track_epochs_per_s_kernel": n * C4_T / (k_ms / 1000.0),
             "iterations": iters, "targets_recovered_fraction": recovered,
             "median_best_over_true_chi2": float(np.median(final.min(axis=1) / true_c2))}
+
+
+# configs[4], supernova multi-band multi-image: four 8192^2 FP32 maps (one per lensed
+# image, seeds 6..9, distinct kappa* and gamma), an expanding photosphere R(t) from 1 to
+# 100 px over 40 epochs in 3 bands (limb-darkened discs, one limb-darkening coefficient
+# per band) = 120 convolutions per map, 2x10^5 tracks per image sampled at the epochs,
+# then the offset magnitude-difference chi2 of every track pair of the 6 image pairs
+# (T = 120) with a 1000-bin log histogram and the 10^4 smallest per pair.
+C5_N, C5_EPOCHS, C5_TRACKS = 8192, 40, 200_000
+C5_LENS = [(0.40, 0.35), (0.45, 0.40), (0.50, 0.45), (0.55, 0.50)]
+C5_U = (0.6, 0.45, 0.3)
+
+
+def c5_workload(args, ctx, dev, rank):
+    import itertools
+
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    from microsn_gb300 import synth
+    N = C5_N
+    ntr = min(C5_TRACKS, args.tracks) if args.tracks else C5_TRACKS
+    maps = []
+    for i, (ks, g) in enumerate(C5_LENS):
+        mp, _ = synth.rayshoot_gpu(ctx, N, 20.0, ks, g, seed=6 + i + 10 * rank, rays_per_pixel=4.0,
+                                   dtype=torch.float32)
+        maps.append(mlc.Map(ctx, mp, "f32"))
+        del mp
+    R = np.linspace(1.0, 100.0, C5_EPOCHS)
+    profs = [mlc.profile("limb_darkened", r / np.sqrt(2.0), 1.0, ref_compat=False, u=u) for r in R for u in C5_U]
+    nb = len(C5_U)
+    conv = torch.empty((len(profs), N, N), dtype=torch.float32, device=dev)  # 32 GB
+    rng = np.random.default_rng(60 + rank)
+    t = torch.as_tensor(np.arange(C5_EPOCHS) * 2.0, dtype=torch.float32, device=dev)  # every 2 days
+    span = 2.0 * (C5_EPOCHS - 1)
+    tracks = []
+    for i in range(len(maps)):
+        v = rng.uniform(0.2, 1.0, ntr); phi = rng.uniform(0, 2 * np.pi, ntr)
+        L = v * span; mg = 110.0
+        x0 = mg + np.maximum(-L * np.cos(phi), 0) + rng.uniform(0, 1, ntr) * (N - 2 * mg - np.abs(L * np.cos(phi)))
+        y0 = mg + np.maximum(-L * np.sin(phi), 0) + rng.uniform(0, 1, ntr) * (N - 2 * mg - np.abs(L * np.sin(phi)))
+        tracks.append([torch.as_tensor(a, dtype=torch.float32, device=dev) for a in (x0, y0, phi, v)])
+    T = C5_EPOCHS * nb
+    w = 1.0 / rng.uniform(0.02, 0.1, T) ** 2
+    lcs = [torch.empty((ntr, T), dtype=torch.float32, device=dev) for _ in maps]
+    pairs = list(itertools.combinations(range(len(maps)), 2))
+
+    def curves():
+        for i, m in enumerate(maps):
+            m.refresh()
+            mlc.convolve_many(ctx, m, profs, out=conv, graph=True)
+            mlc.sample_expanding(ctx, conv, nb, *tracks[i], t, out=lcs[i])
+
+    def pair_stage():
+        res = []
+        for a, b in pairs:
+            res.append(mlc.pair_chi2_magdiff(ctx, lcs[a], lcs[b], w, None, True, method="tensor", nbins=PAIR_BINS,
+                                             lo=-1.0, hi=9.0, k=PAIR_K))
+        return res
+
+    curves(); pair_stage()  # warm-up: captures the convolution graphs, sizes the workspaces
+    torch.cuda.synchronize()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    steps = max(1, min(args.steps, 2))
+    t_curves = t_pairs = 0.0
+    for _ in range(steps):
+        e[0].record()
+        curves()
+        e[1].record()
+        res = pair_stage()
+        e[2].record()
+        torch.cuda.synchronize()
+        t_curves += e[0].elapsed_time(e[1]); t_pairs += e[1].elapsed_time(e[2])
+    t_curves /= steps; t_pairs /= steps
+    # the same convolutions without the graph, for the launch-overhead comparison
+    e[0].record()
+    for m in maps:
+        mlc.convolve_many(ctx, m, profs, out=conv, graph=False)
+    e[1].record(); torch.cuda.synchronize()
+    conv_eager = e[0].elapsed_time(e[1])
+    e[0].record()
+    for m in maps:
+        mlc.convolve_many(ctx, m, profs, out=conv, graph=True)
+    e[1].record(); torch.cuda.synchronize()
+    conv_graph = e[0].elapsed_time(e[1])
+    npairs = len(pairs) * float(ntr) * ntr
+    total = t_curves + t_pairs
+    out = {"workload": f"configs[4]: {len(maps)} x {N}^2 FP32 maps, {len(profs)} limb-darkened expanding-photosphere "
+                       f"profiles per map ({C5_EPOCHS} epochs x {nb} bands), {ntr} tracks per image, offset "
+                       f"magnitude-difference chi2 of all track pairs of {len(pairs)} image pairs (T = {T})",
+           "ms_per_step": total, "curves_ms": t_curves, "pairs_ms": t_pairs,
+           "light_curves_per_s": len(maps) * ntr * nb / (total / 1000.0),
+           "pair_chi2_per_s": npairs / (t_pairs / 1000.0),
+           "convolutions_per_s": len(maps) * len(profs) / (t_curves / 1000.0),
+           "conv_ms_graph": conv_graph, "conv_ms_eager": conv_eager,
+           "refined_pairs": int(sum(r["stats"]["refined"] for r in res)),
+           "histogram_total": float(sum(float(r["hist"].sum()) for r in res))}
+    for m in maps:
+        m.close()
+    del conv
+    torch.cuda.empty_cache()
+    return out
 
 
 # Multi-filter flux-ratio likelihood at the reference chi2 driver's size
@@ -791,11 +895,13 @@ def main():
     pair = None
     if not args.no_pair:
         pair = pair_workload(args, ctx, m, profs, n, dev, world, rank, stream)
-    flux = c1 = c4 = None
+    flux = c1 = c4 = c5 = None
     if not args.no_pair:
         flux = flux_ratio_workload(args, ctx, dev, rank)
         c1 = c1_workload(args, ctx, dev, rank)
         c4 = c4_workload(args, ctx, dev, rank)
+    if not args.no_c5:
+        c5 = c5_workload(args, ctx, dev, rank)
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -812,7 +918,8 @@ def main():
                        "ms_per_step": e2e_ms},
                "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
                "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair,
-               "flux_ratio": flux, "c1_small_fp64": c1, "c4_fit": c4}
+               "flux_ratio": flux, "c1_small_fp64": c1, "c4_fit": c4,
+               "c5_supernova": c5}
         print(json.dumps(res), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -193,6 +193,7 @@ typedef struct {
 
 #define MLC_IO_HOST 1 /* pixels, the track arrays and out are host memory */
 #define MLC_ASYNC 2   /* return once queued (see below) */
+#define MLC_GRAPH 4   /* mlc_convolve_many: capture / replay the kernel sequence as a CUDA graph */
 
 /* The light-curve step of one lensed image in one call -- expanding_source
  * (gpu_functions.cu:82-225) with straight tracks in place of fixed locations:
@@ -214,6 +215,25 @@ typedef struct {
 int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof,
                                const mlc_profile* profiles_host, const mlc_tracks* tracks, int mode,
                                int mag, void* out, int flags);
+
+/* The map convolved with nprof profiles (mode MLC_CONV_*) into out + k*out_stride
+ * elements (device, the map's precision): the profiles of an expanding source or of
+ * several bands in one call, rasters staged and uploaded once.  With MLC_GRAPH the
+ * kernel sequence is captured into a CUDA graph on its first call and replayed by later
+ * calls with the same map, profile raster sizes and output (profile values may change).
+ * No reference counterpart beyond the per-profile loop of expanding_source. */
+int mlc_convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* profiles_host, int mode, void* out,
+                      long long out_stride, int flags);
+
+/* Expanding source (one profile per epoch, the supernova case; no reference counterpart):
+ * the nep*nbands maps of the epochs and bands stored contiguously (map e*nbands + b starts
+ * at maps + (e*nbands + b)*Nx*Ny, e.g. from mlc_convolve_many), ntracks straight tracks
+ * (x0, y0, phi, v in the map's precision) sampled bilinearly at the shared epochs t[nep]:
+ * out[i*nep*nbands + e*nbands + b], magnitudes when mag != 0 (rows are the curves the
+ * pair stage takes, T = nep*nbands). */
+int mlc_sample_expanding(mlc_ctx* ctx, const void* maps, int Nx, int Ny, int precision, int nep, int nbands,
+                         int ntracks, const void* x0, const void* y0, const void* phi, const void* v, const void* t,
+                         int mag, void* out);
 
 /* Makes the context's stream wait (on the device, without blocking the host) for all
  * copies queued by MLC_IO_HOST calls, so that an event recorded on the stream afterwards

@@ -29,7 +29,7 @@ class MlcTracks(C.Structure):
                 ("phi", C.c_void_p), ("v", C.c_void_p), ("off", C.c_void_p), ("t", C.c_void_p)]
 
 
-MLC_IO_HOST, MLC_ASYNC = 1, 2
+MLC_IO_HOST, MLC_ASYNC, MLC_GRAPH = 1, 2, 4
 
 
 class MlcPairStats(C.Structure):
@@ -78,6 +78,8 @@ SIGNATURES = {
     "mlc_convolve_sample_tracks": (i32, [vp, vp, vp, i32, C.POINTER(MlcProfile), C.POINTER(MlcTracks), i32, i32, vp,
                                          i32]),
     "mlc_ctx_join": (i32, [vp]),
+    "mlc_convolve_many": (i32, [vp, vp, i32, C.POINTER(MlcProfile), i32, vp, C.c_longlong, i32]),
+    "mlc_sample_expanding": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, i32, vp]),
     "mlc_track_chi2_offset": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp]),
     "mlc_fit_raster": (i32, [f64, f64, i32, vp, vp, vp, vp]),
     "mlc_radius_stack": (i32, [vp, vp, i32, vp, f64, i32, vp]),

@@ -369,6 +369,35 @@ def mpd_divide(ctx: Context, binsA, countsA, binsB, countsB, binsR) -> np.ndarra
     return out
 
 
+def convolve_many(ctx: Context, m: Map, profiles, mode: str = "fused", out: torch.Tensor | None = None,
+                  graph: bool = False) -> torch.Tensor:
+    """The map convolved with every profile: (nprof, Ny, Nx) in the map's precision.
+    graph=True captures the kernel sequence as a CUDA graph on the first call and replays
+    it on later calls with the same map, raster sizes and output."""
+    n = len(profiles)
+    if out is None:
+        out = torch.empty((n, m.Ny, m.Nx), dtype=m.dtype, device=f"cuda:{ctx.device}")
+    P = (_lib.MlcProfile * n)(*profiles)
+    ctx.check(ctx.L.mlc_convolve_many(ctx.h, m.h, n, P, _MODES[mode], _ptr(out), m.Ny * m.Nx,
+                                      _lib.MLC_GRAPH if graph else 0))
+    return out
+
+
+def sample_expanding(ctx: Context, maps: torch.Tensor, nbands: int, x0, y0, phi, v, t, mag=True,
+                     out: torch.Tensor | None = None) -> torch.Tensor:
+    """Expanding source: maps (nep*nbands, Ny, Nx), epoch e's band b is map e*nbands + b;
+    returns (ntracks, nep*nbands) light curves sampled at the shared epochs t (nep,)."""
+    nm, Ny, Nx = maps.shape
+    nep = t.numel()
+    assert nm == nep * nbands
+    n = x0.numel()
+    if out is None:
+        out = torch.empty((n, nep * nbands), dtype=maps.dtype, device=maps.device)
+    ctx.check(ctx.L.mlc_sample_expanding(ctx.h, _ptr(maps), Nx, Ny, _PREC[maps.dtype], nep, nbands, n, _ptr(x0),
+                                         _ptr(y0), _ptr(phi), _ptr(v), _ptr(t), int(mag), _ptr(out)))
+    return out
+
+
 TRACK_KEYS = ("x0", "y0", "phi", "v", "off", "t")
 
 

@@ -462,6 +462,28 @@ int mlc_mpd_divide(mlc_ctx* ctx, int NA, const double* binsA_host, const double*
   });
 }
 
+int mlc_convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* profiles_host, int mode, void* out,
+                      long long out_stride, int flags) {
+  if (!ctx || !map || !profiles_host || !out) return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (nprof < 1 || out_stride < (long long)map->Nx * map->Ny) return fail(ctx, MLC_ERR_ARG, "bad count or stride");
+  if (mode != MLC_CONV_FUSED && mode != MLC_CONV_PLAIN) return fail(ctx, MLC_ERR_ARG, "unknown convolution mode");
+  if (flags & ~MLC_GRAPH) return fail(ctx, MLC_ERR_ARG, "unknown flags");
+  if (map->device != ctx->device) return fail(ctx, MLC_ERR_ARG, "map lives on another device");
+  return guarded(ctx, [&] { convolve_many(ctx, map, nprof, profiles_host, mode, out, out_stride, flags); });
+}
+
+int mlc_sample_expanding(mlc_ctx* ctx, const void* maps, int Nx, int Ny, int precision, int nep, int nbands,
+                         int ntracks, const void* x0, const void* y0, const void* phi, const void* v, const void* t,
+                         int mag, void* out) {
+  if (!ctx || !maps || !out || (ntracks > 0 && (!x0 || !y0 || !phi || !v || !t)))
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (Nx < 2 || Ny < 2 || nep < 1 || nbands < 1 || ntracks < 0 || (precision != MLC_F64 && precision != MLC_F32))
+    return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  return guarded(ctx, [&] {
+    sample_expanding(ctx, maps, Nx, Ny, precision, nep, nbands, ntracks, x0, y0, phi, v, t, mag, out);
+  });
+}
+
 int mlc_ctx_join(mlc_ctx* ctx) {
   return guarded(ctx, [&] { ctx_join(ctx); });
 }

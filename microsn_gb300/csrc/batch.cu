@@ -47,6 +47,12 @@ struct BatchIO {
   size_t prof_cap[2] = {};
   cudaEvent_t prof_sent[2] = {};
   int parity = 0;
+  // the kernel sequence of the last mlc_convolve_many call with MLC_GRAPH, replayed while
+  // every pointer and size it baked in stays the same
+  cudaStream_t cap = nullptr;
+  std::vector<uint64_t> graph_key;
+  cudaGraphExec_t graph = nullptr;
+  unsigned long long graph_launches = 0;  // kernels in the graph
 };
 
 static void ev_create(cudaEvent_t* e) { MLC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming)); }
@@ -57,6 +63,7 @@ static BatchIO* batch_get(mlc_ctx* ctx) {
   ctx->batch = b;  // released by batch_release even if a creation below fails
   MLC_CUDA(cudaStreamCreateWithFlags(&b->h2d, cudaStreamNonBlocking));
   MLC_CUDA(cudaStreamCreateWithFlags(&b->d2h, cudaStreamNonBlocking));
+  MLC_CUDA(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
   ev_create(&b->pix_free);
   ev_create(&b->pix_in);
   ev_create(&b->h2d_last);
@@ -104,6 +111,8 @@ void batch_release(mlc_ctx* ctx) {
   }
   for (cudaEvent_t e : {b->pix_free, b->pix_in, b->h2d_last, b->d2h_last})
     if (e) cudaEventDestroy(e);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->cap) cudaStreamDestroy(b->cap);
   if (b->h2d) cudaStreamDestroy(b->h2d);
   if (b->d2h) cudaStreamDestroy(b->d2h);
   delete b;
@@ -131,23 +140,14 @@ static int pow2_at_least(int n) {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-template <typename T>
-static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const mlc_profile* profs,
-                const mlc_tracks& tr, int mode, int mag, void* out, int flags) {
-  const bool host = (flags & MLC_IO_HOST) != 0;
-  const size_t es = sizeof(T);
-  const int Nx = map->Nx, Ny = map->Ny;
-  const long npix = (long)Nx * Ny;
-  FftPlan2D* p = plan_get(ctx, Nx, Ny, map->prec);
-  BatchIO* b = batch_get(ctx);
-  const int par = b->parity;
-  b->parity ^= 1;
-  const int ntr = tr.ntracks;
-  const int64_t E = tr.nepochs;
-
-  // ---- profiles: all rasters into page-locked staging, one upload on the compute stream
-  std::vector<int> pN(nprof);
-  std::vector<size_t> poff(nprof + 1, 0);
+// Rasters of nprof profiles into page-locked staging (host threads, largest first: they
+// take milliseconds each while the previous call's kernels still run) and one upload into
+// the profile workspace on the context's stream.  pN / poff receive the raster sides and
+// element offsets.
+static const double* stage_profiles(mlc_ctx* ctx, BatchIO* b, int par, int nprof, const mlc_profile* profs, int Nx,
+                                    int Ny, std::vector<int>& pN, std::vector<size_t>& poff) {
+  pN.assign(nprof, 0);
+  poff.assign(nprof + 1, 0);
   for (int k = 0; k < nprof; k++) {
     pN[k] = profile_dims(profs[k]);
     MLC_REQUIRE(pN[k] > 0, MLC_ERR_ARG, "invalid profile parameters");
@@ -163,29 +163,47 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     MLC_CUDA(cudaMallocHost((void**)&b->prof_host[par], pbytes));
     b->prof_cap[par] = pbytes;
   }
-  {
-    // rasters on host threads, largest first (they take milliseconds each, and the
-    // previous call's kernels are still running meanwhile)
-    std::vector<int> order(nprof);
-    std::iota(order.begin(), order.end(), 0);
-    std::sort(order.begin(), order.end(), [&](int a, int c) { return pN[a] > pN[c]; });
-    std::atomic<int> next{0}, bad{0};
-    auto work = [&] {
-      for (int i = next++; i < nprof; i = next++) {
-        const int k = order[i];
-        if (profile_raster(profs[k], b->prof_host[par] + poff[k], (long)(poff[k + 1] - poff[k])) != pN[k]) bad = 1;
-      }
-    };
-    const int nth = std::max(1, std::min<int>(nprof, (int)std::thread::hardware_concurrency()) - 1);
-    std::vector<std::thread> pool;
-    for (int i = 0; i < nth; i++) pool.emplace_back(work);
-    work();
-    for (auto& th : pool) th.join();
-    MLC_REQUIRE(!bad, MLC_ERR_ARG, "profile raster failed");
-  }
+  std::vector<int> order(nprof);
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(), [&](int a, int c) { return pN[a] > pN[c]; });
+  std::atomic<int> next{0}, bad{0};
+  double* host = b->prof_host[par];
+  auto work = [&] {
+    for (int i = next++; i < nprof; i = next++) {
+      const int k = order[i];
+      if (profile_raster(profs[k], host + poff[k], (long)(poff[k + 1] - poff[k])) != pN[k]) bad = 1;
+    }
+  };
+  const int nth = std::max(0, std::min<int>(nprof, (int)std::thread::hardware_concurrency()) - 1);
+  std::vector<std::thread> pool;
+  for (int i = 0; i < nth; i++) pool.emplace_back(work);
+  work();
+  for (auto& th : pool) th.join();
+  MLC_REQUIRE(!bad, MLC_ERR_ARG, "profile raster failed");
   double* dprof = (double*)ws_get(ctx, WS_PROFILE, pbytes);
-  MLC_CUDA(cudaMemcpyAsync(dprof, b->prof_host[par], pbytes, cudaMemcpyHostToDevice, ctx->stream));
+  MLC_CUDA(cudaMemcpyAsync(dprof, host, pbytes, cudaMemcpyHostToDevice, ctx->stream));
   MLC_CUDA(cudaEventRecord(b->prof_sent[par], ctx->stream));
+  return dprof;
+}
+
+template <typename T>
+static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const mlc_profile* profs,
+                const mlc_tracks& tr, int mode, int mag, void* out, int flags) {
+  const bool host = (flags & MLC_IO_HOST) != 0;
+  const size_t es = sizeof(T);
+  const int Nx = map->Nx, Ny = map->Ny;
+  const long npix = (long)Nx * Ny;
+  FftPlan2D* p = plan_get(ctx, Nx, Ny, map->prec);
+  BatchIO* b = batch_get(ctx);
+  const int par = b->parity;
+  b->parity ^= 1;
+  const int ntr = tr.ntracks;
+  const int64_t E = tr.nepochs;
+
+  // ---- profiles: all rasters into page-locked staging, one upload on the compute stream
+  std::vector<int> pN;
+  std::vector<size_t> poff;
+  const double* dprof = stage_profiles(ctx, b, par, nprof, profs, Nx, Ny, pN, poff);
 
   // ---- map pixels and forward spectrum
   if (pixels) {
@@ -313,6 +331,78 @@ void convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int 
                             const mlc_tracks& tr, int mode, int mag, void* out, int flags) {
   if (map->prec == MLC_F64) run<double>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags);
   else run<float>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags);
+}
+
+// Convolutions of one map with many profiles into out + k * stride (the map's precision):
+// rasters staged and uploaded once, then the fused (or plain) convolution per profile.
+// With MLC_GRAPH the per-profile kernel sequence is captured once into a CUDA graph (on an
+// internal stream, after an eager run has sized every workspace) and later calls with the
+// same map, profile sizes, output and workspace replay it with one launch.
+void convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* profs, int mode, void* out,
+                   long long stride, int flags) {
+  BatchIO* b = batch_get(ctx);
+  const int par = b->parity;
+  b->parity ^= 1;
+  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
+  map_prepare(ctx, map);
+  std::vector<int> pN;
+  std::vector<size_t> poff;
+  const double* dprof = stage_profiles(ctx, b, par, nprof, profs, map->Nx, map->Ny, pN, poff);
+  const size_t es = map->prec == MLC_F64 ? 8 : 4;
+  auto enqueue = [&] {
+    for (int k = 0; k < nprof; k++) {
+      void* o = (char*)out + (size_t)k * stride * es;
+      if (mode == MLC_CONV_FUSED) conv_fused(ctx, *p, map->spec, dprof + poff[k], pN[k], o);
+      else conv_plain(ctx, *p, map->spec, dprof + poff[k], pN[k], o);
+    }
+  };
+  auto key = [&] {
+    std::vector<uint64_t> kv = {(uint64_t)map, (uint64_t)map->spec, (uint64_t)nprof, (uint64_t)mode, (uint64_t)out,
+                                (uint64_t)stride, (uint64_t)dprof};
+    for (int s = 0; s < WS_NSLOTS; s++) kv.push_back((uint64_t)ctx->ws_ptr[s]);
+    for (int k = 0; k < nprof; k++) kv.push_back((uint64_t)pN[k]);
+    return kv;
+  };
+  if (!(flags & MLC_GRAPH) || ctx->timing) {
+    enqueue();
+    return;
+  }
+  if (b->graph && b->graph_key == key()) {
+    ctx->launches += b->graph_launches;
+    MLC_CUDA(cudaGraphLaunch(b->graph, ctx->stream));
+    return;
+  }
+  const unsigned long long l0 = ctx->launches;
+  enqueue();  // this call's result; also grows every workspace slot the sequence uses
+  const unsigned long long nl = ctx->launches - l0;
+  if (b->graph) {
+    MLC_CUDA(cudaGraphExecDestroy(b->graph));
+    b->graph = nullptr;
+  }
+  const unsigned long long launches = ctx->launches;
+  cudaStream_t saved = ctx->stream;
+  ctx->stream = b->cap;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    try {
+      enqueue();
+    } catch (...) {
+      cudaStreamEndCapture(b->cap, &g);
+      if (g) cudaGraphDestroy(g);
+      ctx->stream = saved;
+      throw;
+    }
+    e = cudaStreamEndCapture(b->cap, &g);
+  }
+  ctx->stream = saved;
+  ctx->launches = launches;
+  MLC_CUDA(e);
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  MLC_CUDA(e);
+  b->graph_key = key();
+  b->graph_launches = nl;
 }
 
 void ctx_join(mlc_ctx* ctx) {

@@ -58,6 +58,11 @@ void batch_synchronize(mlc_ctx* ctx);
 void convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const mlc_profile* profs,
                             const mlc_tracks& tr, int mode, int mag, void* out, int flags);
 void ctx_join(mlc_ctx* ctx);
+void convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* profs, int mode, void* out,
+                   long long stride, int flags);
+void sample_expanding(mlc_ctx* ctx, const void* maps, int Nx, int Ny, int prec, int nep, int nbands, int ntracks,
+                      const void* x0, const void* y0, const void* phi, const void* v, const void* t, int mag,
+                      void* out);
 void set_chunk_bytes(mlc_ctx* ctx, size_t bytes);
 }  // namespace mlc
 

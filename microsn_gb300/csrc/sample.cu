@@ -282,6 +282,63 @@ void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int
   MLC_CHECK_LAUNCH();
 }
 
+// Expanding source: epoch e has its own nbands maps (map s = e*nbands + b, npix pixels
+// apart), all tracks share the epochs t[nep]; one thread per (track, epoch) reads its
+// bands' four bilinear corners and writes out[i*nep*nbands + e*nbands + b] -- curves as
+// rows of nep*nbands values, the layout the pair stage reads.
+template <typename T>
+__global__ void __launch_bounds__(256) k_sample_expanding(const T* __restrict__ maps, long npix, int Nx, int Ny,
+                                                          int nbands, int ntracks, int nep, const T* __restrict__ x0,
+                                                          const T* __restrict__ y0, const T* __restrict__ phi,
+                                                          const T* __restrict__ v, const T* __restrict__ t, int mag,
+                                                          T* __restrict__ out) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long)ntracks * nep) return;
+  const long tr = idx / nep;
+  const int e = (int)(idx - tr * nep);
+  const T X0 = x0[tr], Y0 = y0[tr];
+  T sn, cs;
+  if (sizeof(T) == 8) {
+    double s_, c_;
+    sincos((double)phi[tr], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  } else {
+    float s_, c_;
+    sincosf((float)phi[tr], &s_, &c_);
+    sn = (T)s_;
+    cs = (T)c_;
+  }
+  const long bx = (long)floor(X0), by = (long)floor(Y0);
+  const T vt = v[tr] * t[e];
+  const Bilin<T> B = bilin_weights<T>(bx, X0 - (T)bx + vt * cs, by, Y0 - (T)by + vt * sn, Nx, Ny);
+  T* o = out + idx * nbands;
+  for (int b = 0; b < nbands; b++) {
+    const T mu = B.inside ? bilin_read<T>(maps + (long)(e * nbands + b) * npix, B, Nx) : (T)0;
+    o[b] = mag ? (T)-2.5 * mlc_log10(mu) : mu;
+  }
+}
+
+void sample_expanding(mlc_ctx* ctx, const void* maps, int Nx, int Ny, int prec, int nep, int nbands, int ntracks,
+                      const void* x0, const void* y0, const void* phi, const void* v, const void* t, int mag,
+                      void* out) {
+  const long n = (long)ntracks * nep;
+  if (n <= 0) return;
+  const int grid = (int)((n + 255) / 256);
+  const long npix = (long)Nx * Ny;
+  MLC_KSCOPE(ctx, "sample_expanding");
+  if (prec == MLC_F64)
+    k_sample_expanding<double><<<grid, 256, 0, ctx->stream>>>((const double*)maps, npix, Nx, Ny, nbands, ntracks, nep,
+                                                              (const double*)x0, (const double*)y0,
+                                                              (const double*)phi, (const double*)v,
+                                                              (const double*)t, mag, (double*)out);
+  else
+    k_sample_expanding<float><<<grid, 256, 0, ctx->stream>>>((const float*)maps, npix, Nx, Ny, nbands, ntracks, nep,
+                                                             (const float*)x0, (const float*)y0, (const float*)phi,
+                                                             (const float*)v, (const float*)t, mag, (float*)out);
+  MLC_CHECK_LAUNCH();
+}
+
 // Fused sample -> magnitude -> offset-minimised chi2 of every track against one observed
 // curve on shared epochs t[T] (no light curve is written): one warp per track, lanes over
 // the epochs.  Pass 1 samples the NM interleaved maps and accumulates sum w (o - m) per
