@@ -200,30 +200,70 @@ __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ 
     const T vt = V * t[e];
     const T fx = fx0 + vt * cs, fy = fy0 + vt * sn;
     const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
-    T acc[NM];
-    if (B.inside) {
-      T a[NM], b[NM], c[NM], d[NM];
-      load_pix<T, NM>(imap + ((long)B.iu * Nx + B.jl) * NM, a);
-      load_pix<T, NM>(imap + ((long)B.iu * Nx + B.jr) * NM, b);
-      load_pix<T, NM>(imap + ((long)B.il * Nx + B.jl) * NM, c);
-      load_pix<T, NM>(imap + ((long)B.il * Nx + B.jr) * NM, d);
+    // 16 bytes of maps at a time (4 FP32 / 2 FP64): the four corners of one chunk in
+    // registers, not all NM maps of all four corners (which needed 100 registers and left
+    // 2 CTAs per SM, too few warps to hide the gather latency)
+    constexpr int CH = (NM * (int)sizeof(T) >= 16) ? 16 / (int)sizeof(T) : NM;
+    const T* pa = imap + ((long)B.iu * Nx + B.jl) * NM;
+    const T* pb = imap + ((long)B.iu * Nx + B.jr) * NM;
+    const T* pc = imap + ((long)B.il * Nx + B.jl) * NM;
+    const T* pd = imap + ((long)B.il * Nx + B.jr) * NM;
+#pragma unroll 1
+    for (int c0 = 0; c0 < NM; c0 += CH) {
+      T acc[CH];
+      if (B.inside) {
+        T a[CH], b[CH], c[CH], d[CH];
+        load_pix<T, CH>(pa + c0, a);
+        load_pix<T, CH>(pb + c0, b);
+        load_pix<T, CH>(pc + c0, c);
+        load_pix<T, CH>(pd + c0, d);
 #pragma unroll
-      for (int q = 0; q < NM; q++) {
-        T z = B.w0 * a[q];
-        z += B.w1 * b[q];
-        z += B.w2 * c[q];
-        z += B.w3 * d[q];
-        acc[q] = z;
+        for (int q = 0; q < CH; q++) {
+          T z = B.w0 * a[q];
+          z += B.w1 * b[q];
+          z += B.w2 * c[q];
+          z += B.w3 * d[q];
+          acc[q] = z;
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < CH; q++) acc[q] = (T)0;
       }
-    } else {
 #pragma unroll
-      for (int q = 0; q < NM; q++) acc[q] = (T)0;
+      for (int q = 0; q < CH; q++)
+        if (c0 + q < nm_out) out[(long)(c0 + q) * E + (e - ebase)] = mag ? (T)-2.5 * mlc_log10(acc[q]) : acc[q];
     }
-#pragma unroll
-    for (int q = 0; q < NM; q++)
-      if (q < nm_out) out[(long)q * E + (e - ebase)] = mag ? (T)-2.5 * mlc_log10(acc[q]) : acc[q];
   }
 }
+
+// FP32 with a contiguous output (width == S, off == 0, W in {4, 8, 16}), npix % 4 == 0 and
+// 16-byte aligned maps: tiles of 512 pixels moved as float4 on both sides.
+template <int W>
+__global__ void __launch_bounds__(256) k_interleave_f4(MapList<float> maps, int nm, long npix,
+                                                      float* __restrict__ out) {
+  __shared__ __align__(16) float tile[W][516];  // 516: rows stay 16-byte aligned
+  const long ntiles = (npix + 511) / 512;
+  for (long tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const long p0 = tb * 512;
+    const int np = (int)min(512L, npix - p0);  // a multiple of 4
+    for (int f = threadIdx.x; f < W * 128; f += 256) {
+      const int q = f >> 7, c = (f & 127) * 4;
+      float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (q < nm && c < np) val = __ldg(reinterpret_cast<const float4*>(maps.m[q] + p0 + c));
+      *reinterpret_cast<float4*>(&tile[q][c]) = val;
+    }
+    __syncthreads();
+    float4* o = reinterpret_cast<float4*>(out + p0 * W);
+    const int nf = np * (W / 4);
+    for (int f = threadIdx.x; f < nf; f += 256) {
+      const int px = f / (W / 4), q0 = (f % (W / 4)) * 4;
+      o[f] = make_float4(tile[q0][px], tile[q0 + 1][px], tile[q0 + 2][px], tile[q0 + 3][px]);
+    }
+    __syncthreads();
+  }
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 static void interleave_impl(mlc_ctx* ctx, const void* const* maps_host, int nmaps, int width, int S, int off,
                             long npix, int prec, void* out) {
@@ -231,6 +271,20 @@ static void interleave_impl(mlc_ctx* ctx, const void* const* maps_host, int nmap
   int wshift = -1;
   for (int b = 0; b < 5; b++)
     if (width == (1 << b)) wshift = b;
+  bool fast = prec == MLC_F32 && width == S && off == 0 && (width == 4 || width == 8 || width == 16) &&
+              npix % 4 == 0 && aligned16(out);
+  for (int q = 0; q < nmaps && fast; q++) fast = aligned16(maps_host[q]);
+  if (fast) {
+    MapList<float> ml{};
+    for (int q = 0; q < nmaps; q++) ml.m[q] = (const float*)maps_host[q];
+    const int g = (int)std::min<long>((npix + 511) / 512, (long)ctx->sm_count * 8);
+    MLC_KSCOPE(ctx, "interleave");
+    if (width == 16) k_interleave_f4<16><<<g, 256, 0, ctx->stream>>>(ml, nmaps, npix, (float*)out);
+    else if (width == 8) k_interleave_f4<8><<<g, 256, 0, ctx->stream>>>(ml, nmaps, npix, (float*)out);
+    else k_interleave_f4<4><<<g, 256, 0, ctx->stream>>>(ml, nmaps, npix, (float*)out);
+    MLC_CHECK_LAUNCH();
+    return;
+  }
   if (prec == MLC_F64) {
     MapList<double> ml{};
     for (int q = 0; q < nmaps; q++) ml.m[q] = (const double*)maps_host[q];
