@@ -20,6 +20,7 @@
 //     P3  inverse real FFT of each row (c2r)
 //   plain convolution (MLC_CONV_PLAIN): full-size wrapped kernel, full forward,
 //     pointwise multiply, full inverse -- one launch per stage, like the reference.
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 #include <unordered_map>
@@ -57,8 +58,11 @@ RadixList factor_radices(int L, int tw_stride) {
   }
   for (int i = 0; i < n8; i++) rl.r[rl.n++] = 8;
   int Ns = 1;
+  rl.tlen = 0;
   for (int p = 0; p < rl.n; p++) {
     rl.Ns[p] = Ns;
+    rl.toff[p] = rl.tlen;
+    rl.tlen += p == 0 ? 0 : Ns * (rl.r[p] - 1);
     // exact j / Ns = umulhi(j, magic) for j * Ns < 2^32 (here j < L <= 65535)
     rl.magic[p] = Ns > 1 ? (uint32_t)((0x100000000ull + Ns - 1) / Ns) : 0u;
     rl.twstep[p] = (L / (Ns * rl.r[p])) * tw_stride;
@@ -267,6 +271,8 @@ __global__ void __launch_bounds__(256) k_colpass(C2<T>* __restrict__ buf, long p
   extern __shared__ unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + L * CW;
+  C2<T>* tab = b + L * CW;   // stage twiddles (rl.tlen)
+  C2<T>* pw = tab + rl.tlen; // post twiddles W_Ny^(set j), j < L
   const int set = blockIdx.y;
   const long col0 = (long)blockIdx.x * CW;
   const long base = (long)set * set_mul;
@@ -274,16 +280,63 @@ __global__ void __launch_bounds__(256) k_colpass(C2<T>* __restrict__ buf, long p
     int j = idx / CW, c = idx % CW;
     a[idx] = buf[(base + j * j_mul) * pitch + col0 + c];
   }
+  fill_stage_twiddles<T>(rl, twy, tab);
+  if (post_tw)
+    for (int j = threadIdx.x; j < L; j += blockDim.x) pw[j] = ldc(twy + (long)set * j);  // set*j < Ny
   __syncthreads();
-  C2<T>* r = fft_smem<T, INV, CW>(a, b, rl, twy);
+  C2<T>* r = fft_smem_st<T, INV, CW>(a, b, rl, tab);
   for (int idx = threadIdx.x; idx < L * CW; idx += blockDim.x) {
     int j = idx / CW, c = idx % CW;
     C2<T> v = r[idx];
-    if (post_tw) {
-      C2<T> w = ldc(twy + (long)set * j);  // set*j < Ny for both sub-pass kinds
-      v = INV ? cmulc(v, w) : cmul(v, w);
-    }
+    if (post_tw) v = INV ? cmulc(v, pw[j]) : cmul(v, pw[j]);
     buf[(base + j * j_mul) * pitch + col0 + c] = v;
+  }
+}
+
+// The same sub-pass for L = L1 * L2 with both factors done in registers (four-step):
+// thread (n2, c) loads x[L2 n1 + n2] (n1 < L1) straight from global memory, DFT_L1 over n1,
+// twiddle W_L^(n2 k1), one transpose through shared memory, then thread (k1, c) does
+// DFT_L2 over n2 and writes X[k1 + L1 k2] straight back.  One shared-memory round trip and
+// fixed per-thread indices instead of a Stockham stage loop per radix.
+template <typename T, int CW, int L1, int L2, bool INV>
+__global__ void __launch_bounds__(256) k_colpass2(C2<T>* __restrict__ buf, long pitch, long set_mul, long j_mul,
+                                                  const C2<T>* __restrict__ twy, int tw_stride, int post_tw) {
+  constexpr int L = L1 * L2;
+  __shared__ C2<T> y[L2][L1][CW];
+  __shared__ C2<T> wl[L];  // W_L^m
+  __shared__ C2<T> pw[L];  // post twiddles W_Ny^(set j)
+  const int set = blockIdx.y;
+  const long col0 = (long)blockIdx.x * CW;
+  const long base = (long)set * set_mul;
+  const int c = threadIdx.x % CW, g = threadIdx.x / CW;
+  for (int m = threadIdx.x; m < L; m += blockDim.x) {
+    wl[m] = ldc(twy + (long)m * tw_stride);
+    if (post_tw) pw[m] = ldc(twy + (long)set * m);  // set*m < Ny
+  }
+  C2<T> v[L1];
+  if (g < L2) {
+#pragma unroll
+    for (int n1 = 0; n1 < L1; n1++) v[n1] = buf[(base + (long)(L2 * n1 + g) * j_mul) * pitch + col0 + c];
+  }
+  __syncthreads();
+  if (g < L2) {
+    Dft<T, L1, INV>::run(v);
+#pragma unroll
+    for (int k1 = 0; k1 < L1; k1++) y[g][k1][c] = (k1 == 0) ? v[0] : (INV ? cmulc(v[k1], wl[g * k1]) : cmul(v[k1], wl[g * k1]));
+  }
+  __syncthreads();
+  if (g < L1) {
+    C2<T> u[L2];
+#pragma unroll
+    for (int n2 = 0; n2 < L2; n2++) u[n2] = y[n2][g][c];
+    Dft<T, L2, INV>::run(u);
+#pragma unroll
+    for (int k2 = 0; k2 < L2; k2++) {
+      const int j = g + L1 * k2;
+      C2<T> val = u[k2];
+      if (post_tw) val = INV ? cmulc(val, pw[j]) : cmul(val, pw[j]);
+      buf[(base + (long)j * j_mul) * pitch + col0 + c] = val;
+    }
   }
 }
 
@@ -296,10 +349,14 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
   extern __shared__ unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + N2 * CW;
-  C2<T>* w1 = b + N2 * CW;  // W_N1^(n1 k1) for n1 < N1, this CTA's k1
+  C2<T>* w1 = b + N2 * CW;   // W_N1^(n1 k1) for n1 < N1, this CTA's k1
+  C2<T>* w2 = w1 + N1;       // W_Ny^(n2 k1) for n2 < N2
+  C2<T>* tab = w2 + N2;      // stage twiddles of the N2 transforms (rl2.tlen)
   const int k1 = blockIdx.y;
   const long col0 = (long)blockIdx.x * CW;
   for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * k1) % N1) * N2);
+  for (int n2 = threadIdx.x; n2 < N2; n2 += blockDim.x) w2[n2] = ldc(twy + (long)n2 * k1);
+  fill_stage_twiddles<T>(rl2, twy, tab);
   __syncthreads();
   // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 k1)
   const int lo = Ny - h;  // first non-zero high row
@@ -316,10 +373,10 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
       const long j = (long)n1 * N2 + n2 - (Ny - 2L * h);
       acc = cadd(acc, cmul(Kx[j * pitch + col0 + c], w1[n1]));
     }
-    a[idx] = cmul(acc, ldc(twy + n2 * k1));
+    a[idx] = cmul(acc, w2[n2]);
   }
   __syncthreads();
-  C2<T>* K = fft_smem<T, false, CW>(a, b, rl2, twy);
+  C2<T>* K = fft_smem_st<T, false, CW>(a, b, rl2, tab);
   C2<T>* other = (K == a) ? b : a;
   for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
     const int k2 = idx / CW, c = idx % CW;
@@ -327,11 +384,97 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
     K[idx] = cscale(cmul(f, K[idx]), scale);
   }
   __syncthreads();
-  C2<T>* U = fft_smem<T, true, CW>(K, other, rl2, twy);
+  C2<T>* U = fft_smem_st<T, true, CW>(K, other, rl2, tab);
   for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
     const int n2 = idx / CW, c = idx % CW;
-    C2<T> v = cmulc(U[idx], ldc(twy + (long)n2 * k1));
+    C2<T> v = cmulc(U[idx], w2[n2]);
     out[((long)k1 * N2 + n2) * pitch + col0 + c] = v;
+  }
+}
+
+// P1 for N2 = L1 * L2 with both factors in registers.  Forward N2 transform of the profile
+// column (built in shared memory as in k_conv_fused) as a four-step: thread (n2, c) DFT_L1
+// over x[L2 n1 + n2], twiddle, transpose, thread (k1, c) DFT_L2 -> it now holds frequencies
+// k = k1 + L1 k2, multiplies them by the map spectrum (read straight from global memory)
+// and 1/(Nx Ny), and starts the inverse as the transposed four-step on the same registers:
+// DFT^-1_L2 over k2, twiddle W_N2^-(k1 n2), transpose, thread (n2, c) DFT^-1_L1 over k1 ->
+// rows n2 + L2 n1, times W_Ny^-(n kk), stored.
+template <typename T, int CW, int L1, int L2>
+__global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
+                                                     long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
+                                                     int N1, const C2<T>* __restrict__ twy, T scale) {
+  constexpr int N2 = L1 * L2;
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);  // [N2][CW] profile column sub-pass
+  C2<T>* y = a + N2 * CW;                         // [max(L1,L2)][max(L1,L2)][CW] transposes
+  C2<T>* w1 = y + N2 * CW;                        // W_N1^(n1 kk), n1 < N1
+  C2<T>* w2 = w1 + N1;                            // W_Ny^(n kk), n < N2
+  C2<T>* wl = w2 + N2;                            // W_N2^m, m < N2
+  const int kk = blockIdx.y;
+  const long col0 = (long)blockIdx.x * CW;
+  const int c = threadIdx.x % CW, g = threadIdx.x / CW;
+  for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * kk) % N1) * N2);
+  for (int n = threadIdx.x; n < N2; n += blockDim.x) {
+    w2[n] = ldc(twy + (long)n * kk);
+    wl[n] = ldc(twy + (long)n * N1);
+  }
+  __syncthreads();
+  // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 kk)
+  const int lo = Ny - h;
+  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
+    const int n2 = idx / CW, cc = idx & (CW - 1);
+    C2<T> acc{(T)0, (T)0};
+    for (int n1 = 0; n1 * N2 + n2 < h; n1++) {
+      const long j = (long)n1 * N2 + n2;
+      acc = cadd(acc, cmul(Kx[j * pitch + col0 + cc], w1[n1]));
+    }
+    int n1s = (lo - n2 + N2 - 1) / N2;
+    if (n1s < 0) n1s = 0;
+    for (int n1 = n1s; n1 < N1; n1++) {
+      const long j = (long)n1 * N2 + n2 - (Ny - 2L * h);
+      acc = cadd(acc, cmul(Kx[j * pitch + col0 + cc], w1[n1]));
+    }
+    a[idx] = cmul(acc, w2[n2]);
+  }
+  __syncthreads();
+  // forward stage 1: thread (n2 = g, c)
+  if (g < L2) {
+    C2<T> v[L1];
+#pragma unroll
+    for (int n1 = 0; n1 < L1; n1++) v[n1] = a[(L2 * n1 + g) * CW + c];
+    Dft<T, L1, false>::run(v);
+#pragma unroll
+    for (int k1 = 0; k1 < L1; k1++) y[(g * L1 + k1) * CW + c] = k1 == 0 ? v[0] : cmul(v[k1], wl[g * k1]);
+  }
+  __syncthreads();
+  // forward stage 2, product, inverse stage A: thread (k1 = g, c)
+  if (g < L1) {
+    C2<T> u[L2];
+#pragma unroll
+    for (int n2 = 0; n2 < L2; n2++) u[n2] = y[(n2 * L1 + g) * CW + c];
+    Dft<T, L2, false>::run(u);
+#pragma unroll
+    for (int k2 = 0; k2 < L2; k2++) {
+      const C2<T> f = Fmap[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c];
+      u[k2] = cscale(cmul(f, u[k2]), scale);
+    }
+    Dft<T, L2, true>::run(u);  // over k2 -> n2
+    // the thread rewrites exactly the entries of y it read above: no other thread's data
+#pragma unroll
+    for (int n2 = 0; n2 < L2; n2++) y[(n2 * L1 + g) * CW + c] = n2 == 0 ? u[0] : cmulc(u[n2], wl[g * n2]);
+  }
+  __syncthreads();
+  // inverse stage B: thread (n2 = g, c) over k1 -> rows n2 + L2 n1
+  if (g < L2) {
+    C2<T> v[L1];
+#pragma unroll
+    for (int k1 = 0; k1 < L1; k1++) v[k1] = y[(g * L1 + k1) * CW + c];
+    Dft<T, L1, true>::run(v);
+#pragma unroll
+    for (int n1 = 0; n1 < L1; n1++) {
+      const int n = g + L2 * n1;
+      out[((long)kk * N2 + n) * pitch + col0 + c] = cmulc(v[n1], w2[n]);
+    }
   }
 }
 
@@ -403,7 +546,29 @@ static void launch_colpass(mlc_ctx* ctx, const FftPlan2D& p, void* buf, char kin
     L = p.N2; nsets = p.N1; set_mul = p.N2; j_mul = 1; tw_stride = p.N1; rl = p.rlN2;
   }
   if (L == 1 && !post_tw) return;
-  size_t smem = 2 * (size_t)L * CW * sizeof(C2<T>);
+  // two-level register kernels for the lengths that split into two supported factors
+  using K2 = void (*)(C2<T>*, long, long, long, const C2<T>*, int, int);
+  K2 k2 = nullptr;
+  int nthr = 0;
+  switch (L) {
+    case 100: k2 = k_colpass2<T, CW, 10, 10, INV>; nthr = 10 * CW; break;
+    case 128: k2 = k_colpass2<T, CW, 8, 16, INV>; nthr = 16 * CW; break;
+    case 64: k2 = k_colpass2<T, CW, 8, 8, INV>; nthr = 8 * CW; break;
+    case 80: k2 = k_colpass2<T, CW, 8, 10, INV>; nthr = 10 * CW; break;
+    case 50: k2 = k_colpass2<T, CW, 5, 10, INV>; nthr = 10 * CW; break;
+    case 40: k2 = k_colpass2<T, CW, 5, 8, INV>; nthr = 8 * CW; break;
+    default: break;
+  }
+  if (k2) {
+    dim3 grid(nstrips, nsets);
+    {
+      MLC_KSCOPE(ctx, kind == 'A' ? "fft_col_A" : "fft_col_B");
+      k2<<<grid, nthr, 0, ctx->stream>>>((C2<T>*)buf, p.Wp, set_mul, j_mul, (const C2<T>*)p.twy, tw_stride, post_tw);
+    }
+    MLC_CHECK_LAUNCH();
+    return;
+  }
+  size_t smem = (2 * (size_t)L * CW + rl.tlen + L) * sizeof(C2<T>);
   auto kern = k_colpass<T, CW, INV>;
   set_max_smem((const void*)kern, smem);
   dim3 grid(nstrips, nsets);
@@ -441,11 +606,40 @@ static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
   void* tmp = ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
   launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
   const int nstrips = ceil_div(p.Wc, CW);
-  size_t smem = (2 * (size_t)p.N2 * CW + p.N1) * sizeof(C2<T>);
+  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
+  {
+    // two-level register kernel where N2 splits into two supported factors
+    using K2 = void (*)(const C2<T>*, C2<T>*, long, const C2<T>*, int, int, int, const C2<T>*, T);
+    K2 k2 = nullptr;
+    int nthr = 0;
+    switch (p.N2) {
+      case 100: k2 = k_conv_fused2<T, CW, 10, 10>; nthr = 10 * CW; break;
+      case 128: k2 = k_conv_fused2<T, CW, 8, 16>; nthr = 16 * CW; break;
+      case 64: k2 = k_conv_fused2<T, CW, 8, 8>; nthr = 8 * CW; break;
+      case 80: k2 = k_conv_fused2<T, CW, 8, 10>; nthr = 10 * CW; break;
+      case 50: k2 = k_conv_fused2<T, CW, 5, 10>; nthr = 10 * CW; break;
+      case 40: k2 = k_conv_fused2<T, CW, 5, 8>; nthr = 8 * CW; break;
+      default: break;
+    }
+    if (k2) {
+      const size_t smem2 = (2 * (size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
+      set_max_smem((const void*)k2, smem2);
+      {
+        MLC_KSCOPE(ctx, "conv_fused_spectrum");
+        k2<<<dim3(nstrips, p.N1), nthr, smem2, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp,
+                                                              (const C2<T>*)kx, h, p.Ny, p.N1,
+                                                              (const C2<T>*)p.twy, scale);
+      }
+      MLC_CHECK_LAUNCH();
+      launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
+      launch_rows_c2r<T>(ctx, p, tmp, out);
+      return;
+    }
+  }
+  size_t smem = (2 * (size_t)p.N2 * CW + p.N1 + p.N2 + p.rlN2.tlen) * sizeof(C2<T>);
   auto kern = k_conv_fused<T, CW>;
   set_max_smem((const void*)kern, smem);
   dim3 grid(nstrips, p.N1);
-  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
   {
     MLC_KSCOPE(ctx, "conv_fused_spectrum");
     kern<<<grid, 256, smem, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp, (const C2<T>*)kx, h, p.Ny,

@@ -17,6 +17,8 @@ struct RadixList {
   int Ns[20];
   uint32_t magic[20];
   int twstep[20];
+  int toff[20];  // offset of stage p's twiddles in a staged table: Ns[p] * (r[p] - 1) entries
+  int tlen;      // entries of the whole staged table
 };
 
 // Radix plan for length L (2^a 3^b 5^c) whose twiddles come from a table of
@@ -111,6 +113,51 @@ struct Dft<T, 8, INV> {
   }
 };
 
+// Radix 2 over two half-length DFTs: X[k] = E[k] + W^k O[k], X[k + R/2] = E[k] - W^k O[k],
+// W = exp(-/+ 2 pi i / R); wr[k], wi[k] = cos, sin(2 pi k / R).
+template <typename T, int H, bool INV>
+__device__ __forceinline__ void dft_split2(C2<T>* v, const T* wr, const T* wi) {
+  C2<T> e[H], o[H];
+#pragma unroll
+  for (int i = 0; i < H; i++) {
+    e[i] = v[2 * i];
+    o[i] = v[2 * i + 1];
+  }
+  Dft<T, H, INV>::run(e);
+  Dft<T, H, INV>::run(o);
+#pragma unroll
+  for (int k = 0; k < H; k++) {
+    // W^k o with W^k = (wr, -wi) forward, (wr, wi) inverse
+    const T sr = INV ? -wi[k] : wi[k];
+    const C2<T> t = C2<T>{wr[k] * o[k].x + sr * o[k].y, wr[k] * o[k].y - sr * o[k].x};
+    v[k] = cadd(e[k], t);
+    v[k + H] = csub(e[k], t);
+  }
+}
+
+template <typename T, bool INV>
+struct Dft<T, 10, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    // cos, sin(2 pi k / 10), k = 0..4
+    const T wr[5] = {(T)1, (T)0.80901699437494742410229341718282, (T)0.30901699437494742410229341718282,
+                     (T)-0.30901699437494742410229341718282, (T)-0.80901699437494742410229341718282};
+    const T wi[5] = {(T)0, (T)0.58778525229247312916870595463907, (T)0.95105651629515357211643933337938,
+                     (T)0.95105651629515357211643933337938, (T)0.58778525229247312916870595463907};
+    dft_split2<T, 5, INV>(v, wr, wi);
+  }
+};
+
+template <typename T, bool INV>
+struct Dft<T, 16, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    const T c1 = (T)0.92387953251128675612818318939679, s1 = (T)0.38268343236508977172845998403040;
+    const T r = (T)0.70710678118654752440084436210485;
+    const T wr[8] = {(T)1, c1, r, s1, (T)0, -s1, -r, -c1};
+    const T wi[8] = {(T)0, s1, r, c1, (T)1, c1, r, s1};
+    dft_split2<T, 8, INV>(v, wr, wi);
+  }
+};
+
 // ---------------------------------------------------------------- Stockham stage
 // src/dst are [L][CW] complex arrays in shared memory; tw is the length-(L*tw_stride)
 // table exp(-2 pi i m / (L*tw_stride)) in global memory.
@@ -148,6 +195,78 @@ __device__ __forceinline__ void stockham_stage(const C2<T>* __restrict__ src, C2
 #pragma unroll
     for (int i = 0; i < R; i++) dst[(d + i * Ns) * CW + c] = v[i];
   }
+}
+
+// The same stage with the twiddles W^(i k) (i = 1 .. R-1) of every k read from a table
+// staged in shared memory, tws[k * (R-1) + i - 1] (fill_stage_twiddles): no table reads
+// from global memory and no chain of multiplications for the powers.
+template <typename T, int R, bool INV, int CW>
+__device__ __forceinline__ void stockham_stage_st(const C2<T>* __restrict__ src, C2<T>* __restrict__ dst, int L,
+                                                  int Ns, uint32_t magic, const C2<T>* __restrict__ tws) {
+  const int Lr = L / R;
+  const int nb = Lr * CW;
+  for (int bt = threadIdx.x; bt < nb; bt += blockDim.x) {
+    const int c = bt & (CW - 1);
+    const int j = bt / CW;
+    int q, k;
+    if (Ns == 1) {
+      q = j;
+      k = 0;
+    } else {
+      q = (int)__umulhi((uint32_t)j, magic);
+      k = j - q * Ns;
+    }
+    C2<T> v[R];
+#pragma unroll
+    for (int i = 0; i < R; i++) v[i] = src[(j + i * Lr) * CW + c];
+    if (Ns > 1) {
+      const C2<T>* w = tws + k * (R - 1);
+#pragma unroll
+      for (int i = 1; i < R; i++) v[i] = INV ? cmulc(v[i], w[i - 1]) : cmul(v[i], w[i - 1]);
+    }
+    Dft<T, R, INV>::run(v);
+    const int d = q * Ns * R + k;
+#pragma unroll
+    for (int i = 0; i < R; i++) dst[(d + i * Ns) * CW + c] = v[i];
+  }
+}
+
+// Stage twiddle table of a radix plan in shared memory: stage p, index k < Ns, power
+// i = 1 .. R-1 -> W^(i k twstep) from the global table tw (i k twstep < L tw_stride).
+template <typename T>
+__device__ __forceinline__ void fill_stage_twiddles(const RadixList& rl, const C2<T>* __restrict__ tw,
+                                                    C2<T>* __restrict__ tab) {
+  for (int p = 1; p < rl.n; ++p) {
+    const int R = rl.r[p], Ns = rl.Ns[p], ts = rl.twstep[p], o = rl.toff[p];
+    for (int e = threadIdx.x; e < Ns * (R - 1); e += blockDim.x) {
+      const int k = e / (R - 1), i = e - k * (R - 1) + 1;
+      tab[o + e] = ldc(tw + (long)i * k * ts);
+    }
+  }
+}
+
+// fft_smem with the stage twiddles staged in shared memory (tab filled by
+// fill_stage_twiddles and synchronised before the call).
+template <typename T, bool INV, int CW>
+__device__ C2<T>* fft_smem_st(C2<T>* a, C2<T>* b, const RadixList& rl, const C2<T>* __restrict__ tab) {
+  const int L = rl.L;
+  for (int p = 0; p < rl.n; ++p) {
+    const int Ns = rl.Ns[p];
+    const uint32_t mg = rl.magic[p];
+    const C2<T>* tws = tab + rl.toff[p];
+    switch (rl.r[p]) {
+      case 2: stockham_stage_st<T, 2, INV, CW>(a, b, L, Ns, mg, tws); break;
+      case 3: stockham_stage_st<T, 3, INV, CW>(a, b, L, Ns, mg, tws); break;
+      case 4: stockham_stage_st<T, 4, INV, CW>(a, b, L, Ns, mg, tws); break;
+      case 5: stockham_stage_st<T, 5, INV, CW>(a, b, L, Ns, mg, tws); break;
+      default: stockham_stage_st<T, 8, INV, CW>(a, b, L, Ns, mg, tws); break;
+    }
+    __syncthreads();
+    C2<T>* t = a;
+    a = b;
+    b = t;
+  }
+  return a;
 }
 
 // Batched length-L transform of the CW columns held in a ([L][CW]); b is scratch of the
