@@ -260,6 +260,82 @@ __global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, 
   for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = z[n];
 }
 
+// Inverse real FFT of one spectrum row per CTA with M = L1 L2 L3 (J = L2 L3) in three
+// register levels.  b[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W_Nx^-k is the
+// complex sequence whose inverse FFT z gives the real row (out[2n], out[2n+1]) = z[n].
+//   level 1, item j < J:        b[J a + j] (a < L1) from global memory, DFT^-1_L1 over a,
+//                               twiddle W_M^-(j n1)                   -> s[n1 J + j]
+//   level 2, item (n1, m < L3): DFT^-1_L2 over b of s[n1 J + L3 b + m], twiddle W_J^-(m n2)
+//                                                                      -> s[n1 J + n2 L3 + m]
+//   level 3, item (n1, n2):     DFT^-1_L3 over m                      -> z[n1 + L1 (n2 + L2 n3)]
+// and one coalesced copy of z to the output row.  Levels 2 and 3 read all their inputs
+// before a barrier and then overwrite the same buffer (M complex values, 40 KB at
+// M = 5000 in FP32).  Items of levels 2 and 3 fit in one pass of the CTA (L1 L3 and
+// L1 L2 <= blockDim).
+template <typename T, int L1, int L2, int L3>
+__global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in, long pitch, T* __restrict__ out,
+                                                   long ldo, const C2<T>* __restrict__ twx) {
+  constexpr int J = L2 * L3, M = L1 * J;
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
+  C2<T>* wJ = s + M;  // W_J^e = W_Nx^(2 L1 e), e < J
+  const int row = blockIdx.x, tid = threadIdx.x;
+  const C2<T>* a = in + (long)row * pitch;
+  for (int e = tid; e < J; e += blockDim.x) wJ[e] = ldc(twx + 2L * L1 * e);
+  for (int j = tid; j < J; j += blockDim.x) {
+    C2<T> v[L1];
+#pragma unroll
+    for (int q = 0; q < L1; q++) {
+      const int k = J * q + j;
+      const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
+      const C2<T> e = cadd(xk, xm);
+      const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
+      v[q] = C2<T>{e.x - o.y, e.y + o.x};
+    }
+    Dft<T, L1, true>::run(v);
+    s[j] = v[0];
+#pragma unroll
+    for (int n1 = 1; n1 < L1; n1++) s[n1 * J + j] = cmulc(v[n1], ldc(twx + 2L * j * n1));  // W_M^-(j n1)
+  }
+  __syncthreads();
+  {
+    const bool act = tid < L1 * L3;
+    const int n1 = tid / L3, m = tid - n1 * L3;
+    C2<T> u[L2];
+    if (act) {
+#pragma unroll
+      for (int b = 0; b < L2; b++) u[b] = s[n1 * J + L3 * b + m];
+      Dft<T, L2, true>::run(u);
+#pragma unroll
+      for (int n2 = 1; n2 < L2; n2++) u[n2] = cmulc(u[n2], wJ[m * n2]);
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int n2 = 0; n2 < L2; n2++) s[n1 * J + n2 * L3 + m] = u[n2];
+    }
+  }
+  __syncthreads();
+  {
+    const bool act = tid < L1 * L2;
+    const int n1 = tid / L2, n2 = tid - n1 * L2;
+    C2<T> w[L3];
+    if (act) {
+#pragma unroll
+      for (int m = 0; m < L3; m++) w[m] = s[n1 * J + n2 * L3 + m];
+      Dft<T, L3, true>::run(w);
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int n3 = 0; n3 < L3; n3++) s[n1 + L1 * (n2 + L2 * n3)] = w[n3];
+    }
+  }
+  __syncthreads();
+  C2<T>* dst = reinterpret_cast<C2<T>*>(out + (long)row * ldo);
+  for (int n = tid; n < M; n += blockDim.x) dst[n] = s[n];
+}
+
 // ---------------------------------------------------------------- column kernels
 
 // In-place sub-pass over the row set {set*set_mul + j*j_mul : j < L} of one strip of CW
@@ -521,6 +597,28 @@ static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, 
 
 template <typename T>
 static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, void* out) {
+  {
+    using K3 = void (*)(const C2<T>*, long, T*, long, const C2<T>*);
+    K3 k3 = nullptr;
+    int J = 0;
+    switch (p.M) {
+      case 5000: k3 = k_rows_c2r3<T, 8, 25, 25>; J = 625; break;
+      case 4096: k3 = k_rows_c2r3<T, 16, 16, 16>; J = 256; break;
+      case 2000: k3 = k_rows_c2r3<T, 8, 10, 25>; J = 250; break;
+      case 1000: k3 = k_rows_c2r3<T, 10, 10, 10>; J = 100; break;
+      default: break;
+    }
+    if (k3) {
+      const size_t smem3 = ((size_t)p.M + J) * sizeof(C2<T>);
+      set_max_smem((const void*)k3, smem3);
+      {
+        MLC_KSCOPE(ctx, "fft_rows_c2r");
+        k3<<<p.Ny, 256, smem3, ctx->stream>>>((const C2<T>*)in, p.Wp, (T*)out, p.Nx, (const C2<T>*)p.twx);
+      }
+      MLC_CHECK_LAUNCH();
+      return;
+    }
+  }
   size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
   auto kern = k_rows_c2r<T>;
   set_max_smem((const void*)kern, smem);

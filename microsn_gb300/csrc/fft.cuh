@@ -158,6 +158,69 @@ struct Dft<T, 16, INV> {
   }
 };
 
+template <typename T, bool INV>
+struct Dft<T, 20, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    // cos, sin(2 pi k / 20), k = 0..9
+    const T a = (T)0.95105651629515357211643933337938214, b = (T)0.30901699437494742410229341718281906;
+    const T c = (T)0.80901699437494742410229341718281906, d = (T)0.58778525229247312916870595463907277;
+    const T wr[10] = {(T)1, a, c, d, b, (T)0, -b, -d, -c, -a};
+    const T wi[10] = {(T)0, b, d, c, a, (T)1, a, c, d, b};
+    dft_split2<T, 10, INV>(v, wr, wi);
+  }
+};
+
+// 25 points as 5 x 5 (four-step in registers): DFT5 over n1 of x[5 n1 + n2], twiddle
+// W25^(n2 k1), DFT5 over n2 -> X[k1 + 5 k2].
+template <typename T, bool INV>
+struct Dft<T, 25, INV> {
+  static __device__ __forceinline__ void run(C2<T>* v) {
+    // cos, sin(2 pi m / 25), m = 0..16
+    const T cr[17] = {(T)1,
+                      (T)0.96858316112863111949016837546473581,  (T)0.87630668004386358730811590392206258,
+                      (T)0.72896862742141152314673031905525911,  (T)0.53582679497899661827130876786763998,
+                      (T)0.30901699437494742410229341718281906,  (T)0.062790519529313376076178224565631133,
+                      (T)-0.18738131458572463054255073444729147, (T)-0.42577929156507264886250244574425170,
+                      (T)-0.63742398974868971017671281167601620, (T)-0.80901699437494742410229341718281906,
+                      (T)-0.92977648588825140366094255622199073, (T)-0.99211470131447783104979304278577852,
+                      (T)-0.99211470131447783104979304278577852, (T)-0.92977648588825140366094255622199073,
+                      (T)-0.80901699437494742410229341718281906, (T)-0.63742398974868971017671281167601620};
+    const T ci[17] = {(T)0,
+                      (T)0.24868988716485478824228374600644797, (T)0.48175367410171527498719150287212965,
+                      (T)0.68454710592868867373228335762120927, (T)0.84432792550201507854855806396668151,
+                      (T)0.95105651629515357211643933337938214, (T)0.99802672842827156195233680686345055,
+                      (T)0.98228725072868868108564174286526842, (T)0.90482705246601952771366864793269759,
+                      (T)0.77051324277578923080300963639617785, (T)0.58778525229247312916870595463907277,
+                      (T)0.36812455268467795915694714749296083, (T)0.12533323356430424537311875981650879,
+                      (T)-0.12533323356430424537311875981650879, (T)-0.36812455268467795915694714749296083,
+                      (T)-0.58778525229247312916870595463907277, (T)-0.77051324277578923080300963639617785};
+    C2<T> y[5][5];
+#pragma unroll
+    for (int n2 = 0; n2 < 5; n2++) {
+#pragma unroll
+      for (int n1 = 0; n1 < 5; n1++) y[n2][n1] = v[5 * n1 + n2];
+      Dft<T, 5, INV>::run(y[n2]);
+#pragma unroll
+      for (int k1 = 1; k1 < 5; k1++) {
+        if (n2 == 0) continue;
+        const int m = n2 * k1;
+        const T sr = INV ? -ci[m] : ci[m];  // W^m = (cr, -ci) forward, (cr, ci) inverse
+        const C2<T> q = y[n2][k1];
+        y[n2][k1] = C2<T>{cr[m] * q.x + sr * q.y, cr[m] * q.y - sr * q.x};
+      }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 5; k1++) {
+      C2<T> u[5];
+#pragma unroll
+      for (int n2 = 0; n2 < 5; n2++) u[n2] = y[n2][k1];
+      Dft<T, 5, INV>::run(u);
+#pragma unroll
+      for (int k2 = 0; k2 < 5; k2++) v[k1 + 5 * k2] = u[k2];
+    }
+  }
+};
+
 // ---------------------------------------------------------------- Stockham stage
 // src/dst are [L][CW] complex arrays in shared memory; tw is the length-(L*tw_stride)
 // table exp(-2 pi i m / (L*tw_stride)) in global memory.

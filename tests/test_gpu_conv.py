@@ -70,3 +70,28 @@ def test_expanding_source_matches_oracle(ctx, mode):
     assert np.array_equal(LC[:, 0], LCo[:, 0])  # point source: exact pixel reads
     assert rel_err(LC, LCo, 1e-3) < 1e-9
     assert np.max(np.abs(DLC - DLCo)) < 1e-9 * np.abs(LCo).max()
+
+
+# Every map side with a specialised transform kernel: rows of Nx/2 = 5000, 4096, 2000 and
+# 1000 complex points (three-level register kernels), columns of N1, N2 in {100, 64, 128,
+# 80, 50, 40} (two-level register kernels); the short sides keep the oracle cheap.
+@pytest.mark.parametrize("Ny,Nx", [(100, 10000), (128, 8192), (80, 4000), (50, 2000), (6400, 64), (4000, 80)])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_convolve_specialised_sizes(ctx, Ny, Nx, prec):
+    import microsn_gb300 as mlc
+    rng = np.random.default_rng(Ny + Nx)
+    mp = np.exp(rng.normal(0, 0.5, (Ny, Nx)))
+    prof = mlc.profile("exponential", 7.0, 1.0, ref_compat=False)
+    P = mlc.profile_raster(prof)
+    ref = oracle.conv_fft(mp, P)
+    if prec == "f64":
+        m = mlc.Map(ctx, mp, "f64")
+        for mode in ("fused", "plain"):
+            got = mlc.convolve(ctx, m, prof, mode).cpu().numpy()
+            assert rel_err(got, ref, 1e-3 * ref.mean()) < 1e-9, mode
+    else:
+        m = mlc.Map(ctx, mp.astype(np.float32), "f32")
+        got = mlc.convolve(ctx, m, prof, "fused").cpu().numpy().astype(np.float64)
+        rms = np.sqrt(np.mean(ref ** 2))
+        assert np.max(np.abs(got - ref)) < 2e-5 * rms * np.log2(max(Nx, Ny))
+    m.close()
