@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in,
   __syncthreads();
   {
     const bool act = tid < L1 * L2;
-    const int n1 = tid / L2, n2 = tid - n1 * L2;
+    const int n2 = tid / L1, n1 = tid - n2 * L1;  // n1 fastest: the writes below are contiguous
     C2<T> w[L3];
     if (act) {
 #pragma unroll
@@ -495,22 +495,43 @@ __global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ F
     wl[n] = ldc(twy + (long)n * N1);
   }
   __syncthreads();
-  // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 kk)
-  const int lo = Ny - h;
-  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
-    const int n2 = idx / CW, cc = idx & (CW - 1);
-    C2<T> acc{(T)0, (T)0};
-    for (int n1 = 0; n1 * N2 + n2 < h; n1++) {
-      const long j = (long)n1 * N2 + n2;
-      acc = cadd(acc, cmul(Kx[j * pitch + col0 + cc], w1[n1]));
+  // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 kk).
+  // Thread (g, c) owns the rows n2 = g + G i (G = blockDim / CW); the terms run outer and the
+  // elements inner, so the loads of all its elements for one term are in flight together.
+  {
+    constexpr int G = (L1 > L2 ? L1 : L2), NE = N2 / G;
+    static_assert(N2 % G == 0, "rows per thread");
+    C2<T> acc[NE];
+#pragma unroll
+    for (int i = 0; i < NE; i++) acc[i] = C2<T>{(T)0, (T)0};
+    const int tlo = (h + N2 - 1) / N2;  // low rows: kernel rows n1 N2 + n2 < h
+    for (int n1 = 0; n1 < tlo; n1++) {
+      const C2<T> w = w1[n1];
+#pragma unroll
+      for (int i = 0; i < NE; i++) {
+        const int n2 = g + G * i, j = n1 * N2 + n2;
+        if (j < h) acc[i] = cadd(acc[i], cmul(Kx[(long)j * pitch + col0 + c], w));
+      }
     }
-    int n1s = (lo - n2 + N2 - 1) / N2;
-    if (n1s < 0) n1s = 0;
-    for (int n1 = n1s; n1 < N1; n1++) {
-      const long j = (long)n1 * N2 + n2 - (Ny - 2L * h);
-      acc = cadd(acc, cmul(Kx[j * pitch + col0 + cc], w1[n1]));
+    // high rows: kernel rows >= Ny - h, in the last thi values of n1 (increasing)
+    const int thi = (h + N2 - 1) / N2 + 1;
+    for (int t = 0; t < thi; t++) {
+      const int n1 = N1 - thi + t;
+      if (n1 < 0) continue;
+      const C2<T> w = w1[n1];
+#pragma unroll
+      for (int i = 0; i < NE; i++) {
+        const int n2 = g + G * i;
+        const long jr = (long)n1 * N2 + n2;  // kernel row
+        if (jr >= (long)Ny - h && jr < Ny && (n1 > 0 || jr >= h))
+          acc[i] = cadd(acc[i], cmul(Kx[(jr - (Ny - 2L * h)) * pitch + col0 + c], w));
+      }
     }
-    a[idx] = cmul(acc, w2[n2]);
+#pragma unroll
+    for (int i = 0; i < NE; i++) {
+      const int n2 = g + G * i;
+      a[n2 * CW + c] = cmul(acc[i], w2[n2]);
+    }
   }
   __syncthreads();
   // forward stage 1: thread (n2 = g, c)
