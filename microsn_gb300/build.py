@@ -53,9 +53,29 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_driver()
     if verbose:
         print(LIB)
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "driver", "microlc.cpp")
+DRIVER = os.path.join(HERE, "bin", "microlc")
+
+
+def build_driver() -> str:
+    """The microlc command-line driver (driver/microlc.cpp) against the library."""
+    deps = [DRIVER_SRC, os.path.join(HERE, "driver", "json.hpp"), os.path.join(ROOT, "include", "microlc_compat.hpp"),
+            os.path.join(ROOT, "include", "microlc_gb300.h"), LIB]
+    if os.path.exists(DRIVER) and os.path.getmtime(DRIVER) >= max(os.path.getmtime(d) for d in deps):
+        return DRIVER
+    os.makedirs(os.path.dirname(DRIVER), exist_ok=True)
+    cmd = [NVCC, "-std=c++17", "-O2", "-x", "c++", "-I", os.path.join(ROOT, "include"), DRIVER_SRC,
+           "-L", HERE, "-lmicrolc_gb300", "-Xlinker", "-rpath=$ORIGIN/..", "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":
