@@ -6,8 +6,9 @@
 // is accumulated per diagonal d = a + b of slice exponents (five TMEM accumulators
 // d = 0..4, all nine slice pairs), so
 //     x = p.q = 2^32 X0 + 2^24 X1 + 2^16 X2 + 2^8 X3 + X4   exactly,
-// and chi2 = |P|^2 + |Q|^2 - 2^(ei+ej+1) x is formed in float-float arithmetic from the
-// per-curve norms (natural units) and the five exactly scaled accumulators.  Top-k
+// and chi2 = |P|^2 + |Q|^2 - 2^(ei+ej+1) x is formed from the per-curve norms (natural
+// units, float-float) and the exactly scaled accumulators: in FP32 (within 3.9e-6 relative)
+// where chi2 >= (|P|^2+|Q|^2)/16, in float-float arithmetic below that.  Top-k
 // candidates, pairs whose chi2 is below 1e-7 of |P|^2 + |Q|^2 (where the float-float
 // rounding could matter) and, with a matrix requested, every pair whose quantisation error
 // could exceed 1e-6 relative are recomputed in FP64 by k_pd_refine.
@@ -61,7 +62,7 @@ struct PdParams {
   const int* ea;
   const int* eb;
   int nbins;
-  float lo, inv_width;
+  float hscale, hoff;  // bin = floor(log2(chi2) * hscale + hoff)
   unsigned long long* hist;
   float thr;
   unsigned int cap;
@@ -79,7 +80,8 @@ struct PdParams {
 };
 
 size_t smem_bytes(int nkb, int nbins) {
-  return 1024 + (size_t)3 * nkb * A_BOX + (size_t)NSTAGE * 3 * nkb * B_BOX + 16 * 8 + 16 + sizeof(uint32_t) * nbins;
+  return 1024 + (size_t)3 * nkb * A_BOX + (size_t)NSTAGE * 3 * nkb * B_BOX + 16 * 8 + 16 +
+         sizeof(uint32_t) * ((nbins + 3) & ~3) + (size_t)EPI_WARPS * 16 * sizeof(float4);
 }
 
 // 2^k for k in [-126, 127]; 0 below (the terms it scales are then negligible)
@@ -106,7 +108,7 @@ __device__ __forceinline__ float chi2_assemble(float2 A, float2 B, float u0, flo
 
 __device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" ::"r"(EPI_WARPS * 32) : "memory"); }
 
-template <int NKB>  // 64-element K boxes per slice (Kp / 64)
+template <int NKB, bool OUT>  // 64-element K boxes per slice (Kp / 64); chi2 matrix written
 __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_constant__ CUtensorMap tmA,
                                                              const __grid_constant__ CUtensorMap tmB, PdParams P) {
   extern __shared__ unsigned char smem_raw[];
@@ -124,6 +126,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
   uint32_t* tmem_slot = (uint32_t*)(bars + 16);
   volatile int* abort_s = (volatile int*)(tmem_slot + 1);
   uint32_t* hist_s = tmem_slot + 4;
+  float4* colv = (float4*)(hist_s + ((P.nbins + 3) & ~3));  // [EPI_WARPS][16] column constants
+  const uint32_t hist_sa = tc::smem_u32(hist_s);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -226,20 +230,33 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
       const float2 aff = irow ? P.alpha_ff[i] : make_float2(0.f, 0.f);
       const int ei = irow ? P.ea[i] : PD_EMIN;
       const float pa = pow2f(ei);  // 2^ei
+      float4* cv = colv + (warp - 4) * 16;
+      // this warp's 16 columns h*16 + c of a tile: (beta_ff, 2^(ej+33)) fetched one tile ahead
+      // (the loads run while the previous tile is processed), staged in shared memory and read
+      // back as one broadcast load per element
+      float2 nb = make_float2(0.f, 0.f);
+      int ne = PD_EMIN;
+      auto fetch = [&](int jt) {
+        const int jl = jt * TN + h * 16 + lane;
+        const bool lok = lane < 16 && jt < j1 && jl < P.NB;
+        nb = lok ? __ldg(P.beta_ff + jl) : make_float2(0.f, 0.f);
+        ne = lok ? __ldg(P.eb + jl) : PD_EMIN;
+      };
+      fetch(j0);
       for (int jt = j0; jt < j1; jt++, ct++) {
         const uint32_t tb = ct & 1, tu = ct >> 1;
         if (*abort_s) break;
+        // (the previous tile's reads of cv ended at the __syncwarp closing it)
+        if (lane < 16) cv[lane] = make_float4(nb.x, nb.y, pow2f(ne + 33), 0.f);  // 2 x 2^(ei+ej) x 2^32 with pa
+        fetch(jt + 1);
+        __syncwarp();
         if (!tc::mbar_wait(t_full + tb, tu & 1)) {
           fail();
           break;
         }
         tc::fence_after_sync();
-        // this warp's 16 columns: lane c < 16 holds column h*16 + c (broadcast by shuffles)
-        const int jl = jt * TN + h * 16 + lane;
-        const bool lok = lane < 16 && jl < P.NB;
-        const float2 bl = lok ? __ldg(P.beta_ff + jl) : make_float2(0.f, 0.f);
-        const int el = lok ? __ldg(P.eb + jl) : PD_EMIN;
-        const float pl = pow2f(el + 33);  // 2^(ej+33): 2 x 2^(ei+ej) x 2^32 for the top diagonal
+        // full tiles (every row and column real) skip the per-element range tests
+        const bool fast = irow && (jt + 1) * TN <= P.NB;
         for (int ch = 0; ch < 2; ch++) {
           const int col0 = h * 16 + ch * 8;
           uint32_t r0[8], r1[8], r2[8], r3[8], r4[8];
@@ -252,35 +269,34 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
           tc::tmem_wait_ld();
 #pragma unroll
           for (int c = 0; c < 8; c++) {
-            const int src = ch * 8 + c;
-            const float2 bff = make_float2(__shfl_sync(0xffffffffu, bl.x, src), __shfl_sync(0xffffffffu, bl.y, src));
-            const float pb = __shfl_sync(0xffffffffu, pl, src);
             const int j = jt * TN + col0 + c;
-            if (!irow || j >= P.NB) continue;
+            if (!fast && (!irow || j >= P.NB)) continue;
+            const float4 b = cv[ch * 8 + c];
             // 2 x 2^(ei+ej) = sum_d 2^(ei+ej+33-8d) X_d; s0 = 2^(ei+ej+33) is an exact product
-            const float s0 = pa * pb;
-            const float ab = aff.x + bff.x;
+            const float s0 = pa * b.z;
+            const float ab = aff.x + b.x;
             const float X0 = __uint_as_float(r0[c]), X1 = __uint_as_float(r1[c]);
             const float X2 = __uint_as_float(r2[c]), X3 = __uint_as_float(r3[c]);
             // fast FP32 assembly (rounding below 2^-22 (|P|^2+|Q|^2); the left-out X4 term
-            // below 2^-30 of it): within 1e-6 of chi2 whenever chi2 >= (|P|^2+|Q|^2)/4,
-            // otherwise the float-float form
+            // below 2^-30 of it): within 3.9e-6 of chi2 whenever chi2 >= (|P|^2+|Q|^2)/16
             const float v = fmaf(X1, 0x1p-8f, X0);
             const float w = fmaf(X3, 0x1p-24f, X2 * 0x1p-16f);
-            float chi2 = fmaf(-v, s0, ab) + fmaf(-w, s0, aff.y + bff.y);
-            if (chi2 < 0.25f * ab) {
-              chi2 = chi2_assemble(aff, bff, X0 * s0, X1 * (s0 * 0x1p-8f), X2 * (s0 * 0x1p-16f),
+            float chi2 = fmaf(-v, s0, ab) + fmaf(-w, s0, aff.y + b.y);
+            // below (|P|^2+|Q|^2)/16 the float-float form.  Measured on 10^5 x 10^5 map curves:
+            // the threshold at 1/16 instead of 1/4 took 9% off the kernel (fewer warps enter the
+            // branch); one outer test around both rare cases, or a branch-free mask form of
+            // the 8 columns (128 registers), made it slower
+            if (chi2 < 0.0625f * ab)
+              chi2 = chi2_assemble(aff, make_float2(b.x, b.y), X0 * s0, X1 * (s0 * 0x1p-8f), X2 * (s0 * 0x1p-16f),
                                    X3 * (s0 * 0x1p-24f), __uint_as_float(r4[c]) * (s0 * 0x1p-32f));
-            }
-            // below 1e-7 (|P|^2+|Q|^2) the float-float rounding (about 2^-40 of it) could
-            // exceed 1e-5 relative; matrix mode adds the quantisation-error bound
+            // below 1e-7 (|P|^2+|Q|^2) the float-float rounding (about 2^-40 of it) could exceed
+            // 1e-5 relative; those, the top-k candidates and (matrix mode) pairs within the
+            // quantisation-error bound go to the exact FP64 list (which also histograms them)
             float bound = fmaxf(1e-7f * ab, P.thr);
-            if (P.out) {
-              const float q = pa + pb * 0x1p-33f;
+            if constexpr (OUT) {
+              const float q = pa + b.z * 0x1p-33f;
               bound = fmaxf(bound, P.refine_f * q * q);
             }
-            // top-k candidates and near-zero pairs go to the exact FP64 list (which also
-            // histograms them); every other pair is histogrammed here
             if (chi2 < bound) {
               const unsigned k = atomicAdd(P.nref, 1u);
               if (k < P.rcap) {
@@ -289,9 +305,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
               }
               continue;
             }
-            if (P.out) P.out[(long)i * P.NB + j] = chi2;
-            const int bin = (int)floorf((__log2f(chi2) * 0.30102999566398120f - P.lo) * P.inv_width);
-            if (bin >= 0 && bin < P.nbins) atomicAdd(hist_s + bin, 1u);
+            if constexpr (OUT) P.out[(long)i * P.NB + j] = chi2;
+            // chi2 >= 1e-7 (|P|^2+|Q|^2) > 0 here; a subnormal one (flat curves) falls out of range
+            float lg;
+            asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(lg) : "f"(chi2));
+            const int bin = __float2int_rd(fmaf(lg, P.hscale, P.hoff));
+            if ((unsigned)bin < (unsigned)P.nbins)
+              asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(hist_sa + 4u * (uint32_t)bin) : "memory");
           }
         }
         tc::fence_before_sync();
@@ -523,8 +543,8 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
   prm.ea = ops.ea;
   prm.eb = ops.eb;
   prm.nbins = nbins;
-  prm.lo = (float)lo;
-  prm.inv_width = (float)(nbins / (hi - lo));
+  prm.hscale = (float)(0.30102999566398120 * nbins / (hi - lo));  // log10(2) / bin width
+  prm.hoff = (float)(-lo * nbins / (hi - lo));
   prm.hist = hist;
   prm.cap = cap;
   prm.ncand = counters;
@@ -547,7 +567,8 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
   prm.err = (int*)(counters + 2);
   const size_t smem = smem_bytes(nkb, nbins);
   MLC_REQUIRE(nkb == 1 || nkb == 2, MLC_ERR_LIMIT, "tensor-core pair chi2 supports T <= 128 epochs");
-  auto kern = nkb == 1 ? k_pairdiff_tc<1> : k_pairdiff_tc<2>;
+  auto kern = nkb == 1 ? (out ? k_pairdiff_tc<1, true> : k_pairdiff_tc<1, false>)
+                       : (out ? k_pairdiff_tc<2, true> : k_pairdiff_tc<2, false>);
   set_max_smem((const void*)kern, smem);
   const int grid = std::min(grid_max, prm.nitems);
   // plain form: FP64 chi2 of row chunks, then histogram / candidates of each chunk
