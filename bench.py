@@ -861,7 +861,21 @@ def main():
     barrier()
     e2e_ms = e0.elapsed_time(e1) / esteps
     e2e_val = world * lc_per_step / (e2e_ms / 1000.0)
-    del h_out
+    # the host link itself: plain 1 GiB copies between pinned host memory and HBM on this machine
+    # (the light curves' download bounds the e2e step)
+    link = {}
+    dbuf = torch.empty(1 << 28, dtype=torch.float32, device=dev)
+    hbuf = h_out.view(-1)[: 1 << 28]
+    for name, dst, src in (("d2h_gbs", hbuf, dbuf), ("h2d_gbs", dbuf, hbuf)):
+        dst.copy_(src, non_blocking=True)
+        e0.record(stream)
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        link[name] = 3 * (1 << 30) / (e0.elapsed_time(e1) / 1000.0) / 1e9
+    link["download_floor_ms"] = bo / (link["d2h_gbs"] * 1e9) * 1000.0
+    del h_out, dbuf
 
     # ---- the plain one-launch-per-stage FP64 form of the same step
     plain = None
@@ -915,7 +929,7 @@ def main():
                "data": "synthetic: seeded inverse-ray-shot map, seeded tracks (no public dataset)",
                "config": workload_config(args), "roofline": roof, "cpu_baseline": cpu,
                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
-                       "ms_per_step": e2e_ms},
+                       "ms_per_step": e2e_ms, "link": link},
                "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
                "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair,
                "flux_ratio": flux, "c1_small_fp64": c1, "c4_fit": c4,

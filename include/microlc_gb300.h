@@ -206,10 +206,14 @@ typedef struct {
  * light curves come back in chunks of tracks on an internal device-to-host stream, each
  * chunk's copy overlapping the sampling of the next; host buffers should be page-locked
  * (cudaHostAlloc / cudaHostRegister) for the copies to overlap.
- * The call returns when out holds the result, unless MLC_ASYNC is given: then it returns
- * once the work is queued, the caller keeps pixels, the tracks and out untouched until
- * mlc_ctx_synchronize (or mlc_ctx_join + a sync of its stream), and the next call's
- * uploads and convolutions overlap this call's copies back.  Device memory held: the
+ * With device buffers the call is stream-ordered (it returns once queued; out is ready in
+ * the order of the context's stream, like every other device-buffer entry).  With
+ * MLC_IO_HOST it returns when out holds the result, unless MLC_ASYNC is given: then it
+ * returns once the work is queued, the caller keeps pixels, the tracks and out untouched
+ * until mlc_ctx_synchronize (or mlc_ctx_join + a sync of its stream), and the next call's
+ * uploads and convolutions overlap this call's copies back.  The profile rasters are
+ * computed on host threads and uploaded once per profile list: a call with the same list
+ * and map size as the previous call reuses them.  Device memory held: the
  * group's convolved maps and their interleaved copy (2 x min(nprof,16) maps), two track
  * buffers and an output ring of about twice one call's light curves (4 to 64 chunks). */
 int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof,

@@ -410,8 +410,8 @@ def convolve_sample_tracks(ctx: Context, m: Map, profiles, tracks: dict, mag=Tru
     stream) or all CPU tensors / numpy arrays (host buffers: copies overlap the kernels;
     page-locked tensors let them run asynchronously).  pixels: new map pixels (same
     location as the tracks) or None to keep the map's.  Returns out[nprof, nepochs].
-    With async_=True the call returns once queued; host results are valid after
-    ctx.synchronize().
+    Device buffers: stream-ordered on the context's stream.  Host buffers: the call returns
+    with out filled, or with async_=True once queued (out valid after ctx.synchronize()).
     """
     tr = {k: tracks[k] for k in TRACK_KEYS}
     first = tr["x0"]

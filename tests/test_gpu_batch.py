@@ -193,3 +193,28 @@ def test_no_tracks_and_errors(bctx):
         mixed["t"] = torch.as_tensor(trh["t"], device=DEV)
         mlc.convolve_sample_tracks(bctx, m, profs, mixed)
     m.close()
+
+
+def test_profile_rasters_reused_only_for_the_same_list(bctx):
+    """Back-to-back stream-ordered calls that alternate profile lists (and one repeat of a
+    list with new pixels) equal the one-call-per-stage results: the cached rasters of the
+    previous list are never used for another list."""
+    import microsn_gb300 as mlc
+    N = 300
+    mp1 = synth.lognormal_map(N, seed=31).astype(np.float32)
+    mp2 = synth.lognormal_map(N, seed=32).astype(np.float32)
+    m = mlc.Map(bctx, mp1, "f32")
+    pa = _profiles(6)
+    pb = [mlc.profile("gaussian", r, 1.0, ref_compat=False) for r in (2.0, 4.5, 7.0)]
+    trd = _device(_host_tracks(500, N, 33, np.float32))
+    outs = []
+    for profs in (pa, pb, pa, pa):
+        outs.append((profs, mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=True)))
+    pix2 = torch.as_tensor(mp2, device=DEV)
+    last = mlc.convolve_sample_tracks(bctx, m, pa, trd, mag=True, pixels=pix2)
+    torch.cuda.synchronize()
+    m1 = mlc.Map(bctx, mp1, "f32")
+    for profs, got in outs:
+        assert torch.equal(got, _separate(bctx, m1, profs, trd, True))
+    m2 = mlc.Map(bctx, mp2, "f32")
+    assert torch.equal(last, _separate(bctx, m2, pa, trd, True))
