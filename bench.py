@@ -506,6 +506,85 @@ def c5_workload(args, ctx, dev, rank):
 FR_N, FR_F, FR_T = 10_000, 7, 10
 
 
+RATIO_NLOC, RATIO_SIZES, RATIO_SEED = 9216, [0.0, 0.05, 0.1, 0.2, 0.3], 5
+RATIO_D, RATIO_S, RATIO_T = [0.7, 1.2, 1.4, 1.1, 0.9], [0.1, 0.15, 0.1, 0.1, 0.15], [5.0, 7.0, 12.0, 14.0, 17.0]
+
+
+def ratio_pair_workload(args, ctx, m, dev, rank):
+    """The reference's own pair path at its own size (driver.cpp:143-234 with random
+    locations, Nloc = 9216, 5 sizes, 300 log bins, 5 data points): light curves of two FP64
+    maps at fixed locations (expanding_source), the z-rank sort (setup_integral), and per
+    likelihood evaluation the ratio chi2 of all Nloc^2 pairs + bin means (reference form:
+    calculate_chi2 + bin_chi2) or the rank-free fused kernel; the oracle's C restatement of
+    calculate_chi2_CPU + bin_chi2_CPU timed on one core on a subset of locations."""
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    import oracle
+    n = m.Nx
+    Nloc = RATIO_NLOC if not args.small else 1024
+    mA = mlc.Map(ctx, m.tensor().double(), "f64")
+    mB = mlc.Map(ctx, torch.flip(m.tensor(), [0, 1]).double().contiguous(), "f64")  # image B: the map turned 180 deg
+    Noff = int(np.ceil((n / WIDTH) * RATIO_SIZES[-1]))
+    lx, ly = mlc.locations_random(Nloc, n, Noff, RATIO_SEED + rank)
+    base = mlc.profile("gaussian", 0.0, WIDTH / n)
+    ev = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    e0, e1 = ev()
+    e0.record()
+    LCA, DLCA = mlc.expanding_source(ctx, mA, RATIO_SIZES, base, WIDTH, lx, ly)
+    LCB, DLCB = mlc.expanding_source(ctx, mB, RATIO_SIZES, base, WIDTH, lx, ly)
+    e1.record()
+    torch.cuda.synchronize()
+    es_ms = e0.elapsed_time(e1)
+    del mA, mB
+    edges = mlc.bin_edges(300, 1e-4, 300.0, True)
+    Dfac = np.sqrt(1750.0 * 850.0 / 1570.0)
+    v = mlc.setup_chi2_calculation((0.4, 0.5), (1.0,), Dfac, np.array(RATIO_D), np.array(RATIO_T),
+                                   np.array(RATIO_S), np.array(RATIO_SIZES))
+
+    def timed(fn, k):
+        fn()
+        torch.cuda.synchronize()
+        a, b = ev()
+        a.record()
+        for _ in range(k):
+            r = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / k, r
+
+    setup_ms, (rank_t, lower, nper) = timed(lambda: mlc.setup_integral(ctx, LCA, LCB, edges), 3)
+    ref_ms, (bc, be) = timed(lambda: mlc.bin_chi2(ctx, lower, nper, mlc.calculate_chi2(ctx, v, LCA, DLCA, LCB, DLCB,
+                                                                                        rank_t)), 5)
+    fused_ms, (fb, fe, fn_) = timed(lambda: mlc.pair_bin_fused(ctx, v, LCA, DLCA, LCB, DLCB, edges), 5)
+    full = nper > 0
+    agree = bool(np.array_equal(fn_, nper) and np.allclose(fe[full], be[full], rtol=1e-12, atol=0))
+    pairs = float(Nloc) * Nloc
+    # CPU: the oracle's restatement of calculate_chi2_CPU + bin_chi2_CPU on a subset, one core
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        sub_n = 1200
+        A = LCA[:sub_n].cpu().numpy(); B = LCB[:sub_n].cpu().numpy()
+        dA = DLCA[:sub_n].cpu().numpy(); dB = DLCB[:sub_n].cpu().numpy()
+        r_o, l_o, n_o = oracle.pair_rank(A, B, edges)
+        ov = dict(Njp=v.Njp, indA=v.indA, indB=v.indB, facA=v.facA, facB=v.facB, d=v.d, s=v.s)
+        t0 = time.perf_counter()
+        c_o = oracle.pair_chi2_ratio(ov, A, dA, B, dB, r_o)
+        oracle.bin_chi2(l_o, n_o, c_o)
+        dt = time.perf_counter() - t0
+        cpu = {"kind": "port", "cores": 1, "pairs_per_s": sub_n * sub_n / dt,
+               "sample": f"{sub_n}^2 pairs of the same curves (calculate_chi2 + bin_chi2 restated in C)"}
+    return {"metric": "pair-chi2/s (reference ratio form)", "unit": "pair-chi2/s",
+            "config": {"workload": f"two {n}^2 FP64 maps (the bench map and its 180-degree turn), {Nloc} random "
+                                   f"locations, sizes {RATIO_SIZES} R_E gaussian, 300 log z-bins, Nd = 5",
+                       "pairs_per_evaluation": pairs},
+            "expanding_source_ms_two_maps": es_ms, "setup_integral_ms": setup_ms,
+            "reference_form": {"ms_per_evaluation": ref_ms, "value": pairs / (ref_ms / 1000.0)},
+            "fused": {"ms_per_evaluation": fused_ms, "value": pairs / (fused_ms / 1000.0)},
+            "fused_equals_reference_form": agree, "cpu": cpu}
+
+
 def flux_ratio_workload(args, ctx, dev, rank):
     import numpy as np
     import torch
@@ -611,7 +690,18 @@ def pair_workload(args, ctx, m, profs, n, dev, world, rank, stream):
     torch.cuda.synchronize()
     pms = e0.elapsed_time(e1)
     plain_val = world * sub_rows * float(N) / (pms / 1000.0)
+    # parity on a fixed 10^6-pair subset at full scale: the tensor-core chi2 matrix against
+    # the FP64 plain kernel on the same 1000 x 1000 curves
+    sa = torch.randperm(N, generator=torch.Generator().manual_seed(4))[:1000].to(A.device)
+    sb = torch.randperm(N, generator=torch.Generator().manual_seed(5))[:1000].to(A.device)
+    As, Bs = A[sa].contiguous(), B[sb].contiguous()
+    mt = mlc.pair_chi2_magdiff(ctx, As, Bs, w, d, True, method="tensor", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                               want_matrix=True)["matrix"].double()
+    mp_ = mlc.pair_chi2_magdiff(ctx, As, Bs, w, d, True, method="plain", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                                want_matrix=True)["matrix"].double()
+    rel = ((mt - mp_).abs() / mp_.abs().clamp_min(1e-30)).max().item()
     return {"metric": "pair-chi2/s", "value": value, "unit": "pair-chi2/s", "ms_per_step": ms, "steps": psteps,
+            "parity_subset": {"pairs": 1000 * 1000, "max_rel_err_vs_fp64": rel, "tolerance": 1e-5},
             "config": {"workload": f"images A, B: {N} x {N} FP32 magnitude curves, T={T} shared epochs, "
                                    f"sigma~U(0.02,0.1), offset-minimised, {PAIR_BINS}-bin log10-chi2 histogram, "
                                    f"top-{PAIR_K}", "pairs_per_step": pairs,
@@ -903,14 +993,33 @@ def main():
         plain = {"value": world * lc_per_step / (pms / 1000.0), "unit": UNIT, "ms_per_step": pms, "dtype": "f64",
                  "form": "full-size wrapped kernel + forward FFT + multiply + inverse FFT + sampling, per profile",
                  "batched_over_plain": value / (world * lc_per_step / (pms / 1000.0))}
-        del m64, convs64, tr64, out64
+        del convs64, out64
+        # the batched one-call step in FP64 (same map, profiles and tracks): FP32 and FP64 side by side
+        out64b = torch.empty((len(profs), E), dtype=torch.float64, device=dev)
+        pix64 = m64.tensor()
+
+        def step64b():
+            mlc.convolve_sample_tracks(ctx, m64, profs, tr64, mag=True, pixels=pix64, out=out64b)
+
+        step64b()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(3):
+            step64b()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        bms = e0.elapsed_time(e1) / 3
+        plain["batched_fp64"] = {"value": world * lc_per_step / (bms / 1000.0), "unit": UNIT, "ms_per_step": bms,
+                                 "batched_fp64_over_plain_fp64": pms / bms}
+        del m64, tr64, out64b, pix64
 
     # ---- pair-chi2/s workload on the same device
     pair = None
     if not args.no_pair:
         pair = pair_workload(args, ctx, m, profs, n, dev, world, rank, stream)
-    flux = c1 = c4 = c5 = None
+    flux = c1 = c4 = c5 = ratio = None
     if not args.no_pair:
+        ratio = ratio_pair_workload(args, ctx, m, dev, rank)
         flux = flux_ratio_workload(args, ctx, dev, rank)
         c1 = c1_workload(args, ctx, dev, rank)
         c4 = c4_workload(args, ctx, dev, rank)
@@ -931,6 +1040,10 @@ def main():
                "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(bi), "d2h_bytes_per_step": int(bo),
                        "ms_per_step": e2e_ms, "link": link},
                "gpu_launches": int(launches), "clocks": clk, "plain_fp64": plain, "kernels": kernels,
+               "sampling_stage": ({"value": world * lc_per_step / (kernels["sample_tracks_il"]["ms_per_step"] / 1000.0),
+                                   "unit": UNIT, "ms_per_step": kernels["sample_tracks_il"]["ms_per_step"]}
+                                  if "sample_tracks_il" in kernels else None),
+               "ratio_pairs": ratio,
                "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair,
                "flux_ratio": flux, "c1_small_fp64": c1, "c4_fit": c4,
                "c5_supernova": c5}
