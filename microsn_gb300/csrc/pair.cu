@@ -28,7 +28,8 @@ __global__ void k_pair_z(const double* __restrict__ LCA, const double* __restric
   const long P = (long)Nloc * Nloc;
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
     const int a = (int)(p / Nloc), b = (int)(p % Nloc);
-    keys[p] = key_of(__ldg(LCA + (long)a * Nprof) / __ldg(LCB + (long)b * Nprof));
+    const double z = __ldg(LCA + (long)a * Nprof) / __ldg(LCB + (long)b * Nprof);
+    keys[p] = z == z ? key_of(z) : ~0ull;  // NaN (0/0, whatever its sign bit) after every edge
     idx[p] = (uint32_t)p;
   }
 }
@@ -54,15 +55,28 @@ __global__ void k_upper_bound(const uint64_t* __restrict__ sorted, long P, const
   upper[i] = (uint32_t)lo;
 }
 
-// mA[i*Nloc + a] = LC[a*Nprof + ind_i] + fac_i * DLC[a*(Nprof-1) + ind_i], or 1 (ind_i = -1)
+// mA[i*Nloc + a] = LC[a*Nprof + ind_i] + fac_i * DLC[a*(Nprof-1) + ind_i], or 1 (ind_i = -1);
+// with invert, its correctly rounded reciprocal (the B side: one division per (epoch,
+// location) instead of one per pair)
 __global__ void k_interp(const double* __restrict__ LC, const double* __restrict__ DLC, int Nloc, int Nprof,
-                         int Njp, const int* __restrict__ ind, const double* __restrict__ fac,
+                         int Njp, const int* __restrict__ ind, const double* __restrict__ fac, int invert,
                          double* __restrict__ m) {
   const long n = (long)Nloc * Njp;
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
     const int i = (int)(q / Nloc), a = (int)(q % Nloc);
     const int k = ind[i];
-    m[q] = (k == -1) ? 1.0 : LC[(long)a * Nprof + k] + fac[i] * DLC[(long)a * (Nprof - 1) + k];
+    const double v = (k == -1) ? 1.0 : LC[(long)a * Nprof + k] + fac[i] * DLC[(long)a * (Nprof - 1) + k];
+    m[q] = invert ? 1.0 / v : v;
+  }
+}
+
+// Point-source values for the fused binning's float pre-search: zA[a] = (float)LCA[a*Nprof],
+// zB[b] = (float)(1 / LCB[b*Nprof]).
+__global__ void k_zfloat(const double* __restrict__ LCA, const double* __restrict__ LCB, int Nloc, int Nprof,
+                         float* __restrict__ zA, float* __restrict__ zB) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Nloc; q += gridDim.x * blockDim.x) {
+    zA[q] = (float)LCA[(long)q * Nprof];
+    zB[q] = (float)(1.0 / LCB[(long)q * Nprof]);
   }
 }
 
@@ -71,17 +85,19 @@ struct Chi2Consts {
   const double* s;
 };
 
-// One pair per thread: chi2 = sum_i ((d_i - mA_i/mB_i)/s_i)^2, FP64 with true division.
-__global__ void __launch_bounds__(256) k_pair_chi2_ratio(const double* __restrict__ mA, const double* __restrict__ mB,
+// One pair per thread: chi2 = sum_i ((d_i - mA_i/mB_i)/s_i)^2 in FP64, the divisions as
+// products with the correctly rounded reciprocals iB_i = 1/mB_i and is_i = 1/s_i (each term
+// within a few ulp of the divided form; GB300's FP64 divide is a long instruction sequence).
+__global__ void __launch_bounds__(256) k_pair_chi2_ratio(const double* __restrict__ mA, const double* __restrict__ iB,
                                                          int Nloc, int Njp, const double* __restrict__ d,
-                                                         const double* __restrict__ s, const uint32_t* __restrict__ rank,
+                                                         const double* __restrict__ is, const uint32_t* __restrict__ rank,
                                                          double* __restrict__ chi2) {
   const int b = blockIdx.x * 32 + (threadIdx.x & 31);
   const int a = blockIdx.y * 8 + (threadIdx.x >> 5);
   if (a >= Nloc || b >= Nloc) return;
   double c = 0.0;
   for (int i = 0; i < Njp; i++) {
-    const double tmp = (__ldg(d + i) - (__ldg(mA + (long)i * Nloc + a) / __ldg(mB + (long)i * Nloc + b))) / __ldg(s + i);
+    const double tmp = (__ldg(d + i) - __ldg(mA + (long)i * Nloc + a) * __ldg(iB + (long)i * Nloc + b)) * __ldg(is + i);
     c += tmp * tmp;
   }
   const long p = (long)a * Nloc + b;
@@ -126,43 +142,68 @@ __global__ void __launch_bounds__(256) k_bin_means(const double* __restrict__ ch
   }
 }
 
-// Fused rank-free pair binning.  Bin of z: smallest i with z <= edge_i (binary search),
-// z above the last edge dropped.  Sums in FP64 shared-memory accumulators, one flush
-// per CTA.  Each CTA covers 8 A curves x 256 B curves.
-__global__ void __launch_bounds__(256) k_pair_bin_fused(const double* __restrict__ mA, const double* __restrict__ mB,
+// Fused rank-free pair binning.  Bin of z = LCA_a / LCB_b: smallest i with z <= edge_i,
+// z above the last edge dropped.  The search runs on float copies (z32 = zA_a * zB_b within
+// 1.8e-7 of z, float edges within 6e-8 of the edges): when z32 is more than 2^-20 z32
+// away from both neighbouring float edges the float order is the FP64 order; otherwise
+// (and for zero, non-finite or extreme z32) the exact FP64 quotient is searched in the
+// FP64 edges.  chi2 as k_pair_chi2_ratio.  Sums in FP64 shared-memory accumulators, one
+// flush per CTA.  Each CTA covers 16 A curves x 256 B curves.
+constexpr int FUSED_A = 16;
+__global__ void __launch_bounds__(256) k_pair_bin_fused(const double* __restrict__ mA, const double* __restrict__ iB,
+                                                        const float* __restrict__ zA, const float* __restrict__ zB,
                                                         const double* __restrict__ LCA, const double* __restrict__ LCB,
                                                         int Nloc, int Nprof, int Njp, const double* __restrict__ d,
-                                                        const double* __restrict__ s, int nb,
+                                                        const double* __restrict__ is, int nb,
                                                         const double* __restrict__ edges, double* __restrict__ gsum,
                                                         double* __restrict__ gexp, unsigned long long* __restrict__ gcnt) {
   extern __shared__ double sm[];
   double* e_s = sm;
   double* sum_s = sm + nb;
   double* exp_s = sum_s + nb;
-  unsigned int* cnt_s = reinterpret_cast<unsigned int*>(exp_s + nb);
+  float* ef_s = reinterpret_cast<float*>(exp_s + nb);
+  unsigned int* cnt_s = reinterpret_cast<unsigned int*>(ef_s + nb);
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
     e_s[i] = edges[i];
+    ef_s[i] = (float)edges[i];
     sum_s[i] = 0.0;
     exp_s[i] = 0.0;
     cnt_s[i] = 0u;
   }
   __syncthreads();
   const int b = blockIdx.x * 256 + threadIdx.x;
-  const int a0 = blockIdx.y * 8;
+  const int a0 = blockIdx.y * FUSED_A;
   if (b < Nloc) {
-    const double zb = __ldg(LCB + (long)b * Nprof);
-    for (int a = a0; a < a0 + 8 && a < Nloc; a++) {
-      const double z = __ldg(LCA + (long)a * Nprof) / zb;
-      int lo = 0, hi = nb;  // first edge >= z
+    const float zb = __ldg(zB + b);
+    for (int a = a0; a < a0 + FUSED_A && a < Nloc; a++) {
+      const float z32 = __ldg(zA + a) * zb;
+      int lo = 0, hi = nb;  // first float edge >= z32
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (e_s[mid] < z) lo = mid + 1;
+        if (ef_s[mid] < z32) lo = mid + 1;
         else hi = mid;
+      }
+      bool exact = !(z32 > 0x1p-100f && z32 < 0x1p100f);
+      if (!exact) {
+        const float tol = z32 * 0x1p-20f;
+        exact = (lo < nb && ef_s[lo] - z32 <= tol) || (lo > 0 && z32 - ef_s[lo - 1] <= tol);
+      }
+      if (exact) {
+        const double z = __ldg(LCA + (long)a * Nprof) / __ldg(LCB + (long)b * Nprof);
+        if (z != z) continue;  // 0/0: the rank order puts NaN above every edge
+        lo = 0;
+        hi = nb;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (e_s[mid] < z) lo = mid + 1;
+          else hi = mid;
+        }
       }
       if (lo >= nb) continue;
       double c = 0.0;
       for (int i = 0; i < Njp; i++) {
-        const double tmp = (__ldg(d + i) - (__ldg(mA + (long)i * Nloc + a) / __ldg(mB + (long)i * Nloc + b))) / __ldg(s + i);
+        const double tmp =
+            (__ldg(d + i) - __ldg(mA + (long)i * Nloc + a) * __ldg(iB + (long)i * Nloc + b)) * __ldg(is + i);
         c += tmp * tmp;
       }
       atomicAdd(&sum_s[lo], c);
@@ -229,9 +270,9 @@ void pair_setup(mlc_ctx* ctx, int Nloc, int Nprof, const double* LCA, const doub
 
 struct Interp {
   double* mA;
-  double* mB;
+  double* iB;  // 1 / mB
   double* d;
-  double* s;
+  double* is;  // 1 / s
 };
 
 static Interp build_interp(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, const double* facA,
@@ -243,19 +284,19 @@ static Interp build_interp(mlc_ctx* ctx, int Njp, const int* indA, const int* in
   char* sm = (char*)ws_get(ctx, WS_LOC, sizeof(double) * 2 * n + small);
   Interp I;
   I.mA = (double*)sm;
-  I.mB = I.mA + n;
-  double* fA = I.mB + n;
+  I.iB = I.mA + n;
+  double* fA = I.iB + n;
   double* fB = fA + Njp;
   I.d = fB + Njp;
-  I.s = I.d + Njp;
-  int* iA = reinterpret_cast<int*>(I.s + Njp);
+  I.is = I.d + Njp;
+  int* iA = reinterpret_cast<int*>(I.is + Njp);
   int* iB = iA + Njp;
   std::vector<char> h(sizeof(double) * 4 * Njp + sizeof(int) * 2 * Njp);
   double* hd = reinterpret_cast<double*>(h.data());
   std::copy(facA, facA + Njp, hd);
   std::copy(facB, facB + Njp, hd + Njp);
   std::copy(d, d + Njp, hd + 2 * Njp);
-  std::copy(s, s + Njp, hd + 3 * Njp);
+  for (int i = 0; i < Njp; i++) hd[3 * Njp + i] = 1.0 / s[i];
   int* hi = reinterpret_cast<int*>(hd + 4 * Njp);
   std::copy(indA, indA + Njp, hi);
   std::copy(indB, indB + Njp, hi + Njp);
@@ -267,12 +308,12 @@ static Interp build_interp(mlc_ctx* ctx, int Njp, const int* indA, const int* in
   if (n > 0) {
     {
       MLC_KSCOPE(ctx, "pair_interp");
-      k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCA, DLCA, Nloc, Nprof, Njp, iA, fA, I.mA);
+      k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCA, DLCA, Nloc, Nprof, Njp, iA, fA, 0, I.mA);
     }
     MLC_CHECK_LAUNCH();
     {
       MLC_KSCOPE(ctx, "pair_interp");
-      k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCB, DLCB, Nloc, Nprof, Njp, iB, fB, I.mB);
+      k_interp<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(LCB, DLCB, Nloc, Nprof, Njp, iB, fB, 1, I.iB);
     }
     MLC_CHECK_LAUNCH();
   }
@@ -286,7 +327,7 @@ void pair_chi2_ratio(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, co
   dim3 grid(ceil_div(Nloc, 32), ceil_div(Nloc, 8));
   {
     MLC_KSCOPE(ctx, "pair_chi2_ratio");
-    k_pair_chi2_ratio<<<grid, 256, 0, ctx->stream>>>(I.mA, I.mB, Nloc, Njp, I.d, I.s, rank, chi2);
+    k_pair_chi2_ratio<<<grid, 256, 0, ctx->stream>>>(I.mA, I.iB, Nloc, Njp, I.d, I.is, rank, chi2);
   }
   MLC_CHECK_LAUNCH();
 }
@@ -317,20 +358,27 @@ void pair_bin_fused(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, con
                     double* bchi2_host, double* bexp_host, uint32_t* nper_host) {
   MLC_REQUIRE(Nbins > 0 && Nbins <= 6000, MLC_ERR_LIMIT, "fused pair binning supports 1..6000 bins");
   Interp I = build_interp(ctx, Njp, indA, indB, facA, facB, d, s, Nloc, Nprof, LCA, DLCA, LCB, DLCB);
-  char* sm = (char*)ws_get(ctx, WS_PAIR_ACC, (sizeof(double) * 3 + 8) * Nbins + 64);
+  char* sm = (char*)ws_get(ctx, WS_PAIR_ACC, (sizeof(double) * 3 + 8) * Nbins + 2 * sizeof(float) * Nloc + 128);
   double* de = (double*)sm;
   double* gs = de + Nbins;
   double* ge = gs + Nbins;
   unsigned long long* gc = reinterpret_cast<unsigned long long*>(ge + Nbins);
+  float* zA = reinterpret_cast<float*>(gc + Nbins);
+  float* zB = zA + Nloc;
+  {
+    MLC_KSCOPE(ctx, "pair_interp");
+    k_zfloat<<<grid_for(ctx, Nloc), 256, 0, ctx->stream>>>(LCA, LCB, Nloc, Nprof, zA, zB);
+  }
+  MLC_CHECK_LAUNCH();
   MLC_CUDA(cudaMemcpyAsync(de, edges_host, sizeof(double) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
   MLC_CUDA(cudaMemsetAsync(gs, 0, (sizeof(double) * 2 + 8) * Nbins, ctx->stream));
-  const size_t smem = (sizeof(double) * 3 + sizeof(unsigned)) * Nbins;
+  const size_t smem = (sizeof(double) * 3 + sizeof(float) + sizeof(unsigned)) * Nbins;
   set_max_smem((const void*)k_pair_bin_fused, smem);
-  dim3 grid(ceil_div(Nloc, 256), ceil_div(Nloc, 8));
+  dim3 grid(ceil_div(Nloc, 256), ceil_div(Nloc, FUSED_A));
   {
     MLC_KSCOPE(ctx, "pair_bin_fused");
-    k_pair_bin_fused<<<grid, 256, smem, ctx->stream>>>(I.mA, I.mB, LCA, LCB, Nloc, Nprof, Njp, I.d, I.s, Nbins, de,
-                                                      gs, ge, gc);
+    k_pair_bin_fused<<<grid, 256, smem, ctx->stream>>>(I.mA, I.iB, zA, zB, LCA, LCB, Nloc, Nprof, Njp, I.d, I.is,
+                                                      Nbins, de, gs, ge, gc);
   }
   MLC_CHECK_LAUNCH();
   std::vector<double> hs(Nbins), he(Nbins);

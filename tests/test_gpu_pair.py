@@ -91,3 +91,27 @@ def test_histogram_matches_oracle(ctx):
         got = mlc.histogram_f64(ctx, torch.as_tensor(v, device=DEV), 100, lo, hi, log)
         ref, near = oracle.histogram(v, 100, lo, hi, log, rel_tol=1e-14)
         assert np.abs(got.astype(np.int64) - ref.astype(np.int64)).sum() <= 2 * near
+
+
+def test_fused_bins_exact_at_edges(ctx, golden):
+    """z exactly on a bin edge, one ulp either side, zero, infinite and NaN quotients: the
+    fused kernel's float pre-search must give the rank path's counts exactly."""
+    import microsn_gb300 as mlc
+    edges = mlc.bin_edges(300, 1e-4, 300, True)
+    k = np.arange(0, 300, 7)
+    za = np.concatenate([edges[k], np.nextafter(edges[k], 0), np.nextafter(edges[k], np.inf),
+                         [0.0, 1e-300, 1e300, edges[-1] * 1.0000001, 5e-5]])
+    Nloc, Nprof = za.size, 5
+    rng = np.random.default_rng(3)
+    LCA = np.exp(rng.normal(0, 0.3, (Nloc, Nprof))); LCB = np.exp(rng.normal(0, 0.3, (Nloc, Nprof)))
+    LCA[:, 0] = za
+    LCB[:, 0] = 1.0          # z = LCA / 1 exactly for these columns
+    LCB[-5:, 0] = [0.0, 2.0, 0.5, 1.0, 1e-300]  # 0 -> inf / NaN quotients, tiny -> huge
+    tA = torch.as_tensor(LCA, device=DEV); tB = torch.as_tensor(LCB, device=DEV)
+    dA = torch.as_tensor(np.diff(LCA, axis=1).copy(), device=DEV); dB = torch.as_tensor(np.diff(LCB, axis=1).copy(), device=DEV)
+    _, lower, nper = mlc.setup_integral(ctx, tA, tB, edges)
+    v = _vars(golden)
+    fb, fe, fn = mlc.pair_bin_fused(ctx, v, tA, dA, tB, dB, edges)
+    assert np.array_equal(fn, nper)
+    fin = np.isfinite(LCA[:, 0][:, None] / np.where(LCB[:, 0] == 0, np.nan, LCB[:, 0])[None, :]).all()
+    assert not fin  # the case includes quotients outside the finite range
