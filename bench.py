@@ -994,12 +994,15 @@ def main():
                  "form": "full-size wrapped kernel + forward FFT + multiply + inverse FFT + sampling, per profile",
                  "batched_over_plain": value / (world * lc_per_step / (pms / 1000.0))}
         del convs64, out64
-        # the batched one-call step in FP64 (same map, profiles and tracks): FP32 and FP64 side by side
+        # the batched one-call step in FP64 on the FP32 step's own inputs (the FP32 track
+        # parameters upcast, the same map pixels): FP32 and FP64 side by side, and the FP32
+        # light curves' error against it over every sample
         out64b = torch.empty((len(profs), E), dtype=torch.float64, device=dev)
         pix64 = m64.tensor()
+        tr64f = {k: (a.double() if a.is_floating_point() else a) for k, a in tr.items()}
 
         def step64b():
-            mlc.convolve_sample_tracks(ctx, m64, profs, tr64, mag=True, pixels=pix64, out=out64b)
+            mlc.convolve_sample_tracks(ctx, m64, profs, tr64f, mag=True, pixels=pix64, out=out64b)
 
         step64b()
         torch.cuda.synchronize()
@@ -1009,9 +1012,20 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         bms = e0.elapsed_time(e1) / 3
+        step()  # the FP32 light curves of the same inputs
+        dmax, fin32, fin64 = 0.0, 0, 0
+        for q in range(len(profs)):
+            a32, a64 = out[q].double(), out64b[q]
+            ok = torch.isfinite(a32) & torch.isfinite(a64)
+            fin32 += int(torch.isfinite(a32).sum()); fin64 += int(torch.isfinite(a64).sum())
+            dmax = max(dmax, float((a32 - a64).abs()[ok].max()))
         plain["batched_fp64"] = {"value": world * lc_per_step / (bms / 1000.0), "unit": UNIT, "ms_per_step": bms,
                                  "batched_fp64_over_plain_fp64": pms / bms}
-        del m64, tr64, out64b, pix64
+        plain["fp32_vs_fp64"] = {"samples": int(len(profs) * E), "max_abs_mag": dmax,
+                                 "max_rel_flux": 10 ** (0.4 * dmax) - 1.0,
+                                 "finite_fp32": fin32, "finite_fp64": fin64,
+                                 "inputs": "same map pixels, FP32 track parameters upcast for the FP64 run"}
+        del m64, tr64, out64b, pix64, tr64f
 
     # ---- pair-chi2/s workload on the same device
     pair = None

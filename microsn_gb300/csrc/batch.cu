@@ -296,8 +296,13 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     t = d + 4 * sp + so;
   }
 
-  // ---- profile groups of up to 16: convolve, interleave, sample
-  char* maps = (char*)ws_get(ctx, WS_BATCH_MAPS, (size_t)nm_max * npix * es);
+  // ---- profile groups of up to 16: convolve, interleave, sample.  Where the row length has
+  // a register c2r kernel, each profile stops at its inverse half-spectrum and one
+  // cluster kernel runs the last pass of all the group's profiles straight into the
+  // interleaved layout (no planar maps, no separate interleave pass).
+  const bool fuse_il = ntr > 0 && mode == MLC_CONV_FUSED && rows_c2r_interleave_supported(*p);
+  const size_t slot = fuse_il ? p->spec_bytes() : (size_t)npix * es;
+  char* maps = (char*)ws_get(ctx, WS_BATCH_MAPS, (size_t)nm_max * slot);
   void* imap = ntr > 0 ? ws_get(ctx, WS_BATCH_IMAP, (size_t)pow2_at_least(nm_max) * npix * es) : nullptr;
   bool tracks_ready = false;
   for (int g0 = 0; g0 < nprof; g0 += 16) {
@@ -305,13 +310,15 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     const int stride = pow2_at_least(nm);
     const void* mp[16];
     for (int q = 0; q < nm; q++) {
-      mp[q] = maps + (size_t)q * npix * es;
+      mp[q] = maps + (size_t)q * slot;
       const double* pr = dprof + poff[g0 + q];
-      if (mode == MLC_CONV_FUSED) conv_fused(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+      if (fuse_il) conv_fused_spectrum(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+      else if (mode == MLC_CONV_FUSED) conv_fused(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
       else conv_plain(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
     }
     if (ntr == 0) continue;
-    interleave(ctx, mp, nm, npix, map->prec, stride, imap);
+    if (fuse_il) rows_c2r_interleave(ctx, *p, maps, (long)(slot / (2 * es)), nm, stride, imap);
+    else interleave(ctx, mp, nm, npix, map->prec, stride, imap);
     if (!host) {
       sample_tracks_il(ctx, imap, stride, nm, Nx, Ny, map->prec, ntr, x0, y0, phi, v, off, t, mag,
                        (char*)out + (size_t)g0 * E * es, (long)E, 0);

@@ -20,6 +20,8 @@
 //     P3  inverse real FFT of each row (c2r)
 //   plain convolution (MLC_CONV_PLAIN): full-size wrapped kernel, full forward,
 //     pointwise multiply, full inverse -- one launch per stage, like the reference.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -273,14 +275,10 @@ __global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, 
 // M = 5000 in FP32).  Items of levels 2 and 3 fit in one pass of the CTA (L1 L3 and
 // L1 L2 <= blockDim).
 template <typename T, int L1, int L2, int L3>
-__global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in, long pitch, T* __restrict__ out,
-                                                   long ldo, const C2<T>* __restrict__ twx) {
+__device__ __forceinline__ void c2r3_row(const C2<T>* __restrict__ a, const C2<T>* __restrict__ twx, C2<T>* s) {
   constexpr int J = L2 * L3, M = L1 * J;
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* wJ = s + M;  // W_J^e = W_Nx^(2 L1 e), e < J
-  const int row = blockIdx.x, tid = threadIdx.x;
-  const C2<T>* a = in + (long)row * pitch;
+  const int tid = threadIdx.x;
   for (int e = tid; e < J; e += blockDim.x) wJ[e] = ldc(twx + 2L * L1 * e);
   for (int j = tid; j < J; j += blockDim.x) {
     C2<T> v[L1];
@@ -332,8 +330,68 @@ __global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in,
     }
   }
   __syncthreads();
+}
+
+template <typename T, int L1, int L2, int L3>
+__global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in, long pitch, T* __restrict__ out,
+                                                   long ldo, const C2<T>* __restrict__ twx) {
+  constexpr int M = L1 * L2 * L3;
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
+  const int row = blockIdx.x;
+  c2r3_row<T, L1, L2, L3>(in + (long)row * pitch, twx, s);
   C2<T>* dst = reinterpret_cast<C2<T>*>(out + (long)row * ldo);
-  for (int n = tid; n < M; n += blockDim.x) dst[n] = s[n];
+  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = s[n];
+}
+
+// P3 of eight profiles with the interleave fused in.  A cluster of eight CTAs takes one row
+// of eight profiles' spectra (CTA rank k: profile 8*half + k; ranks past nm hold zeros),
+// each CTA runs the three-level c2r of its row into its own shared memory, and after a
+// cluster barrier CTA k writes pixels [k Nx/8, (k+1) Nx/8) of the interleaved row, reading
+// the eight rows through distributed shared memory: out[(row Nx + x) S + 8 half + q].  With
+// S >= 8 every pixel gets one full 32-byte sector (FP32) per cluster, so the separate
+// interleave pass and the planar maps are not needed; the arithmetic is k_rows_c2r3's.
+template <typename T, int L1, int L2, int L3>
+__global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256)
+    k_rows_c2r3_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm, T* __restrict__ out, int S,
+                   const C2<T>* __restrict__ twx) {
+  constexpr int J = L2 * L3, M = L1 * J, NX = 2 * M;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ unsigned char smem_raw[];
+  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
+  const int row = blockIdx.y;
+  const int k = (int)cl.block_rank(), half = blockIdx.x >> 3, q = 8 * half + k;
+  if (q < nm) {
+    c2r3_row<T, L1, L2, L3>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
+  } else {
+    for (int n = threadIdx.x; n < M; n += blockDim.x) s[n] = C2<T>{T(0), T(0)};
+  }
+  cl.sync();  // every row of the cluster is in its CTA's shared memory
+  const int W = S - 8 * half < 8 ? S - 8 * half : 8;  // values per pixel from this cluster
+  constexpr int CH = (NX + 7) / 8;
+  const int x0 = k * CH, x1 = x0 + CH < NX ? x0 + CH : NX;
+  T* dst = out + (long)row * NX * S + 8 * half;
+  if (W == 8) {
+    const T* src[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) src[r] = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
+    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+      T v[8];
+#pragma unroll
+      for (int r = 0; r < 8; r++) v[r] = src[r][x];
+      float4* d = reinterpret_cast<float4*>(dst + (long)x * S);
+      const float4* w = reinterpret_cast<const float4*>(v);
+#pragma unroll
+      for (int i = 0; i < (int)(8 * sizeof(T) / 16); i++) d[i] = w[i];
+    }
+  } else {
+    for (int r = 0; r < W; r++) {
+      const T* sr = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = sr[x];
+    }
+  }
+  cl.sync();  // no CTA leaves while the others still read its shared memory
 }
 
 // ---------------------------------------------------------------- column kernels
@@ -714,15 +772,17 @@ void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype
   else forward_impl<float>(ctx, p, in, in_dtype, spec);
 }
 
+// spec_out: stop after P2 and leave the inverse half-spectrum there (pitch Wp) instead of
+// running P3 into out.
 template <typename T>
 static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
-                            void* out) {
+                            void* out, void* spec_out = nullptr) {
   constexpr int CW = sizeof(T) == 8 ? 8 : 16;
   const int h = pN / 2;
   MLC_REQUIRE(pN % 2 == 0 && 2 * h <= p.Ny && 2 * h <= p.Nx, MLC_ERR_LIMIT,
               "profile raster larger than the map");
   void* kx = ws_get(ctx, WS_KX, (size_t)(2 * h > 0 ? 2 * h : 1) * p.Wp * sizeof(C2<T>));
-  void* tmp = ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
+  void* tmp = spec_out ? spec_out : ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
   launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
   const int nstrips = ceil_div(p.Wc, CW);
   const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
@@ -751,7 +811,7 @@ static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
       }
       MLC_CHECK_LAUNCH();
       launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
-      launch_rows_c2r<T>(ctx, p, tmp, out);
+      if (!spec_out) launch_rows_c2r<T>(ctx, p, tmp, out);
       return;
     }
   }
@@ -766,7 +826,7 @@ static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
   }
   MLC_CHECK_LAUNCH();
   launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
-  launch_rows_c2r<T>(ctx, p, tmp, out);
+  if (!spec_out) launch_rows_c2r<T>(ctx, p, tmp, out);
 }
 
 template <typename T>
@@ -799,6 +859,48 @@ static void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
 void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
   if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, out);
   else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, out);
+}
+
+void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
+                         void* spec_out) {
+  if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
+  else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
+}
+
+template <typename T>
+static bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
+                                void* out) {
+  using K = void (*)(const C2<T>*, long, long, int, T*, int, const C2<T>*);
+  K k = nullptr;
+  int J = 0;
+  switch (p.M) {
+    case 5000: k = k_rows_c2r3_il<T, 8, 25, 25>; J = 625; break;
+    case 4096: k = k_rows_c2r3_il<T, 16, 16, 16>; J = 256; break;
+    case 2000: k = k_rows_c2r3_il<T, 8, 10, 25>; J = 250; break;
+    case 1000: k = k_rows_c2r3_il<T, 10, 10, 10>; J = 100; break;
+    default: return false;
+  }
+  if (!rows_c2r_interleave_supported(p)) return false;
+  const size_t smem = ((size_t)p.M + J) * sizeof(C2<T>);
+  set_max_smem((const void*)k, smem);
+  const int halves = (nm + 7) / 8;
+  {
+    MLC_KSCOPE(ctx, "fft_rows_c2r_interleave");
+    k<<<dim3(8 * halves, p.Ny), 256, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (T*)out, S,
+                                                          (const C2<T>*)p.twx);
+  }
+  MLC_CHECK_LAUNCH();
+  return true;
+}
+
+bool rows_c2r_interleave_supported(const FftPlan2D& p) {
+  return (p.M == 5000 || p.M == 4096 || p.M == 2000 || p.M == 1000) && p.Ny <= 65535;  // rows on grid.y
+}
+
+bool rows_c2r_interleave(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
+                         void* out) {
+  if (p.prec == MLC_F64) return c2r_interleave_impl<double>(ctx, p, specs, spec_stride, nm, S, out);
+  return c2r_interleave_impl<float>(ctx, p, specs, spec_stride, nm, S, out);
 }
 
 void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {

@@ -143,6 +143,15 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec);
 void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec);
 void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof_dev, int pN,
                 void* out_real);
+// conv_fused up to P2: the inverse half-spectrum (Ny x Wp complex) into spec_out.
+void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
+                         void* spec_out);
+// P3 of nm (<= 16) such spectra (spec_stride complex elements apart) written straight into
+// the interleaved layout out[(y Nx + x) S + q] (S a power of two >= nm, slots >= nm zero).
+// False (nothing launched) when the row length has no register kernel.
+bool rows_c2r_interleave_supported(const FftPlan2D& p);
+bool rows_c2r_interleave(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
+                         void* out);
 void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof_dev, int pN,
                 void* out_real);
 

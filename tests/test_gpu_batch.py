@@ -218,3 +218,21 @@ def test_profile_rasters_reused_only_for_the_same_list(bctx):
         assert torch.equal(got, _separate(bctx, m1, profs, trd, True))
     m2 = mlc.Map(bctx, mp2, "f32")
     assert torch.equal(last, _separate(bctx, m2, pa, trd, True))
+
+
+@pytest.mark.parametrize("prec,nprof", [("f32", 3), ("f32", 8), ("f32", 12), ("f32", 16), ("f32", 21), ("f64", 9)])
+def test_fused_last_pass_interleave_equals_separate_calls(bctx, prec, nprof):
+    """At a row length with a register c2r kernel (2000^2: 1000-point rows) the step runs the
+    last inverse pass of a group's profiles as one cluster kernel writing the interleaved
+    layout (interleave strides 4, 8 and 16, clusters with empty slots, two groups).  Its
+    light curves must equal the one-call-per-stage results bit for bit."""
+    import microsn_gb300 as mlc
+    N = 2000
+    dt = np.float32 if prec == "f32" else np.float64
+    mp = synth.lognormal_map(N, seed=41).astype(dt)
+    m = mlc.Map(bctx, mp, prec)
+    profs = _profiles(nprof)
+    trd = _device(_host_tracks(600, N, 42, dt))
+    got = mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=True)
+    ref = _separate(bctx, m, profs, trd, True)
+    assert torch.equal(got, ref)
