@@ -1058,6 +1058,7 @@ def main():
                                    "unit": UNIT, "ms_per_step": kernels["sample_tracks_il"]["ms_per_step"]}
                                   if "sample_tracks_il" in kernels else None),
                "ratio_pairs": ratio,
+               "autotune": {k: {"choice": c, "ms": m} for k, (c, m) in ctx.autotune_report().items()},
                "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair,
                "flux_ratio": flux, "c1_small_fp64": c1, "c4_fit": c4,
                "c5_supernova": c5}

@@ -96,6 +96,17 @@ unsigned long long mlc_ctx_launch_count(const mlc_ctx* ctx);
  * '\n'-separated list into names_host (size name_cap) -- and returns the entry count
  * (or a negative status).  reset != 0 clears the totals afterwards. */
 int mlc_ctx_set_timing(mlc_ctx* ctx, int on);
+
+/* Launch autotuner (on by default; no reference counterpart).  For each new (map size,
+ * profile size) of an FP32 fused convolution the first call times the FFT form against
+ * the direct tiled form's tile shapes (mlc_convolve_direct) on the context's stream and
+ * keeps the fastest; later calls reuse the choice.  Tuning synchronises the stream once
+ * per key and is skipped while the stream is captured into a CUDA graph.  Off: the FFT
+ * form everywhere (results then do not depend on timings).  The report lists every tuned
+ * key, its choice and the candidates' times: NUL-terminated text into buf (cap bytes);
+ * returns the text length, or a negative status. */
+int mlc_ctx_set_autotune(mlc_ctx* ctx, int on);
+int mlc_ctx_autotune_report(mlc_ctx* ctx, char* buf, int cap);
 int mlc_ctx_kernel_times(mlc_ctx* ctx, char* names_host, int name_cap, double* ms_host, long* launches_host,
                          int cap, int reset);
 
@@ -133,6 +144,12 @@ int mlc_map_refresh(mlc_ctx* ctx, mlc_map* map);
  * (magnification_map.cpp:172-193), forward transform, multiply / (Nx Ny)
  * (kernel_multiplyFFTs :571-577) and inverse transform, with hand-written FFTs. */
 int mlc_convolve(mlc_ctx* ctx, mlc_map* map, const mlc_profile* prof, int mode, void* out);
+
+/* The direct tiled convolution (no FFT) of an FP32 map with a profile of 2..32 pixels,
+ * tile shape variant 0..3 (4x4, 4x8, 8x4, 8x8 outputs per thread): the same circular
+ * convolution with the reference's kernel wrap as mlc_convolve (Kernel::setKernel,
+ * magnification_map.cpp:172-193).  No reference counterpart. */
+int mlc_convolve_direct(mlc_ctx* ctx, mlc_map* map, const mlc_profile* prof, int variant, void* out);
 
 /* Replaces expanding_source (gpu_functions.cu:82-225) for an FP64 map: LC (Nloc x Nprof)
  * and DLC (Nloc x (Nprof-1)), location-major like SimLC (data_structs.hpp:50-63).

@@ -5,7 +5,7 @@ FFT convolution of magnification maps with source profiles, light-curve sampling
 pairwise, sort and binning), as hand-written sm_103a CUDA kernels behind the C ABI in
 include/microlc_gb300.h.  This package is the Python host mirror of that ABI.
 """
-from .api import (Chi2Vars, Context, Map, bin_chi2, bin_edges, calculate_chi2, chi2_offset, convolve,
+from .api import (Chi2Vars, Context, Map, bin_chi2, bin_edges, calculate_chi2, chi2_offset, convolve, convolve_direct,
                   expanding_source, histogram_f64, interleave_maps, locations_grid, locations_random, pair_bin_fused, profile,
                   profile_raster, read_gerlumph, sample_tracks, sample_tracks_interleaved, setup_chi2_calculation, setup_integral,
                   sort_f64_u32, trapezium)
@@ -17,7 +17,7 @@ from .api import FIT_PARAMS, TrackChi2, fit_raster, radius_stack, track_chi2, tr
 from ._lib import MlcError
 
 __all__ = [
-    "Chi2Vars", "Context", "Map", "MlcError", "bin_chi2", "bin_edges", "calculate_chi2", "chi2_offset", "convolve",
+    "Chi2Vars", "Context", "Map", "MlcError", "bin_chi2", "bin_edges", "calculate_chi2", "chi2_offset", "convolve", "convolve_direct",
     "convolve_sample_tracks", "pair_chi2_magdiff", "pair_chi2_magdiff_list", "map_binned_mpd", "mpd_divide",
     "mpd_normalize", "flux_ratio_chi2", "track_chi2_offset", "convolve_many", "sample_expanding", "FIT_PARAMS", "TrackChi2", "fit_raster", "radius_stack", "track_chi2",
     "track_fit",

@@ -61,6 +61,8 @@ SIGNATURES = {
     "mlc_ctx_workspace_bytes": (C.c_size_t, [vp]),
     "mlc_ctx_launch_count": (C.c_ulonglong, [vp]),
     "mlc_ctx_set_timing": (i32, [vp, i32]),
+    "mlc_ctx_set_autotune": (i32, [vp, i32]),
+    "mlc_ctx_autotune_report": (i32, [vp, C.c_char_p, i32]),
     "mlc_ctx_kernel_times": (i32, [vp, C.c_char_p, i32, vp, vp, i32, i32]),
     "mlc_map_refresh": (i32, [vp, vp]),
     "mlc_profile_dims": (i32, [C.POINTER(MlcProfile), P_i32]),
@@ -70,6 +72,7 @@ SIGNATURES = {
     "mlc_map_data": (i32, [vp, C.POINTER(vp)]),
     "mlc_map_prepare": (i32, [vp, vp]),
     "mlc_convolve": (i32, [vp, vp, C.POINTER(MlcProfile), i32, vp]),
+    "mlc_convolve_direct": (i32, [vp, vp, C.POINTER(MlcProfile), i32, vp]),
     "mlc_expanding_source": (i32, [vp, vp, vp, i32, C.POINTER(MlcProfile), f64, i32, vp, vp, i32, vp, vp]),
     "mlc_sample_nearest": (i32, [vp, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
     "mlc_sample_tracks": (i32, [vp, vp, i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),

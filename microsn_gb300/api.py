@@ -79,6 +79,23 @@ class Context:
     def set_timing(self, on: bool):
         self.check(self.L.mlc_ctx_set_timing(self.h, int(on)))
 
+    def set_autotune(self, on: bool):
+        """Launch autotuner on (default) or off (FFT form everywhere)."""
+        self.check(self.L.mlc_ctx_set_autotune(self.h, int(on)))
+
+    def autotune_report(self) -> dict:
+        """{key: (choice, {candidate: ms})} of every tuned key."""
+        buf = C.create_string_buffer(1 << 16)
+        n = self.L.mlc_ctx_autotune_report(self.h, buf, len(buf))
+        if n < 0:
+            self.check(-n)
+        out = {}
+        for line in buf.value.decode().splitlines():
+            key, rest = line.split(": ", 1)
+            choice, _, cands = rest.partition(" (")
+            out[key] = (choice, {c.split("=")[0]: float(c.split("=")[1]) for c in cands.rstrip(")").split()})
+        return out
+
     def kernel_times(self, reset: bool = True) -> dict:
         """{kernel name: (total ms, launches)} from the per-launch CUDA events."""
         names = C.create_string_buffer(1 << 16)
@@ -196,6 +213,14 @@ def convolve(ctx: Context, m: Map, prof: MlcProfile, mode: str = "fused", out: t
     if out is None:
         out = torch.empty((m.Ny, m.Nx), dtype=m.dtype, device=f"cuda:{ctx.device}")
     ctx.check(ctx.L.mlc_convolve(ctx.h, m.h, C.byref(prof), _MODES[mode], _ptr(out)))
+    return out
+
+
+def convolve_direct(ctx: Context, m: Map, prof: MlcProfile, variant: int = 0, out: torch.Tensor | None = None):
+    """The direct tiled convolution (FP32 map, profile of 2..32 pixels), tile shape 0..3."""
+    if out is None:
+        out = torch.empty((m.Ny, m.Nx), dtype=m.dtype, device=f"cuda:{ctx.device}")
+    ctx.check(ctx.L.mlc_convolve_direct(ctx.h, m.h, C.byref(prof), int(variant), _ptr(out)))
     return out
 
 

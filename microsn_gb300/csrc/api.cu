@@ -2,6 +2,7 @@
 // Every entry point catches mlc::Error (and std::exception) and returns a status; the
 // message is kept in the context for mlc_ctx_last_error().
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -135,6 +136,23 @@ static void resolve_timings(mlc_ctx* ctx) {
     cudaEventDestroy(p.b);
   }
   ctx->pending.clear();
+}
+
+int mlc_ctx_set_autotune(mlc_ctx* ctx, int on) {
+  return guarded(ctx, [&] { ctx->autotune = on != 0; });
+}
+
+int mlc_ctx_autotune_report(mlc_ctx* ctx, char* buf, int cap) {
+  if (!ctx || !buf || cap < 1) return -MLC_ERR_ARG;
+  int n = 0;
+  const int st = guarded(ctx, [&] {
+    const std::string s = autotune_report(ctx);
+    n = (int)s.size();
+    const int m = std::min(n, cap - 1);
+    std::memcpy(buf, s.data(), (size_t)m);
+    buf[m] = 0;
+  });
+  return st == MLC_OK ? n : -st;
 }
 
 int mlc_ctx_set_timing(mlc_ctx* ctx, int on) {
@@ -317,8 +335,19 @@ static void convolve_impl(mlc_ctx* ctx, mlc_map* map, const mlc_profile& pr, int
   FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
   int N = 0;
   const double* prof = upload_profile(ctx, pr, &N);
-  if (mode == MLC_CONV_FUSED) conv_fused(ctx, *p, map->spec, prof, N, out);
+  if (mode == MLC_CONV_FUSED) conv_auto(ctx, *p, map->data, map->spec, prof, N, out);
   else conv_plain(ctx, *p, map->spec, prof, N, out);
+}
+
+int mlc_convolve_direct(mlc_ctx* ctx, mlc_map* map, const mlc_profile* prof, int variant, void* out) {
+  if (!ctx || !map || !prof || !out) return fail(ctx, MLC_ERR_ARG, "null argument");
+  return guarded(ctx, [&] {
+    MLC_REQUIRE(map->prec == MLC_F32, MLC_ERR_ARG, "the direct convolution takes FP32 maps");
+    FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
+    int N = 0;
+    const double* d = upload_profile(ctx, *prof, &N);
+    conv_direct(ctx, *p, map->data, d, N, variant, out);
+  });
 }
 
 int mlc_convolve(mlc_ctx* ctx, mlc_map* map, const mlc_profile* prof, int mode, void* out) {

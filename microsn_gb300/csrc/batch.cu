@@ -309,15 +309,26 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     const int nm = std::min(16, nprof - g0);
     const int stride = pow2_at_least(nm);
     const void* mp[16];
+    unsigned planar = 0;  // slots holding a real map from the direct form
     for (int q = 0; q < nm; q++) {
       mp[q] = maps + (size_t)q * slot;
       const double* pr = dprof + poff[g0 + q];
-      if (fuse_il) conv_fused_spectrum(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
-      else if (mode == MLC_CONV_FUSED) conv_fused(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
-      else conv_plain(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+      const int dv = mode == MLC_CONV_FUSED
+                         ? conv_direct_choice(ctx, *p, map->data, map->spec, pr, pN[g0 + q], (void*)mp[q], fuse_il)
+                         : -1;
+      if (dv >= 0) {
+        conv_direct(ctx, *p, map->data, pr, pN[g0 + q], dv, (void*)mp[q]);
+        planar |= 1u << q;
+      } else if (fuse_il) {
+        conv_fused_spectrum(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+      } else if (mode == MLC_CONV_FUSED) {
+        conv_fused(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+      } else {
+        conv_plain(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+      }
     }
     if (ntr == 0) continue;
-    if (fuse_il) rows_c2r_interleave(ctx, *p, maps, (long)(slot / (2 * es)), nm, stride, imap);
+    if (fuse_il) rows_c2r_interleave(ctx, *p, maps, (long)(slot / (2 * es)), nm, stride, imap, planar);
     else interleave(ctx, mp, nm, npix, map->prec, stride, imap);
     if (!host) {
       sample_tracks_il(ctx, imap, stride, nm, Nx, Ny, map->prec, ntr, x0, y0, phi, v, off, t, mag,
@@ -384,7 +395,7 @@ void convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* pro
   auto enqueue = [&] {
     for (int k = 0; k < nprof; k++) {
       void* o = (char*)out + (size_t)k * stride * es;
-      if (mode == MLC_CONV_FUSED) conv_fused(ctx, *p, map->spec, dprof + poff[k], pN[k], o);
+      if (mode == MLC_CONV_FUSED) conv_auto(ctx, *p, map->data, map->spec, dprof + poff[k], pN[k], o);
       else conv_plain(ctx, *p, map->spec, dprof + poff[k], pN[k], o);
     }
   };

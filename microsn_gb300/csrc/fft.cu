@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in,
 template <typename T, int L1, int L2, int L3>
 __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256)
     k_rows_c2r3_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm, T* __restrict__ out, int S,
-                   const C2<T>* __restrict__ twx) {
+                   const C2<T>* __restrict__ twx, unsigned planar) {
   constexpr int J = L2 * L3, M = L1 * J, NX = 2 * M;
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -362,7 +362,11 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256)
   C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
   const int row = blockIdx.y;
   const int k = (int)cl.block_rank(), half = blockIdx.x >> 3, q = 8 * half + k;
-  if (q < nm) {
+  if (q < nm && ((planar >> q) & 1u)) {  // the direct form's real map: copy its row
+    const T* src = reinterpret_cast<const T*>(specs + (long)q * spec_stride) + (long)row * NX;
+    T* d = reinterpret_cast<T*>(s);
+    for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = src[n];
+  } else if (q < nm) {
     c2r3_row<T, L1, L2, L3>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
   } else {
     for (int n = threadIdx.x; n < M; n += blockDim.x) s[n] = C2<T>{T(0), T(0)};
@@ -869,8 +873,8 @@ void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, con
 
 template <typename T>
 static bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
-                                void* out) {
-  using K = void (*)(const C2<T>*, long, long, int, T*, int, const C2<T>*);
+                                void* out, unsigned planar) {
+  using K = void (*)(const C2<T>*, long, long, int, T*, int, const C2<T>*, unsigned);
   K k = nullptr;
   int J = 0;
   switch (p.M) {
@@ -887,7 +891,7 @@ static bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* sp
   {
     MLC_KSCOPE(ctx, "fft_rows_c2r_interleave");
     k<<<dim3(8 * halves, p.Ny), 256, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (T*)out, S,
-                                                          (const C2<T>*)p.twx);
+                                                          (const C2<T>*)p.twx, planar);
   }
   MLC_CHECK_LAUNCH();
   return true;
@@ -898,9 +902,9 @@ bool rows_c2r_interleave_supported(const FftPlan2D& p) {
 }
 
 bool rows_c2r_interleave(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
-                         void* out) {
-  if (p.prec == MLC_F64) return c2r_interleave_impl<double>(ctx, p, specs, spec_stride, nm, S, out);
-  return c2r_interleave_impl<float>(ctx, p, specs, spec_stride, nm, S, out);
+                         void* out, unsigned planar) {
+  if (p.prec == MLC_F64) return c2r_interleave_impl<double>(ctx, p, specs, spec_stride, nm, S, out, planar);
+  return c2r_interleave_impl<float>(ctx, p, specs, spec_stride, nm, S, out, planar);
 }
 
 void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {

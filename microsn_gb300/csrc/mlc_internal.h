@@ -84,6 +84,10 @@ struct mlc_ctx {
   size_t ws_size[mlc::WS_NSLOTS] = {};
   std::map<std::tuple<int, int, int>, std::unique_ptr<mlc::FftPlan2D>> plans;
   mlc::BatchIO* batch = nullptr;
+  // launch autotuner: key -> choice (-1: FFT form; >= 0: direct tile shape), candidate timings
+  bool autotune = true;
+  std::map<std::string, int> tune;
+  std::map<std::string, std::string> tune_log;
 };
 
 struct mlc_map {
@@ -143,6 +147,19 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec);
 void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec);
 void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof_dev, int pN,
                 void* out_real);
+// Direct tiled convolution of an FP32 map (real pixels) with a profile of 2..32 pixels, tile
+// shape `variant`; and the autotuned choice for (map size, profile size): -1 for the FFT
+// form, else the fastest direct tile shape (the first call times every candidate into out).
+void conv_direct(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const double* prof, int pN, int variant,
+                 void* out);
+// spectrum: the FFT alternative is conv_fused_spectrum (the caller runs the last pass of
+// several profiles together), so out must hold a half-spectrum.
+int conv_direct_choice(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const void* Fmap, const double* prof,
+                       int pN, void* out, bool spectrum);
+// conv_fused, or the direct form where the autotuner chose it.
+void conv_auto(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const void* Fmap, const double* prof, int pN,
+               void* out);
+std::string autotune_report(mlc_ctx* ctx);
 // conv_fused up to P2: the inverse half-spectrum (Ny x Wp complex) into spec_out.
 void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
                          void* spec_out);
@@ -150,8 +167,10 @@ void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, con
 // the interleaved layout out[(y Nx + x) S + q] (S a power of two >= nm, slots >= nm zero).
 // False (nothing launched) when the row length has no register kernel.
 bool rows_c2r_interleave_supported(const FftPlan2D& p);
+// planar: bit q set = slot q holds the real convolved map (Ny x Nx, from the direct form)
+// instead of a half-spectrum.
 bool rows_c2r_interleave(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
-                         void* out);
+                         void* out, unsigned planar = 0);
 void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof_dev, int pN,
                 void* out_real);
 
