@@ -954,8 +954,9 @@ def main():
     # the host link itself: plain 1 GiB copies between pinned host memory and HBM on this machine
     # (the light curves' download bounds the e2e step)
     link = {}
-    dbuf = torch.empty(1 << 28, dtype=torch.float32, device=dev)
-    hbuf = h_out.view(-1)[: 1 << 28]
+    nl = min(1 << 28, h_out.numel())  # up to 1 GiB
+    dbuf = torch.empty(nl, dtype=torch.float32, device=dev)
+    hbuf = h_out.view(-1)[:nl]
     for name, dst, src in (("d2h_gbs", hbuf, dbuf), ("h2d_gbs", dbuf, hbuf)):
         dst.copy_(src, non_blocking=True)
         e0.record(stream)
@@ -963,7 +964,7 @@ def main():
             dst.copy_(src, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
-        link[name] = 3 * (1 << 30) / (e0.elapsed_time(e1) / 1000.0) / 1e9
+        link[name] = 3 * 4 * nl / (e0.elapsed_time(e1) / 1000.0) / 1e9
     link["download_floor_ms"] = bo / (link["d2h_gbs"] * 1e9) * 1000.0
     del h_out, dbuf
 
