@@ -395,7 +395,10 @@ __global__ void __cluster_dims__(8, 1, 1) __launch_bounds__(256)
       for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = sr[x];
     }
   }
-  cl.sync();  // no CTA leaves while the others still read its shared memory
+  // no CTA leaves while the others still read its shared memory.  Execution order is all
+  // this barrier needs (every remote load has returned before the stores that use it), so
+  // the arrive is relaxed: no release fence for this CTA's global stores.
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
 }
 
 // ---------------------------------------------------------------- column kernels
