@@ -7,8 +7,9 @@
 // d = 0..4, all nine slice pairs), so
 //     x = p.q = 2^32 X0 + 2^24 X1 + 2^16 X2 + 2^8 X3 + X4   exactly,
 // and chi2 = |P|^2 + |Q|^2 - 2^(ei+ej+1) x is formed from the per-curve norms (natural
-// units, float-float) and the exactly scaled accumulators: in FP32 (within 3.9e-6 relative)
-// where chi2 >= (|P|^2+|Q|^2)/16, in float-float arithmetic below that.  Top-k
+// units, float-float) and the exactly scaled accumulators: in FP32 summed from the largest
+// term down (within 4e-6 relative) where chi2 >= 2^-14 (|P|^2+|Q|^2), in float-float
+// arithmetic below that.  Top-k
 // candidates, pairs whose chi2 is below 1e-7 of |P|^2 + |Q|^2 (where the float-float
 // rounding could matter) and, with a matrix requested, every pair whose quantisation error
 // could exceed 1e-6 relative are recomputed in FP64 by k_pd_refine.
@@ -274,19 +275,22 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
             const float4 b = cv[ch * 8 + c];
             // 2 x 2^(ei+ej) = sum_d 2^(ei+ej+33-8d) X_d; s0 = 2^(ei+ej+33) is an exact product
             const float s0 = pa * b.z;
-            const float ab = aff.x + b.x;
             const float X0 = __uint_as_float(r0[c]), X1 = __uint_as_float(r1[c]);
             const float X2 = __uint_as_float(r2[c]), X3 = __uint_as_float(r3[c]);
-            // fast FP32 assembly (rounding below 2^-22 (|P|^2+|Q|^2); the left-out X4 term
-            // below 2^-30 of it): within 3.9e-6 of chi2 whenever chi2 >= (|P|^2+|Q|^2)/16
-            const float v = fmaf(X1, 0x1p-8f, X0);
-            const float w = fmaf(X3, 0x1p-24f, X2 * 0x1p-16f);
-            float chi2 = fmaf(-v, s0, ab) + fmaf(-w, s0, aff.y + b.y);
-            // below (|P|^2+|Q|^2)/16 the float-float form.  Measured on 10^5 x 10^5 map curves:
-            // the threshold at 1/16 instead of 1/4 took 9% off the kernel (fewer warps enter the
-            // branch); one outer test around both rare cases, or a branch-free mask form of
-            // the 8 columns (128 registers), made it slower
-            if (chi2 < 0.0625f * ab)
+            // FP32 assembly from the largest term down: ab + e = |P|^2 + |Q|^2 (high parts)
+            // exactly; s0 X0 is exact (integer < 2^24 times a power of two), so ab - s0 X0 is
+            // rounded once, relative to itself, then the X1 term, then the small rest.  Error
+            // about 3 2^-24 chi2 + 2^-32 (|P|^2+|Q|^2) (the left-out X4 term below 2^-30 of it):
+            // within 4e-6 of chi2 whenever chi2 >= 2^-14 (|P|^2+|Q|^2)
+            float e;
+            const float ab = two_sum(aff.x, b.x, e);
+            const float t1 = fmaf(-X0, s0, ab);
+            const float t2 = fmaf(-X1, s0 * 0x1p-8f, t1);
+            const float w = fmaf(X3, 0x1p-8f, X2);
+            float chi2 = t2 + fmaf(-w, s0 * 0x1p-16f, e + (aff.y + b.y));
+            // below that the float-float form: with this assembly almost no warp enters it (the
+            // earlier form, good to (|P|^2+|Q|^2)/16, sent some lane of most warps there)
+            if (chi2 < 0x1p-14f * ab)
               chi2 = chi2_assemble(aff, make_float2(b.x, b.y), X0 * s0, X1 * (s0 * 0x1p-8f), X2 * (s0 * 0x1p-16f),
                                    X3 * (s0 * 0x1p-24f), __uint_as_float(r4[c]) * (s0 * 0x1p-32f));
             // below 1e-7 (|P|^2+|Q|^2) the float-float rounding (about 2^-40 of it) could exceed
