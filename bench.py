@@ -732,6 +732,10 @@ def algorithmic_bytes(name, n, E, nprof, e=4):
         "sample_tracks": E * e + nprof * real + E * nprof * e,  # t in, one read of each map, LCs out
         "sample_tracks_il": E * e + nprof * real + E * nprof * e,
         "interleave": 2 * nprof * real,          # read nprof planar maps, write the interleaved map
+        # last inverse pass of a group's profiles with the interleave (one launch per group):
+        # read each profile's half spectrum, write its values into the interleaved map
+        "fft_rows_c2r_interleave": nprof * (spec + real),
+        "conv_direct": 2 * real,                  # read the map, write the convolved map
     }
     return table.get(name)
 
@@ -747,10 +751,13 @@ def load_traffic():
 
 # ----------------------------------------------------------------------------- CPU baseline (oracle port)
 
-def cpu_baseline(mp64, host_tracks, n, ntr_sample=20000, workers=None):
+def cpu_baseline(mp64, host_tracks, n, ntr_sample=20000, workers=None, parity=None):
     """FP64 oracle port on the host cores: scipy FFT convolution of the full map with one
     profile, and bilinear sampling + magnitudes of ntr_sample tracks on it (threads over
-    track chunks).  Scaled to light curves/s for the whole workload."""
+    track chunks).  Scaled to light curves/s for the whole workload.  With parity (the GPU's
+    batched FP64 light curves of that profile for the first tracks, and those tracks), the
+    oracle samples the same tracks on its convolved map and the largest differences are
+    reported: the full-size FP64 check."""
     import concurrent.futures as cf
 
     import numpy as np
@@ -786,7 +793,19 @@ def cpu_baseline(mp64, host_tracks, n, ntr_sample=20000, workers=None):
     t_samp = time.perf_counter() - t0
     per_profile = t_conv + t_samp * (N_TRACKS / ntr)
     value = N_TRACKS / per_profile
-    return {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+    check = None
+    if parity is not None:
+        pt = parity["tracks"]
+        ref = oracle.sample_tracks(cm, pt["x0"], pt["y0"], pt["phi"], pt["v"], pt["off"], pt["t"])
+        got = parity["lc"]
+        fin = np.isfinite(ref) & np.isfinite(got)
+        dm = np.abs(got[fin] - ref[fin])
+        check = {"samples": int(ref.size), "tracks": int(len(pt["x0"])), "finite_agree": bool(np.array_equal(
+                     np.isfinite(ref), np.isfinite(got))), "max_abs_mag": float(dm.max()),
+                 "max_rel_flux": float(np.max(np.abs(10 ** (-0.4 * (got[fin] - ref[fin])) - 1.0))),
+                 "tolerance_rel": 1e-9,
+                 "what": f"batched FP64 step on the GPU vs the FP64 oracle, full {n}^2 map, thin disc 16 px"}
+    return {"value": value, "unit": UNIT, "cores": workers, "kind": "port", "fp64_parity_full_scale": check,
             "sample": f"oracle FP64: scipy.fft convolution of the full {n}^2 map with one thin-disc profile "
                       f"({t_conv:.2f} s) + bilinear magnitudes of {ntr} tracks ({t_samp:.2f} s), scaled to "
                       f"{N_TRACKS} tracks x 16 profiles"}
@@ -970,6 +989,7 @@ def main():
 
     # ---- the plain one-launch-per-stage FP64 form of the same step
     plain = None
+    parity_in = None
     if not args.no_plain:
         m64 = mlc.Map(ctx, mp_t.double(), "f64")
         convs64 = [torch.empty((n, n), dtype=torch.float64, device=dev) for _ in range(2)]
@@ -1022,6 +1042,14 @@ def main():
             dmax = max(dmax, float((a32 - a64).abs()[ok].max()))
         plain["batched_fp64"] = {"value": world * lc_per_step / (bms / 1000.0), "unit": UNIT, "ms_per_step": bms,
                                  "batched_fp64_over_plain_fp64": pms / bms}
+        # kept for the full-scale FP64 check against the oracle in the CPU leg: the thin-disc
+        # 16 px light curves of the first tracks and those tracks' parameters
+        kpar = len(RHALF_PX) + 3
+        npar = min(20000, int(tr["off"].numel()) - 1)
+        epar = int(tr["off"][npar].item())
+        parity_in = {"lc": out64b[kpar, :epar].cpu().numpy(),
+                     "tracks": {k: tr64f[k][: (npar + 1 if k == "off" else (epar if k == "t" else npar))].cpu().numpy()
+                                for k in tr64f}}
         plain["fp32_vs_fp64"] = {"samples": int(len(profs) * E), "max_abs_mag": dmax,
                                  "max_rel_flux": 10 ** (0.4 * dmax) - 1.0,
                                  "finite_fp32": fin32, "finite_fp64": fin64,
@@ -1044,7 +1072,7 @@ def main():
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(mp_t.double().cpu().numpy(), host_tr, n)
+        cpu = cpu_baseline(mp_t.double().cpu().numpy(), host_tr, n, parity=parity_in)
 
     if rank == 0:
         res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ F
   constexpr int N2 = L1 * L2;
   extern __shared__ unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);  // [N2][CW] profile column sub-pass
-  C2<T>* y = a + N2 * CW;                         // [max(L1,L2)][max(L1,L2)][CW] transposes
+  C2<T>* y = a;                                   // the transposes reuse it ([L2][L1][CW])
   C2<T>* w1 = y + N2 * CW;                        // W_N1^(n1 kk), n1 < N1
   C2<T>* w2 = w1 + N1;                            // W_Ny^(n kk), n < N2
   C2<T>* wl = w2 + N2;                            // W_N2^m, m < N2
@@ -599,14 +599,20 @@ __global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ F
     }
   }
   __syncthreads();
-  // forward stage 1: thread (n2 = g, c)
-  if (g < L2) {
+  // forward stage 1: thread (n2 = g, c); every input is read before the shared buffer is
+  // overwritten with the transposed result
+  {
     C2<T> v[L1];
+    if (g < L2) {
 #pragma unroll
-    for (int n1 = 0; n1 < L1; n1++) v[n1] = a[(L2 * n1 + g) * CW + c];
-    Dft<T, L1, false>::run(v);
+      for (int n1 = 0; n1 < L1; n1++) v[n1] = a[(L2 * n1 + g) * CW + c];
+      Dft<T, L1, false>::run(v);
+    }
+    __syncthreads();
+    if (g < L2) {
 #pragma unroll
-    for (int k1 = 0; k1 < L1; k1++) y[(g * L1 + k1) * CW + c] = k1 == 0 ? v[0] : cmul(v[k1], wl[g * k1]);
+      for (int k1 = 0; k1 < L1; k1++) y[(g * L1 + k1) * CW + c] = k1 == 0 ? v[0] : cmul(v[k1], wl[g * k1]);
+    }
   }
   __syncthreads();
   // forward stage 2, product, inverse stage A: thread (k1 = g, c)
@@ -808,7 +814,7 @@ static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
       default: break;
     }
     if (k2) {
-      const size_t smem2 = (2 * (size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
+      const size_t smem2 = ((size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
       set_max_smem((const void*)k2, smem2);
       {
         MLC_KSCOPE(ctx, "conv_fused_spectrum");

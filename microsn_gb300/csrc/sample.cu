@@ -5,6 +5,8 @@
 #include <cmath>
 
 #include "bilinear.cuh"
+#include <algorithm>
+
 #include "mlc_internal.h"
 
 namespace mlc {
@@ -168,6 +170,65 @@ __device__ __forceinline__ void load_pix(const T* __restrict__ p, T* v) {
   }
 }
 
+// One epoch of one track on an interleaved map: bilinear weights at (bx + fx, by + fy),
+// fx = fx0 + vt cos phi, fy = fy0 + vt sin phi, then every map's value (or magnitude)
+// into out[q * E + o].
+template <typename T, int NM>
+__device__ __forceinline__ void sample_epoch(const T* __restrict__ imap, int Nx, int Ny, long bx, long by, T fx0, T fy0,
+                                             T cs, T sn, T vt, int mag, T* __restrict__ out, long E, int nm_out,
+                                             int64_t o) {
+  const T fx = fx0 + vt * cs, fy = fy0 + vt * sn;
+  const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
+  // 16 bytes of maps at a time (4 FP32 / 2 FP64): the four corners of one chunk in
+  // registers, not all NM maps of all four corners (which needed 100 registers and left
+  // 2 CTAs per SM, too few warps to hide the gather latency)
+  constexpr int CH = (NM * (int)sizeof(T) >= 16) ? 16 / (int)sizeof(T) : NM;
+  const T* pa = imap + ((long)B.iu * Nx + B.jl) * NM;
+  const T* pb = imap + ((long)B.iu * Nx + B.jr) * NM;
+  const T* pc = imap + ((long)B.il * Nx + B.jl) * NM;
+  const T* pd = imap + ((long)B.il * Nx + B.jr) * NM;
+#pragma unroll 1
+  for (int c0 = 0; c0 < NM; c0 += CH) {
+    T acc[CH];
+    if (B.inside) {
+      T a[CH], b[CH], c[CH], d[CH];
+      load_pix<T, CH>(pa + c0, a);
+      load_pix<T, CH>(pb + c0, b);
+      load_pix<T, CH>(pc + c0, c);
+      load_pix<T, CH>(pd + c0, d);
+#pragma unroll
+      for (int q = 0; q < CH; q++) {
+        T z = B.w0 * a[q];
+        z += B.w1 * b[q];
+        z += B.w2 * c[q];
+        z += B.w3 * d[q];
+        acc[q] = z;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < CH; q++) acc[q] = (T)0;
+    }
+#pragma unroll
+    for (int q = 0; q < CH; q++)
+      if (c0 + q < nm_out) out[(long)(c0 + q) * E + o] = mag ? (T)-2.5 * mlc_log10(acc[q]) : acc[q];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void sincos_t(T phi, T* sn, T* cs) {
+  if (sizeof(T) == 8) {
+    double s_, c_;
+    sincos((double)phi, &s_, &c_);
+    *sn = (T)s_;
+    *cs = (T)c_;
+  } else {
+    float s_, c_;
+    sincosf((float)phi, &s_, &c_);
+    *sn = (T)s_;
+    *cs = (T)c_;
+  }
+}
+
 // One warp per track, lanes over epochs; each epoch reads 4 corners x NM interleaved
 // values and writes nm_out light-curve values out[q*E + e].
 template <typename T, int NM>
@@ -182,58 +243,12 @@ __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ 
   if (track >= ntracks) return;
   const T X0 = x0[track], Y0 = y0[track], V = v[track];
   T sn, cs;
-  if (sizeof(T) == 8) {
-    double s_, c_;
-    sincos((double)phi[track], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  } else {
-    float s_, c_;
-    sincosf((float)phi[track], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  }
+  sincos_t<T>(phi[track], &sn, &cs);
   const long bx = (long)floor(X0), by = (long)floor(Y0);
   const T fx0 = X0 - (T)bx, fy0 = Y0 - (T)by;
   const int64_t e0 = off[track], e1 = off[track + 1];
-  for (int64_t e = e0 + lane; e < e1; e += 32) {
-    const T vt = V * t[e];
-    const T fx = fx0 + vt * cs, fy = fy0 + vt * sn;
-    const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
-    // 16 bytes of maps at a time (4 FP32 / 2 FP64): the four corners of one chunk in
-    // registers, not all NM maps of all four corners (which needed 100 registers and left
-    // 2 CTAs per SM, too few warps to hide the gather latency)
-    constexpr int CH = (NM * (int)sizeof(T) >= 16) ? 16 / (int)sizeof(T) : NM;
-    const T* pa = imap + ((long)B.iu * Nx + B.jl) * NM;
-    const T* pb = imap + ((long)B.iu * Nx + B.jr) * NM;
-    const T* pc = imap + ((long)B.il * Nx + B.jl) * NM;
-    const T* pd = imap + ((long)B.il * Nx + B.jr) * NM;
-#pragma unroll 1
-    for (int c0 = 0; c0 < NM; c0 += CH) {
-      T acc[CH];
-      if (B.inside) {
-        T a[CH], b[CH], c[CH], d[CH];
-        load_pix<T, CH>(pa + c0, a);
-        load_pix<T, CH>(pb + c0, b);
-        load_pix<T, CH>(pc + c0, c);
-        load_pix<T, CH>(pd + c0, d);
-#pragma unroll
-        for (int q = 0; q < CH; q++) {
-          T z = B.w0 * a[q];
-          z += B.w1 * b[q];
-          z += B.w2 * c[q];
-          z += B.w3 * d[q];
-          acc[q] = z;
-        }
-      } else {
-#pragma unroll
-        for (int q = 0; q < CH; q++) acc[q] = (T)0;
-      }
-#pragma unroll
-      for (int q = 0; q < CH; q++)
-        if (c0 + q < nm_out) out[(long)(c0 + q) * E + (e - ebase)] = mag ? (T)-2.5 * mlc_log10(acc[q]) : acc[q];
-    }
-  }
+  for (int64_t e = e0 + lane; e < e1; e += 32)
+    sample_epoch<T, NM>(imap, Nx, Ny, bx, by, fx0, fy0, cs, sn, V * t[e], mag, out, E, nm_out, e - ebase);
 }
 
 // FP32 with a contiguous output (width == S, off == 0, W in {4, 8, 16}), npix % 4 == 0 and
