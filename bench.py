@@ -199,7 +199,7 @@ def bf16_peak():
 PAIR_N, PAIR_T, PAIR_BINS, PAIR_K = 100_000, 128, 1000, 10_000
 
 
-# configs[0], the small plain-FP64 end-to-end case: 2000^2 ray-shot map (kappa* = 0.4,
+# The small FP64 end-to-end case: 2000^2 ray-shot map (kappa* = 0.4,
 # gamma = 0.4, width 20, seed 0) convolved with a Gaussian of sigma 10 px, 10^4 straight
 # tracks of 50 epochs at 5 px per epoch, offset chi2 against one noisy observed curve,
 # sort and a 100-bin histogram.
@@ -284,14 +284,14 @@ def c1_workload(args, ctx, dev, rank):
         cpu = {"kind": "port", "cores": os.cpu_count(), "ms_per_step": dt_ * 1000.0,
                "light_curves_per_s": C1_TRACKS / dt_}
     m.close()
-    return {"workload": "configs[0]: 2000^2 FP64 ray-shot map, Gaussian sigma 10 px, 10^4 tracks x 50 epochs, "
+    return {"workload": "small FP64 end to end: 2000^2 FP64 ray-shot map, Gaussian sigma 10 px, 10^4 tracks x 50 epochs, "
                         "offset chi2 vs one noisy curve, radix sort, 100-bin log10 chi2 histogram",
             "fused": out["fused"], "plain_fp64": out["plain"],
             "fused_over_plain": out["plain"]["ms_per_step"] / out["fused"]["ms_per_step"], "cpu": cpu,
             "dtype": "f64"}
 
 
-# configs[3], the differentiable fit: 4000^2 FP32 map, thin-disc radius stack (16 radii,
+# The differentiable fit: 4000^2 FP32 map, thin-disc radius stack (16 radii,
 # 4..32 px), 4096 tracks = 64 targets x 64 perturbed starts, 80 uneven epochs each, fused
 # chi2 + gradient kernel with an Adam step, replayed from a CUDA graph.
 C4_N, C4_TARGETS, C4_STARTS, C4_T = 4000, 64, 64, 80
@@ -389,7 +389,7 @@ def c4_workload(args, ctx, dev, rank):
     true_c2 = c2[:C4_TARGETS].cpu().numpy()
     recovered = float(np.mean(final.min(axis=1) <= 1.2 * true_c2 + 5.0))
     m.close()
-    return {"workload": "configs[3]: 4000^2 FP32 map, 16-radius thin-disc stack, 4096 tracks (64 targets x 64 "
+    return {"workload": "gradient fit: 4000^2 FP32 map, 16-radius thin-disc stack, 4096 tracks (64 targets x 64 "
                         "starts) x 80 uneven epochs, 6 parameters, Adam from a CUDA graph",
             "stack_build_ms": stack_ms, "iteration_ms": ms / iters,
             "gradient_evaluations_per_s": n / (ms / iters / 1000.0),
@@ -398,7 +398,7 @@ def c4_workload(args, ctx, dev, rank):
             "median_best_over_true_chi2": float(np.median(final.min(axis=1) / true_c2))}
 
 
-# configs[4], supernova multi-band multi-image: four 8192^2 FP32 maps (one per lensed
+# Supernova, multi-band and multi-image: four 8192^2 FP32 maps (one per lensed
 # image, seeds 6..9, distinct kappa* and gamma), an expanding photosphere R(t) from 1 to
 # 100 px over 40 epochs in 3 bands (limb-darkened discs, one limb-darkening coefficient
 # per band) = 120 convolutions per map, 2x10^5 tracks per image sampled at the epochs,
@@ -484,7 +484,7 @@ def c5_workload(args, ctx, dev, rank):
     conv_graph = e[0].elapsed_time(e[1])
     npairs = len(pairs) * float(ntr) * ntr
     total = t_curves + t_pairs
-    out = {"workload": f"configs[4]: {len(maps)} x {N}^2 FP32 maps, {len(profs)} limb-darkened expanding-photosphere "
+    out = {"workload": f"supernova: {len(maps)} x {N}^2 FP32 maps, {len(profs)} limb-darkened expanding-photosphere "
                        f"profiles per map ({C5_EPOCHS} epochs x {nb} bands), {ntr} tracks per image, offset "
                        f"magnitude-difference chi2 of all track pairs of {len(pairs)} image pairs (T = {T})",
            "ms_per_step": total, "curves_ms": t_curves, "pairs_ms": t_pairs,
@@ -583,6 +583,38 @@ def ratio_pair_workload(args, ctx, m, dev, rank):
             "reference_form": {"ms_per_evaluation": ref_ms, "value": pairs / (ref_ms / 1000.0)},
             "fused": {"ms_per_evaluation": fused_ms, "value": pairs / (fused_ms / 1000.0)},
             "fused_equals_reference_form": agree, "cpu": cpu}
+
+
+def mpd_workload(args, ctx, m, rank):
+    """The map's binned magnification distribution (getBinnedMpd, magnification_map_gpu.cu:45-87)
+    of the bench map in FP64 with the reference input's bins (500 log bins, 1e-4..400): one
+    pass with shared-memory counters on the GPU, against the oracle's C restatement of the
+    reference's sort-and-upper_bound form on one host core, bins compared bit for bit."""
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    import oracle
+    m64 = mlc.Map(ctx, m.tensor().double(), "f64")
+    nb, lo, hi = 500, 1e-4, 400.0
+    mlc.map_binned_mpd(ctx, m64, nb, lo, hi)
+    torch.cuda.synchronize()
+    k = 5
+    t0 = time.perf_counter()
+    for _ in range(k):
+        bins, counts = mlc.map_binned_mpd(ctx, m64, nb, lo, hi)  # returns host arrays (synchronous)
+    gpu_ms = (time.perf_counter() - t0) * 1000.0 / k
+    res = {"workload": f"{m.Nx}^2 FP64 map, {nb} log bins {lo}..{hi}", "gpu_ms": gpu_ms,
+           "pixels_per_s": m.Nx * m.Ny / (gpu_ms / 1000.0)}
+    if rank == 0 and not args.no_cpu:
+        host = m64.tensor().cpu().numpy()
+        t0 = time.perf_counter()
+        b_o, c_o = oracle.binned_mpd(host, nb, lo, hi)
+        res["cpu"] = {"kind": "port", "cores": 1, "ms": (time.perf_counter() - t0) * 1000.0,
+                      "sample": "the whole map"}
+        res["bins_equal"] = bool(np.array_equal(bins, b_o) and np.array_equal(counts, c_o))
+    del m64
+    return res
 
 
 def flux_ratio_workload(args, ctx, dev, rank):
@@ -1069,9 +1101,10 @@ def main():
     pair = None
     if not args.no_pair:
         pair = pair_workload(args, ctx, m, profs, n, dev, world, rank, stream)
-    flux = c1 = c4 = c5 = ratio = None
+    flux = c1 = c4 = c5 = ratio = mpd = None
     if not args.no_pair:
         ratio = ratio_pair_workload(args, ctx, m, dev, rank)
+        mpd = mpd_workload(args, ctx, m, rank)
         flux = flux_ratio_workload(args, ctx, dev, rank)
         c1 = c1_workload(args, ctx, dev, rank)
         c4 = c4_workload(args, ctx, dev, rank)
@@ -1096,6 +1129,7 @@ def main():
                                    "unit": UNIT, "ms_per_step": kernels["sample_tracks_il"]["ms_per_step"]}
                                   if "sample_tracks_il" in kernels else None),
                "ratio_pairs": ratio,
+               "map_mpd": mpd,
                "autotune": {k: {"choice": c, "ms": m} for k, (c, m) in ctx.autotune_report().items()},
                "light_curves_per_step": lc_per_step, "epochs_per_step": E, "pair_chi2": pair,
                "flux_ratio": flux, "c1_small_fp64": c1, "c4_fit": c4,
