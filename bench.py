@@ -251,10 +251,23 @@ def c1_workload(args, ctx, dev, rank):
         mlc.sort_f64_u32(ctx, c2, idx)
         return mlc.histogram_f64(ctx, c2, 100, 0.0, 7.0, log=True)
 
+    def ff_step():
+        # the fused step with the map's transforms in float-float arithmetic (FP64 results)
+        m.set_fft("f32x2")
+        try:
+            return step("fused")
+        finally:
+            m.set_fft("native")
+
     out = {}
-    for name, fn in (("fused", lambda: step("fused")), ("plain", plain_step)):
+    chi_ref = None
+    for name, fn in (("fused", lambda: step("fused")), ("fused_f32x2", ff_step), ("plain", plain_step)):
         for _ in range(max(args.warmup, 1)):
             h = fn()
+        if name == "fused":
+            chi_ref = chi2.clone()
+        elif name == "fused_f32x2":
+            out["f32x2_vs_native_max_rel_chi2"] = float(((chi2 - chi_ref).abs() / chi_ref.abs()).max())
         torch.cuda.synchronize()
         steps = max(1, min(args.steps, 10))
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
@@ -286,9 +299,12 @@ def c1_workload(args, ctx, dev, rank):
     m.close()
     return {"workload": "small FP64 end to end: 2000^2 FP64 ray-shot map, Gaussian sigma 10 px, 10^4 tracks x 50 epochs, "
                         "offset chi2 vs one noisy curve, radix sort, 100-bin log10 chi2 histogram",
-            "fused": out["fused"], "plain_fp64": out["plain"],
-            "fused_over_plain": out["plain"]["ms_per_step"] / out["fused"]["ms_per_step"], "cpu": cpu,
-            "dtype": "f64"}
+            "fused": out["fused"], "fused_f32x2": out["fused_f32x2"], "plain_fp64": out["plain"],
+            "fused_over_plain": out["plain"]["ms_per_step"] / out["fused"]["ms_per_step"],
+            "fused_f32x2_over_plain": out["plain"]["ms_per_step"] / out["fused_f32x2"]["ms_per_step"],
+            "f32x2_vs_native_max_rel_chi2": out["f32x2_vs_native_max_rel_chi2"], "cpu": cpu, "dtype": "f64",
+            "f32x2": "FP64 map whose forward transform and fused convolution run in float-float arithmetic "
+                     "(pairs of FP32); pixels, light curves and chi2 FP64"}
 
 
 # The differentiable fit: 4000^2 FP32 map, thin-disc radius stack (16 radii,
@@ -1074,6 +1090,27 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         bms = e0.elapsed_time(e1) / 3
+        # the same FP64 step with float-float transforms
+        m64.set_fft("f32x2")
+        out64f = torch.empty_like(out64b)
+
+        def step64f():
+            mlc.convolve_sample_tracks(ctx, m64, profs, tr64f, mag=True, pixels=pix64, out=out64f)
+
+        step64f()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(3):
+            step64f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fms = e0.elapsed_time(e1) / 3
+        fdev = 0.0
+        for q in range(len(profs)):
+            ok = torch.isfinite(out64b[q]) & torch.isfinite(out64f[q])
+            fdev = max(fdev, float((out64f[q] - out64b[q]).abs()[ok].max()))
+        m64.set_fft("native")
+        del out64f
         step()  # the FP32 light curves of the same inputs
         dmax, fin32, fin64 = 0.0, 0, 0
         for q in range(len(profs)):
@@ -1083,6 +1120,10 @@ def main():
             dmax = max(dmax, float((a32 - a64).abs()[ok].max()))
         plain["batched_fp64"] = {"value": world * lc_per_step / (bms / 1000.0), "unit": UNIT, "ms_per_step": bms,
                                  "batched_fp64_over_plain_fp64": pms / bms}
+        plain["batched_fp64_f32x2"] = {"value": world * lc_per_step / (fms / 1000.0), "unit": UNIT,
+                                       "ms_per_step": fms, "over_plain_fp64": pms / fms,
+                                       "max_abs_mag_vs_native_fp64": fdev,
+                                       "what": "the batched FP64 step with float-float transforms"}
         # kept for the full-scale FP64 check against the oracle in the CPU leg: the thin-disc
         # 16 px light curves of the first tracks and those tracks' parameters
         kpar = len(RHALF_PX) + 3

@@ -137,6 +137,17 @@ int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map);
  * rewritten through mlc_map_data). */
 int mlc_map_refresh(mlc_ctx* ctx, mlc_map* map);
 
+/* Arithmetic of an FP64 map's Fourier transforms (no reference counterpart).  GB300 runs
+ * FP64 at a small fraction of its FP32 rate; with MLC_FFT_F32X2 the map's forward
+ * transform and its fused convolutions run in float-float arithmetic (pairs of FP32
+ * values, about 48 significant bits: convolved maps within about 1e-13 relative of FP64
+ * transforms) while pixels, convolved maps, light curves and everything after them stay
+ * FP64.  The plain form (MLC_CONV_PLAIN) keeps native FP64 and refuses such a map.
+ * Changing the mode drops the cached spectrum.  FP32 maps accept MLC_FFT_NATIVE only. */
+#define MLC_FFT_NATIVE 0
+#define MLC_FFT_F32X2 1
+int mlc_map_set_fft(mlc_map* map, int mode);
+
 /* ======================================================================= convolution */
 
 /* Convolve the map with one profile into out (Ny x Nx, the map's precision), the

@@ -65,6 +65,7 @@ SIGNATURES = {
     "mlc_ctx_autotune_report": (i32, [vp, C.c_char_p, i32]),
     "mlc_ctx_kernel_times": (i32, [vp, C.c_char_p, i32, vp, vp, i32, i32]),
     "mlc_map_refresh": (i32, [vp, vp]),
+    "mlc_map_set_fft": (i32, [vp, i32]),
     "mlc_profile_dims": (i32, [C.POINTER(MlcProfile), P_i32]),
     "mlc_profile_raster": (i32, [C.POINTER(MlcProfile), vp, C.c_long, P_i32]),
     "mlc_map_create": (i32, [vp, vp, i32, i32, i32, i32, i32, C.POINTER(vp)]),

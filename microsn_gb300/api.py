@@ -189,6 +189,10 @@ class Map:
     def prepare(self):
         self.ctx.check(self.ctx.L.mlc_map_prepare(self.ctx.h, self.h))
 
+    def set_fft(self, mode: str):
+        """Transforms of an FP64 map in "native" FP64 or "f32x2" (float-float) arithmetic."""
+        self.ctx.check(self.ctx.L.mlc_map_set_fft(self.h, {"native": 0, "f32x2": 1}[mode]))
+
     def refresh(self):
         """Recompute the spectrum from the current pixels."""
         self.ctx.check(self.ctx.L.mlc_map_refresh(self.ctx.h, self.h))

@@ -296,7 +296,7 @@ int mlc_map_data(mlc_map* map, void** dev_ptr) {
 extern "C++" {
 void mlc::map_prepare(mlc_ctx* ctx, mlc_map* map) {
   if (map->spec_valid) return;
-  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
+  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map_fft_prec(map));
   if (!map->spec) MLC_CUDA(cudaMalloc(&map->spec, p->spec_bytes()));
   fft2_forward(ctx, *p, map->data, map->prec, map->spec);
   map->spec_valid = true;
@@ -306,6 +306,18 @@ void mlc::map_prepare(mlc_ctx* ctx, mlc_map* map) {
 int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map) {
   if (!map) return fail(ctx, MLC_ERR_ARG, "null map");
   return guarded(ctx, [&] { map_prepare(ctx, map); });
+}
+
+int mlc_map_set_fft(mlc_map* map, int mode) {
+  if (!map) return MLC_ERR_ARG;
+  if (mode != MLC_FFT_NATIVE && mode != MLC_FFT_F32X2) return fail(map->ctx, MLC_ERR_ARG, "unknown FFT mode");
+  if (mode == MLC_FFT_F32X2 && map->prec != MLC_F64)
+    return fail(map->ctx, MLC_ERR_ARG, "float-float transforms are for FP64 maps");
+  if (map->fft != mode) {
+    map->fft = mode;
+    map->spec_valid = false;  // the spectrum's element type changes (same size)
+  }
+  return MLC_OK;
 }
 
 int mlc_map_refresh(mlc_ctx* ctx, mlc_map* map) {
@@ -332,7 +344,7 @@ static const double* upload_profile(mlc_ctx* ctx, const mlc_profile& pr, int* pN
 static void convolve_impl(mlc_ctx* ctx, mlc_map* map, const mlc_profile& pr, int mode, void* out) {
   MLC_REQUIRE(mode == MLC_CONV_FUSED || mode == MLC_CONV_PLAIN, MLC_ERR_ARG, "unknown convolution mode");
   map_prepare(ctx, map);
-  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
+  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map_fft_prec(map));
   int N = 0;
   const double* prof = upload_profile(ctx, pr, &N);
   if (mode == MLC_CONV_FUSED) conv_auto(ctx, *p, map->data, map->spec, prof, N, out);

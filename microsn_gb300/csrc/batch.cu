@@ -216,7 +216,7 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
   const size_t es = sizeof(T);
   const int Nx = map->Nx, Ny = map->Ny;
   const long npix = (long)Nx * Ny;
-  FftPlan2D* p = plan_get(ctx, Nx, Ny, map->prec);
+  FftPlan2D* p = plan_get(ctx, Nx, Ny, map_fft_prec(map));
   BatchIO* b = batch_get(ctx);
   const int par = b->parity;
   b->parity ^= 1;
@@ -386,7 +386,7 @@ void convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* pro
   BatchIO* b = batch_get(ctx);
   const int par = b->parity;
   b->parity ^= 1;
-  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
+  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map_fft_prec(map));
   map_prepare(ctx, map);
   std::vector<int> pN;
   std::vector<size_t> poff;

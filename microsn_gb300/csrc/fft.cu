@@ -160,8 +160,8 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
   p->M = Nx / 2;
   p->Wc = Nx / 2 + 1;
   p->Wp = (int)round_up(p->Wc, 16);
-  p->elem = prec == MLC_F64 ? sizeof(C2<double>) : sizeof(C2<float>);
-  p->CW = prec == MLC_F64 ? 8 : 16;
+  p->elem = prec == MLC_F64 ? sizeof(C2<double>) : prec == PREC_FF ? sizeof(C2<ff>) : sizeof(C2<float>);
+  p->CW = prec == MLC_F32 ? 16 : 8;
   split_columns(Ny, p->N1, p->N2);
   p->rlM = factor_radices(p->M, 2);
   p->rlN1 = factor_radices(p->N1, p->N2);
@@ -175,6 +175,9 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
   if (prec == MLC_F64) {
     p->twx = upload_twiddles<double>(Nx);
     p->twy = upload_twiddles<double>(Ny);
+  } else if (prec == PREC_FF) {
+    p->twx = upload_twiddles<ff>(Nx);
+    p->twy = upload_twiddles<ff>(Ny);
   } else {
     p->twx = upload_twiddles<float>(Nx);
     p->twy = upload_twiddles<float>(Ny);
@@ -240,8 +243,9 @@ __global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__
 
 // Inverse real FFT (unnormalised, like cuFFT Z2D) of one spectrum row per CTA.
 template <typename T>
-__global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, long pitch, T* __restrict__ out,
-                                                  long ldo, int M, RadixList rl, const C2<T>* __restrict__ twx) {
+__global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, long pitch,
+                                                  typename RealOut<T>::type* __restrict__ out, long ldo, int M,
+                                                  RadixList rl, const C2<T>* __restrict__ twx) {
   extern __shared__ unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + (M + 1);
@@ -258,8 +262,9 @@ __global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, 
   }
   __syncthreads();
   C2<T>* z = fft_smem<T, true, 1>(b, a, rl, twx);
-  C2<T>* dst = reinterpret_cast<C2<T>*>(out + (long)row * ldo);
-  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = z[n];
+  using TO = typename RealOut<T>::type;
+  C2<TO>* dst = reinterpret_cast<C2<TO>*>(out + (long)row * ldo);
+  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{RealOut<T>::cvt(z[n].x), RealOut<T>::cvt(z[n].y)};
 }
 
 // Inverse real FFT of one spectrum row per CTA with M = L1 L2 L3 (J = L2 L3) in three
@@ -333,15 +338,17 @@ __device__ __forceinline__ void c2r3_row(const C2<T>* __restrict__ a, const C2<T
 }
 
 template <typename T, int L1, int L2, int L3>
-__global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in, long pitch, T* __restrict__ out,
-                                                   long ldo, const C2<T>* __restrict__ twx) {
+__global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in, long pitch,
+                                                   typename RealOut<T>::type* __restrict__ out, long ldo,
+                                                   const C2<T>* __restrict__ twx) {
   constexpr int M = L1 * L2 * L3;
   extern __shared__ unsigned char smem_raw[];
   C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
   const int row = blockIdx.x;
   c2r3_row<T, L1, L2, L3>(in + (long)row * pitch, twx, s);
-  C2<T>* dst = reinterpret_cast<C2<T>*>(out + (long)row * ldo);
-  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = s[n];
+  using TO = typename RealOut<T>::type;
+  C2<TO>* dst = reinterpret_cast<C2<TO>*>(out + (long)row * ldo);
+  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{RealOut<T>::cvt(s[n].x), RealOut<T>::cvt(s[n].y)};
 }
 
 // P3 of four profiles with the interleave fused in.  A cluster of four CTAs takes one row
@@ -356,8 +363,9 @@ __global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in,
 // of 2 or 1 (8- or 4-byte strided stores) 9.8 ms.)
 template <typename T, int L1, int L2, int L3>
 __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
-    k_rows_c2r3_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm, T* __restrict__ out, int S,
-                   const C2<T>* __restrict__ twx, unsigned planar) {
+    k_rows_c2r3_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm,
+                   typename RealOut<T>::type* __restrict__ out, int S, const C2<T>* __restrict__ twx, unsigned planar) {
+  using TO = typename RealOut<T>::type;
   constexpr int J = L2 * L3, M = L1 * J, NX = 2 * M;
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -366,9 +374,9 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
   const int row = blockIdx.y;
   const int k = (int)cl.block_rank(), quad = blockIdx.x >> 2, q = 4 * quad + k;
   if (q < nm && ((planar >> q) & 1u)) {  // the direct form's real map: copy its row
-    const T* src = reinterpret_cast<const T*>(specs + (long)q * spec_stride) + (long)row * NX;
+    const TO* src = reinterpret_cast<const TO*>(specs + (long)q * spec_stride) + (long)row * NX;
     T* d = reinterpret_cast<T*>(s);
-    for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = src[n];
+    for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = T(src[n]);
   } else if (q < nm) {
     c2r3_row<T, L1, L2, L3>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
   } else {
@@ -378,24 +386,24 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
   const int W = S - 4 * quad < 4 ? S - 4 * quad : 4;  // values per pixel from this cluster
   constexpr int CH = (NX + 3) / 4;
   const int x0 = k * CH, x1 = x0 + CH < NX ? x0 + CH : NX;
-  T* dst = out + (long)row * NX * S + 4 * quad;
+  TO* dst = out + (long)row * NX * S + 4 * quad;
   if (W == 4) {
     const T* src[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) src[r] = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
     for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
-      T v[4];
+      TO v[4];
 #pragma unroll
-      for (int r = 0; r < 4; r++) v[r] = src[r][x];
+      for (int r = 0; r < 4; r++) v[r] = RealOut<T>::cvt(src[r][x]);
       float4* d = reinterpret_cast<float4*>(dst + (long)x * S);
       const float4* w = reinterpret_cast<const float4*>(v);
 #pragma unroll
-      for (int i = 0; i < (int)(4 * sizeof(T) / 16); i++) d[i] = w[i];
+      for (int i = 0; i < (int)(4 * sizeof(TO) / 16); i++) d[i] = w[i];
     }
   } else {
     for (int r = 0; r < W; r++) {
       const T* sr = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
-      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = sr[x];
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = RealOut<T>::cvt(sr[x]);
     }
   }
   // no CTA leaves while the others still read its shared memory.  Execution order is all
@@ -693,7 +701,8 @@ static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, 
 template <typename T>
 static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, void* out) {
   {
-    using K3 = void (*)(const C2<T>*, long, T*, long, const C2<T>*);
+    using TO = typename RealOut<T>::type;
+    using K3 = void (*)(const C2<T>*, long, TO*, long, const C2<T>*);
     K3 k3 = nullptr;
     int J = 0;
     switch (p.M) {
@@ -708,7 +717,7 @@ static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, vo
       set_max_smem((const void*)k3, smem3);
       {
         MLC_KSCOPE(ctx, "fft_rows_c2r");
-        k3<<<p.Ny, 256, smem3, ctx->stream>>>((const C2<T>*)in, p.Wp, (T*)out, p.Nx, (const C2<T>*)p.twx);
+        k3<<<p.Ny, 256, smem3, ctx->stream>>>((const C2<T>*)in, p.Wp, (TO*)out, p.Nx, (const C2<T>*)p.twx);
       }
       MLC_CHECK_LAUNCH();
       return;
@@ -719,7 +728,7 @@ static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, vo
   set_max_smem((const void*)kern, smem);
   {
     MLC_KSCOPE(ctx, "fft_rows_c2r");
-    kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (T*)out, p.Nx, p.M, p.rlM,
+    kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (typename RealOut<T>::type*)out, p.Nx, p.M, p.rlM,
                                          (const C2<T>*)p.twx);
   }
   MLC_CHECK_LAUNCH();
@@ -784,7 +793,8 @@ static void forward_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int i
 }
 
 void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec) {
-  if (p.prec == MLC_F64) forward_impl<double>(ctx, p, in, in_dtype, spec);
+  if (p.prec == PREC_FF) forward_impl<ff>(ctx, p, in, in_dtype, spec);
+  else if (p.prec == MLC_F64) forward_impl<double>(ctx, p, in, in_dtype, spec);
   else forward_impl<float>(ctx, p, in, in_dtype, spec);
 }
 
@@ -873,20 +883,23 @@ static void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, 
 }
 
 void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
-  if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, out);
+  if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, out);
+  else if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, out);
   else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, out);
 }
 
 void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
                          void* spec_out) {
-  if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
+  if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
+  else if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
   else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
 }
 
 template <typename T>
 static bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
                                 void* out, unsigned planar) {
-  using K = void (*)(const C2<T>*, long, long, int, T*, int, const C2<T>*, unsigned);
+  using TO = typename RealOut<T>::type;
+  using K = void (*)(const C2<T>*, long, long, int, TO*, int, const C2<T>*, unsigned);
   K k = nullptr;
   int J = 0;
   switch (p.M) {
@@ -902,7 +915,7 @@ static bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* sp
   const int quads = (nm + 3) / 4;
   {
     MLC_KSCOPE(ctx, "fft_rows_c2r_interleave");
-    k<<<dim3(4 * quads, p.Ny), 256, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (T*)out, S,
+    k<<<dim3(4 * quads, p.Ny), 256, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (TO*)out, S,
                                                           (const C2<T>*)p.twx, planar);
   }
   MLC_CHECK_LAUNCH();
@@ -915,11 +928,13 @@ bool rows_c2r_interleave_supported(const FftPlan2D& p) {
 
 bool rows_c2r_interleave(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
                          void* out, unsigned planar) {
+  if (p.prec == PREC_FF) return c2r_interleave_impl<ff>(ctx, p, specs, spec_stride, nm, S, out, planar);
   if (p.prec == MLC_F64) return c2r_interleave_impl<double>(ctx, p, specs, spec_stride, nm, S, out, planar);
   return c2r_interleave_impl<float>(ctx, p, specs, spec_stride, nm, S, out, planar);
 }
 
 void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
+  MLC_REQUIRE(p.prec != PREC_FF, MLC_ERR_ARG, "the plain form runs native FP64 transforms (map in float-float mode)");
   if (p.prec == MLC_F64) conv_plain_impl<double>(ctx, p, Fmap, prof, pN, out);
   else conv_plain_impl<float>(ctx, p, Fmap, prof, pN, out);
 }

@@ -233,7 +233,7 @@ void radius_stack(mlc_ctx* ctx, mlc_map* map, int K, const double* radii, double
   MLC_REQUIRE(N >= 2 && N % 2 == 0 && N <= map->Nx && N <= map->Ny, MLC_ERR_ARG,
               "raster side must be even and at most the map side");
   map_prepare(ctx, map);
-  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map->prec);
+  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map_fft_prec(map));
   const size_t n2 = (size_t)N * N;
   std::vector<double> h(4 * n2 * K);  // per radius: P, dP/dx, dP/dy, dP/dR
   for (int k = 0; k < K; k++) {

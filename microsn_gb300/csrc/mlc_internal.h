@@ -30,6 +30,9 @@ struct FftPlan2D {
   ~FftPlan2D();
 };
 
+// Internal plan precision: FFTs of FP64 maps in float-float arithmetic (mlc_map_set_fft).
+constexpr int PREC_FF = 2;
+
 enum WsSlot {
   WS_SPEC_TMP = 0,
   WS_KX,
@@ -97,7 +100,13 @@ struct mlc_map {
   void* data = nullptr;  // Ny x Nx real
   void* spec = nullptr;  // forward spectrum, digit-transposed row order
   bool spec_valid = false;
+  int fft = 0;  // FP64 maps: 0 native FP64 transforms, 1 float-float (MLC_FFT_F32X2)
 };
+
+namespace mlc {
+// Precision of a map's transforms: PREC_FF for FP64 maps with float-float FFTs.
+inline int map_fft_prec(const mlc_map* m) { return (m->prec == MLC_F64 && m->fft == 1) ? PREC_FF : m->prec; }
+}  // namespace mlc
 
 namespace mlc {
 
