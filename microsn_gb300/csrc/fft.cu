@@ -802,12 +802,12 @@ void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype
 // running P3 into out.
 template <typename T>
 static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
-                            void* out, void* spec_out = nullptr) {
+                            void* out, void* spec_out = nullptr, int kx_slot = WS_KX) {
   constexpr int CW = sizeof(T) == 8 ? 8 : 16;
   const int h = pN / 2;
   MLC_REQUIRE(pN % 2 == 0 && 2 * h <= p.Ny && 2 * h <= p.Nx, MLC_ERR_LIMIT,
               "profile raster larger than the map");
-  void* kx = ws_get(ctx, WS_KX, (size_t)(2 * h > 0 ? 2 * h : 1) * p.Wp * sizeof(C2<T>));
+  void* kx = ws_get(ctx, kx_slot, (size_t)(2 * h > 0 ? 2 * h : 1) * p.Wp * sizeof(C2<T>));
   void* tmp = spec_out ? spec_out : ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
   launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
   const int nstrips = ceil_div(p.Wc, CW);
@@ -889,10 +889,10 @@ void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double
 }
 
 void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
-                         void* spec_out) {
-  if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
-  else if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
-  else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, nullptr, spec_out);
+                         void* spec_out, int kx_slot) {
+  if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
+  else if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
+  else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
 }
 
 template <typename T>

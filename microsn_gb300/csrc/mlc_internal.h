@@ -36,6 +36,7 @@ constexpr int PREC_FF = 2;
 enum WsSlot {
   WS_SPEC_TMP = 0,
   WS_KX,
+  WS_KX2,         // the profile-row spectra of a second concurrent convolution chain
   WS_PROFILE,
   WS_KREAL,
   WS_KSPEC,
@@ -171,7 +172,7 @@ void conv_auto(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const void* Fm
 std::string autotune_report(mlc_ctx* ctx);
 // conv_fused up to P2: the inverse half-spectrum (Ny x Wp complex) into spec_out.
 void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
-                         void* spec_out);
+                         void* spec_out, int kx_slot = WS_KX);
 // P3 of nm (<= 16) such spectra (spec_stride complex elements apart) written straight into
 // the interleaved layout out[(y Nx + x) S + q] (S a power of two >= nm, slots >= nm zero).
 // False (nothing launched) when the row length has no register kernel.
