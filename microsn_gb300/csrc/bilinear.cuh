@@ -6,7 +6,7 @@
 
 namespace mlc {
 
-__device__ __forceinline__ double mlc_log10(double x) { return log10(x); }
+__device__ __forceinline__ double mlc_log10(double x) { return log10_f32x2(x); }
 __device__ __forceinline__ float mlc_log10(float x) { return log10f(x); }
 
 // Bilinear weights of RectGrid::interp2d_bilinear (rectGrid.cpp:349-378) on pixel

@@ -79,6 +79,56 @@ __device__ __forceinline__ ff operator*(ff a, ff b) {
 __device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
 __device__ __forceinline__ double ff_to_double(ff a) { return __dadd_rn((double)a.hi, (double)a.lo); }
 
+// a / b to float-float accuracy: the FP32 quotient, then one correction from the
+// float-float residual.
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const ff r = a - ff(q1, 0.f) * b;
+  return ff_renorm(q1, __fdiv_rn(r.hi, b.hi));
+}
+
+// log10 of an FP64 value in float-float arithmetic (our own evaluation, from the series
+// log m = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...), s = (m - 1)/(m + 1)): x = 2^e m with m
+// in [sqrt(1/2), sqrt(2)), so |s| <= 0.172 and eleven terms reach 2^-48; m is split into
+// its high 24 and low 29 significand bits with integer operations; log10 x =
+// (e ln 2 + log m) / ln 10.  About 1e-14 relative (FP64 magnitudes within 1e-13), at a
+// few FP64 operations where the FP64 library call needs a few dozen (GB300 runs FP64 at a
+// small fraction of its FP32 rate).  Zero, negative, subnormal, infinite and NaN inputs
+// take the library's log10.
+__device__ __forceinline__ double log10_f32x2(double x) {
+  if (!(x >= 2.2250738585072014e-308) || !(x <= 1.7976931348623157e308)) return log10(x);
+  unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+  int e = (int)(bits >> 52) - 1023;
+  unsigned long long mb = (bits & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull;  // m in [1, 2)
+  if (mb > 0x3FF6A09E667F3BCDull) {                                               // m > sqrt(2): m / 2
+    mb -= 0x0010000000000000ull;
+    e += 1;
+  }
+  const int em = (int)(mb >> 52) - 1023;  // -1 or 0
+  const unsigned long long mant = mb & 0x000FFFFFFFFFFFFFull;
+  const float mh = __int_as_float(((em + 127) << 23) | (int)(mant >> 29));           // top 24 bits, exact
+  const float ml = (float)(unsigned)(mant & 0x1FFFFFFFull) * (em ? 0x1p-53f : 0x1p-52f);  // the rest
+  const ff m(mh, ml);
+  const ff one(1.0f, 0.0f);
+  const ff s = ff_div(m - one, m + one);
+  const ff z = s * s;
+  ff p(1.0 / 23.0);
+  p = ff(1.0 / 21.0) + z * p;
+  p = ff(1.0 / 19.0) + z * p;
+  p = ff(1.0 / 17.0) + z * p;
+  p = ff(1.0 / 15.0) + z * p;
+  p = ff(1.0 / 13.0) + z * p;
+  p = ff(1.0 / 11.0) + z * p;
+  p = ff(1.0 / 9.0) + z * p;
+  p = ff(1.0 / 7.0) + z * p;
+  p = ff(1.0 / 5.0) + z * p;
+  p = ff(1.0 / 3.0) + z * p;
+  const ff logm = (s + s * (z * p)) * ff(2.0f, 0.0f);
+  const ff ln = ff((float)e, 0.0f) * ff(0.69314718055994530942) + logm;
+  const ff r = ln * ff(0.43429448190325182765);
+  return __dadd_rn((double)r.hi, (double)r.lo);
+}
+
 // The element type a real transform writes: FP32 and FP64 transforms their own, float-float
 // transforms FP64.
 template <typename T>
