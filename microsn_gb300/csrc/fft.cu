@@ -20,8 +20,9 @@
 //     P3  inverse real FFT of each row (c2r)
 //   plain convolution (MLC_CONV_PLAIN): full-size wrapped kernel, full forward,
 //     pointwise multiply, full inverse -- one launch per stage, like the reference.
-#include <cooperative_groups.h>
-
+//
+// This file holds the plans, the twiddle tables and the dispatch by precision; the
+// kernels and launch sequences are in fft_impl.cuh.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -187,699 +188,12 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
   return raw;
 }
 
-// ---------------------------------------------------------------- row loaders
-
-template <typename T, typename Tin>
-struct RealRows {
-  const Tin* p;
-  long ld;
-  __device__ __forceinline__ C2<T> pair(int row, int n) const {
-    const Tin* r = p + (long)row * ld + 2 * n;
-    return C2<T>{(T)r[0], (T)r[1]};
-  }
-};
-
-// Row j of the compacted wrapped profile: j < h is kernel row j (profile row h + j);
-// j >= h is kernel row Ny - 2h + j (profile row j - h).  Columns follow
-// Kernel::setKernel (magnification_map.cpp:186-193).
-template <typename T>
-struct ProfileRows {
-  const double* prof;
-  int N, h, Nx;
-  __device__ __forceinline__ T at(int pr, int m) const {
-    if (m < h) return (T)prof[(long)pr * N + h + m];
-    if (m >= Nx - h) return (T)prof[(long)pr * N + m - (Nx - h)];
-    return (T)0;
-  }
-  __device__ __forceinline__ C2<T> pair(int j, int n) const {
-    int pr = (j < h) ? h + j : j - h;
-    return C2<T>{at(pr, 2 * n), at(pr, 2 * n + 1)};
-  }
-};
-
-// ---------------------------------------------------------------- row kernels
-
-// Real FFT of one row per CTA; writes Nx/2+1 complex values and zero padding up to Wp.
-template <typename T, typename Loader>
-__global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__ out, long pitch, int M,
-                                                  RadixList rl, const C2<T>* __restrict__ twx) {
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
-  C2<T>* b = a + (M + 1);
-  const int row = blockIdx.x;
-  for (int n = threadIdx.x; n < M; n += blockDim.x) a[n] = ld.pair(row, n);
-  __syncthreads();
-  C2<T>* Z = fft_smem<T, false, 1>(a, b, rl, twx);
-  C2<T>* o = out + (long)row * pitch;
-  for (int k = threadIdx.x; k <= M; k += blockDim.x) {
-    C2<T> zk = Z[k == M ? 0 : k];
-    C2<T> zc = cconj(Z[k == 0 ? 0 : M - k]);
-    C2<T> s = cadd(zk, zc);
-    C2<T> wd = cmul(ldc(twx + k), csub(zk, zc));  // W_Nx^k (Z - conj Z')
-    o[k] = C2<T>{(T)0.5 * (s.x + wd.y), (T)0.5 * (s.y - wd.x)};
-  }
-  for (int k = M + 1 + threadIdx.x; k < pitch; k += blockDim.x) o[k] = C2<T>{(T)0, (T)0};
-}
-
-// Inverse real FFT (unnormalised, like cuFFT Z2D) of one spectrum row per CTA.
-template <typename T>
-__global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, long pitch,
-                                                  typename RealOut<T>::type* __restrict__ out, long ldo, int M,
-                                                  RadixList rl, const C2<T>* __restrict__ twx) {
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
-  C2<T>* b = a + (M + 1);
-  const int row = blockIdx.x;
-  const C2<T>* src = in + (long)row * pitch;
-  for (int k = threadIdx.x; k <= M; k += blockDim.x) a[k] = src[k];
-  __syncthreads();
-  for (int k = threadIdx.x; k < M; k += blockDim.x) {
-    C2<T> xk = a[k];
-    C2<T> xm = cconj(a[M - k]);
-    C2<T> e = cadd(xk, xm);
-    C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
-    b[k] = C2<T>{e.x - o.y, e.y + o.x};
-  }
-  __syncthreads();
-  C2<T>* z = fft_smem<T, true, 1>(b, a, rl, twx);
-  using TO = typename RealOut<T>::type;
-  C2<TO>* dst = reinterpret_cast<C2<TO>*>(out + (long)row * ldo);
-  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{RealOut<T>::cvt(z[n].x), RealOut<T>::cvt(z[n].y)};
-}
-
-// Inverse real FFT of one spectrum row per CTA with M = L1 L2 L3 (J = L2 L3) in three
-// register levels.  b[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W_Nx^-k is the
-// complex sequence whose inverse FFT z gives the real row (out[2n], out[2n+1]) = z[n].
-//   level 1, item j < J:        b[J a + j] (a < L1) from global memory, DFT^-1_L1 over a,
-//                               twiddle W_M^-(j n1)                   -> s[n1 J + j]
-//   level 2, item (n1, m < L3): DFT^-1_L2 over b of s[n1 J + L3 b + m], twiddle W_J^-(m n2)
-//                                                                      -> s[n1 J + n2 L3 + m]
-//   level 3, item (n1, n2):     DFT^-1_L3 over m                      -> z[n1 + L1 (n2 + L2 n3)]
-// and one coalesced copy of z to the output row.  Levels 2 and 3 read all their inputs
-// before a barrier and then overwrite the same buffer (M complex values, 40 KB at
-// M = 5000 in FP32).  Items of levels 2 and 3 fit in one pass of the CTA (L1 L3 and
-// L1 L2 <= blockDim).
-template <typename T, int L1, int L2, int L3>
-__device__ __forceinline__ void c2r3_row(const C2<T>* __restrict__ a, const C2<T>* __restrict__ twx, C2<T>* s) {
-  constexpr int J = L2 * L3, M = L1 * J;
-  C2<T>* wJ = s + M;  // W_J^e = W_Nx^(2 L1 e), e < J
-  const int tid = threadIdx.x;
-  for (int e = tid; e < J; e += blockDim.x) wJ[e] = ldc(twx + 2L * L1 * e);
-  for (int j = tid; j < J; j += blockDim.x) {
-    C2<T> v[L1];
-#pragma unroll
-    for (int q = 0; q < L1; q++) {
-      const int k = J * q + j;
-      const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
-      const C2<T> e = cadd(xk, xm);
-      const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
-      v[q] = C2<T>{e.x - o.y, e.y + o.x};
-    }
-    Dft<T, L1, true>::run(v);
-    s[j] = v[0];
-#pragma unroll
-    for (int n1 = 1; n1 < L1; n1++) s[n1 * J + j] = cmulc(v[n1], ldc(twx + 2L * j * n1));  // W_M^-(j n1)
-  }
-  __syncthreads();
-  {
-    const bool act = tid < L1 * L3;
-    const int n1 = tid / L3, m = tid - n1 * L3;
-    C2<T> u[L2];
-    if (act) {
-#pragma unroll
-      for (int b = 0; b < L2; b++) u[b] = s[n1 * J + L3 * b + m];
-      Dft<T, L2, true>::run(u);
-#pragma unroll
-      for (int n2 = 1; n2 < L2; n2++) u[n2] = cmulc(u[n2], wJ[m * n2]);
-    }
-    __syncthreads();
-    if (act) {
-#pragma unroll
-      for (int n2 = 0; n2 < L2; n2++) s[n1 * J + n2 * L3 + m] = u[n2];
-    }
-  }
-  __syncthreads();
-  {
-    const bool act = tid < L1 * L2;
-    const int n2 = tid / L1, n1 = tid - n2 * L1;  // n1 fastest: the writes below are contiguous
-    C2<T> w[L3];
-    if (act) {
-#pragma unroll
-      for (int m = 0; m < L3; m++) w[m] = s[n1 * J + n2 * L3 + m];
-      Dft<T, L3, true>::run(w);
-    }
-    __syncthreads();
-    if (act) {
-#pragma unroll
-      for (int n3 = 0; n3 < L3; n3++) s[n1 + L1 * (n2 + L2 * n3)] = w[n3];
-    }
-  }
-  __syncthreads();
-}
-
-template <typename T, int L1, int L2, int L3>
-__global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in, long pitch,
-                                                   typename RealOut<T>::type* __restrict__ out, long ldo,
-                                                   const C2<T>* __restrict__ twx) {
-  constexpr int M = L1 * L2 * L3;
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
-  const int row = blockIdx.x;
-  c2r3_row<T, L1, L2, L3>(in + (long)row * pitch, twx, s);
-  using TO = typename RealOut<T>::type;
-  C2<TO>* dst = reinterpret_cast<C2<TO>*>(out + (long)row * ldo);
-  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{RealOut<T>::cvt(s[n].x), RealOut<T>::cvt(s[n].y)};
-}
-
-// P3 of four profiles with the interleave fused in.  A cluster of four CTAs takes one row
-// of four profiles' spectra (CTA rank k: profile 4*quad + k; ranks past nm hold zeros),
-// each CTA runs the three-level c2r of its row into its own shared memory, and after a
-// cluster barrier CTA k writes pixels [k Nx/4, (k+1) Nx/4) of the interleaved row, reading
-// the four rows through distributed shared memory: out[(row Nx + x) S + 4 quad + q], one
-// 16-byte store per pixel (FP32).  The clusters of the other profiles of the same row are
-// launched next to it, so their stores complete each 32-byte sector in L2 before it is
-// written back.  No planar maps and no separate interleave pass; the arithmetic is
-// k_rows_c2r3's.  (Measured at 10000^2, 16 profiles: clusters of 4 6.0 ms, of 8 6.1 ms,
-// of 2 or 1 (8- or 4-byte strided stores) 9.8 ms.)
-template <typename T, int L1, int L2, int L3>
-__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
-    k_rows_c2r3_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm,
-                   typename RealOut<T>::type* __restrict__ out, int S, const C2<T>* __restrict__ twx, unsigned planar) {
-  using TO = typename RealOut<T>::type;
-  constexpr int J = L2 * L3, M = L1 * J, NX = 2 * M;
-  namespace cg = cooperative_groups;
-  cg::cluster_group cl = cg::this_cluster();
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
-  const int row = blockIdx.y;
-  const int k = (int)cl.block_rank(), quad = blockIdx.x >> 2, q = 4 * quad + k;
-  if (q < nm && ((planar >> q) & 1u)) {  // the direct form's real map: copy its row
-    const TO* src = reinterpret_cast<const TO*>(specs + (long)q * spec_stride) + (long)row * NX;
-    T* d = reinterpret_cast<T*>(s);
-    for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = T(src[n]);
-  } else if (q < nm) {
-    c2r3_row<T, L1, L2, L3>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
-  } else {
-    for (int n = threadIdx.x; n < M; n += blockDim.x) s[n] = C2<T>{T(0), T(0)};
-  }
-  cl.sync();  // every row of the cluster is in its CTA's shared memory
-  const int W = S - 4 * quad < 4 ? S - 4 * quad : 4;  // values per pixel from this cluster
-  constexpr int CH = (NX + 3) / 4;
-  const int x0 = k * CH, x1 = x0 + CH < NX ? x0 + CH : NX;
-  TO* dst = out + (long)row * NX * S + 4 * quad;
-  if (W == 4) {
-    const T* src[4];
-#pragma unroll
-    for (int r = 0; r < 4; r++) src[r] = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
-    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
-      TO v[4];
-#pragma unroll
-      for (int r = 0; r < 4; r++) v[r] = RealOut<T>::cvt(src[r][x]);
-      float4* d = reinterpret_cast<float4*>(dst + (long)x * S);
-      const float4* w = reinterpret_cast<const float4*>(v);
-#pragma unroll
-      for (int i = 0; i < (int)(4 * sizeof(TO) / 16); i++) d[i] = w[i];
-    }
-  } else {
-    for (int r = 0; r < W; r++) {
-      const T* sr = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
-      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = RealOut<T>::cvt(sr[x]);
-    }
-  }
-  // no CTA leaves while the others still read its shared memory.  Execution order is all
-  // this barrier needs (every remote load has returned before the stores that use it), so
-  // the arrive is relaxed: no release fence for this CTA's global stores.
-  asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
-}
-
-// ---------------------------------------------------------------- column kernels
-
-// In-place sub-pass over the row set {set*set_mul + j*j_mul : j < L} of one strip of CW
-// columns.  post_tw multiplies output j by W_Ny^(+/- set*j).
-template <typename T, int CW, bool INV>
-__global__ void __launch_bounds__(256) k_colpass(C2<T>* __restrict__ buf, long pitch, int L, long set_mul,
-                                                 long j_mul, RadixList rl, const C2<T>* __restrict__ twy,
-                                                 int tw_stride, int post_tw) {
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
-  C2<T>* b = a + L * CW;
-  C2<T>* tab = b + L * CW;   // stage twiddles (rl.tlen)
-  C2<T>* pw = tab + rl.tlen; // post twiddles W_Ny^(set j), j < L
-  const int set = blockIdx.y;
-  const long col0 = (long)blockIdx.x * CW;
-  const long base = (long)set * set_mul;
-  for (int idx = threadIdx.x; idx < L * CW; idx += blockDim.x) {
-    int j = idx / CW, c = idx % CW;
-    a[idx] = buf[(base + j * j_mul) * pitch + col0 + c];
-  }
-  fill_stage_twiddles<T>(rl, twy, tab);
-  if (post_tw)
-    for (int j = threadIdx.x; j < L; j += blockDim.x) pw[j] = ldc(twy + (long)set * j);  // set*j < Ny
-  __syncthreads();
-  C2<T>* r = fft_smem_st<T, INV, CW>(a, b, rl, tab);
-  for (int idx = threadIdx.x; idx < L * CW; idx += blockDim.x) {
-    int j = idx / CW, c = idx % CW;
-    C2<T> v = r[idx];
-    if (post_tw) v = INV ? cmulc(v, pw[j]) : cmul(v, pw[j]);
-    buf[(base + j * j_mul) * pitch + col0 + c] = v;
-  }
-}
-
-// The same sub-pass for L = L1 * L2 with both factors done in registers (four-step):
-// thread (n2, c) loads x[L2 n1 + n2] (n1 < L1) straight from global memory, DFT_L1 over n1,
-// twiddle W_L^(n2 k1), one transpose through shared memory, then thread (k1, c) does
-// DFT_L2 over n2 and writes X[k1 + L1 k2] straight back.  One shared-memory round trip and
-// fixed per-thread indices instead of a Stockham stage loop per radix.
-template <typename T, int CW, int L1, int L2, bool INV>
-__global__ void __launch_bounds__(256) k_colpass2(C2<T>* __restrict__ buf, long pitch, long set_mul, long j_mul,
-                                                  const C2<T>* __restrict__ twy, int tw_stride, int post_tw) {
-  constexpr int L = L1 * L2;
-  __shared__ C2<T> y[L2][L1][CW];
-  __shared__ C2<T> wl[L];  // W_L^m
-  __shared__ C2<T> pw[L];  // post twiddles W_Ny^(set j)
-  const int set = blockIdx.y;
-  const long col0 = (long)blockIdx.x * CW;
-  const long base = (long)set * set_mul;
-  const int c = threadIdx.x % CW, g = threadIdx.x / CW;
-  for (int m = threadIdx.x; m < L; m += blockDim.x) {
-    wl[m] = ldc(twy + (long)m * tw_stride);
-    if (post_tw) pw[m] = ldc(twy + (long)set * m);  // set*m < Ny
-  }
-  C2<T> v[L1];
-  if (g < L2) {
-#pragma unroll
-    for (int n1 = 0; n1 < L1; n1++) v[n1] = buf[(base + (long)(L2 * n1 + g) * j_mul) * pitch + col0 + c];
-  }
-  __syncthreads();
-  if (g < L2) {
-    Dft<T, L1, INV>::run(v);
-#pragma unroll
-    for (int k1 = 0; k1 < L1; k1++) y[g][k1][c] = (k1 == 0) ? v[0] : (INV ? cmulc(v[k1], wl[g * k1]) : cmul(v[k1], wl[g * k1]));
-  }
-  __syncthreads();
-  if (g < L1) {
-    C2<T> u[L2];
-#pragma unroll
-    for (int n2 = 0; n2 < L2; n2++) u[n2] = y[n2][g][c];
-    Dft<T, L2, INV>::run(u);
-#pragma unroll
-    for (int k2 = 0; k2 < L2; k2++) {
-      const int j = g + L1 * k2;
-      C2<T> val = u[k2];
-      if (post_tw) val = INV ? cmulc(val, pw[j]) : cmul(val, pw[j]);
-      buf[(base + (long)j * j_mul) * pitch + col0 + c] = val;
-    }
-  }
-}
-
-// P1 of the fused convolution, one CTA per (strip, k1).
-template <typename T, int CW>
-__global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
-                                                    long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
-                                                    int N1, int N2, RadixList rl2,
-                                                    const C2<T>* __restrict__ twy, T scale) {
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
-  C2<T>* b = a + N2 * CW;
-  C2<T>* w1 = b + N2 * CW;   // W_N1^(n1 k1) for n1 < N1, this CTA's k1
-  C2<T>* w2 = w1 + N1;       // W_Ny^(n2 k1) for n2 < N2
-  C2<T>* tab = w2 + N2;      // stage twiddles of the N2 transforms (rl2.tlen)
-  const int k1 = blockIdx.y;
-  const long col0 = (long)blockIdx.x * CW;
-  for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * k1) % N1) * N2);
-  for (int n2 = threadIdx.x; n2 < N2; n2 += blockDim.x) w2[n2] = ldc(twy + (long)n2 * k1);
-  fill_stage_twiddles<T>(rl2, twy, tab);
-  __syncthreads();
-  // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 k1)
-  const int lo = Ny - h;  // first non-zero high row
-  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
-    const int n2 = idx / CW, c = idx & (CW - 1);
-    C2<T> acc{(T)0, (T)0};
-    for (int n1 = 0; n1 * N2 + n2 < h; n1++) {
-      const long j = (long)n1 * N2 + n2;
-      acc = cadd(acc, cmul(Kx[j * pitch + col0 + c], w1[n1]));
-    }
-    int n1s = (lo - n2 + N2 - 1) / N2;
-    if (n1s < 0) n1s = 0;
-    for (int n1 = n1s; n1 < N1; n1++) {
-      const long j = (long)n1 * N2 + n2 - (Ny - 2L * h);
-      acc = cadd(acc, cmul(Kx[j * pitch + col0 + c], w1[n1]));
-    }
-    a[idx] = cmul(acc, w2[n2]);
-  }
-  __syncthreads();
-  C2<T>* K = fft_smem_st<T, false, CW>(a, b, rl2, tab);
-  C2<T>* other = (K == a) ? b : a;
-  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
-    const int k2 = idx / CW, c = idx % CW;
-    C2<T> f = Fmap[((long)k1 * N2 + k2) * pitch + col0 + c];
-    K[idx] = cscale(cmul(f, K[idx]), scale);
-  }
-  __syncthreads();
-  C2<T>* U = fft_smem_st<T, true, CW>(K, other, rl2, tab);
-  for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
-    const int n2 = idx / CW, c = idx % CW;
-    C2<T> v = cmulc(U[idx], w2[n2]);
-    out[((long)k1 * N2 + n2) * pitch + col0 + c] = v;
-  }
-}
-
-// P1 for N2 = L1 * L2 with both factors in registers.  Forward N2 transform of the profile
-// column (built in shared memory as in k_conv_fused) as a four-step: thread (n2, c) DFT_L1
-// over x[L2 n1 + n2], twiddle, transpose, thread (k1, c) DFT_L2 -> it now holds frequencies
-// k = k1 + L1 k2, multiplies them by the map spectrum (read straight from global memory)
-// and 1/(Nx Ny), and starts the inverse as the transposed four-step on the same registers:
-// DFT^-1_L2 over k2, twiddle W_N2^-(k1 n2), transpose, thread (n2, c) DFT^-1_L1 over k1 ->
-// rows n2 + L2 n1, times W_Ny^-(n kk), stored.
-template <typename T, int CW, int L1, int L2>
-__global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
-                                                     long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
-                                                     int N1, const C2<T>* __restrict__ twy, T scale) {
-  constexpr int N2 = L1 * L2;
-  extern __shared__ unsigned char smem_raw[];
-  C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);  // [N2][CW] profile column sub-pass
-  C2<T>* y = a;                                   // the transposes reuse it ([L2][L1][CW])
-  C2<T>* w1 = y + N2 * CW;                        // W_N1^(n1 kk), n1 < N1
-  C2<T>* w2 = w1 + N1;                            // W_Ny^(n kk), n < N2
-  C2<T>* wl = w2 + N2;                            // W_N2^m, m < N2
-  const int kk = blockIdx.y;
-  const long col0 = (long)blockIdx.x * CW;
-  const int c = threadIdx.x % CW, g = threadIdx.x / CW;
-  for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * kk) % N1) * N2);
-  for (int n = threadIdx.x; n < N2; n += blockDim.x) {
-    w2[n] = ldc(twy + (long)n * kk);
-    wl[n] = ldc(twy + (long)n * N1);
-  }
-  __syncthreads();
-  // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 kk).
-  // Thread (g, c) owns the rows n2 = g + G i (G = blockDim / CW); the terms run outer and the
-  // elements inner, so the loads of all its elements for one term are in flight together.
-  {
-    constexpr int G = (L1 > L2 ? L1 : L2), NE = N2 / G;
-    static_assert(N2 % G == 0, "rows per thread");
-    C2<T> acc[NE];
-#pragma unroll
-    for (int i = 0; i < NE; i++) acc[i] = C2<T>{(T)0, (T)0};
-    const int tlo = (h + N2 - 1) / N2;  // low rows: kernel rows n1 N2 + n2 < h
-    for (int n1 = 0; n1 < tlo; n1++) {
-      const C2<T> w = w1[n1];
-#pragma unroll
-      for (int i = 0; i < NE; i++) {
-        const int n2 = g + G * i, j = n1 * N2 + n2;
-        if (j < h) acc[i] = cadd(acc[i], cmul(Kx[(long)j * pitch + col0 + c], w));
-      }
-    }
-    // high rows: kernel rows >= Ny - h, in the last thi values of n1 (increasing)
-    const int thi = (h + N2 - 1) / N2 + 1;
-    for (int t = 0; t < thi; t++) {
-      const int n1 = N1 - thi + t;
-      if (n1 < 0) continue;
-      const C2<T> w = w1[n1];
-#pragma unroll
-      for (int i = 0; i < NE; i++) {
-        const int n2 = g + G * i;
-        const long jr = (long)n1 * N2 + n2;  // kernel row
-        if (jr >= (long)Ny - h && jr < Ny && (n1 > 0 || jr >= h))
-          acc[i] = cadd(acc[i], cmul(Kx[(jr - (Ny - 2L * h)) * pitch + col0 + c], w));
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < NE; i++) {
-      const int n2 = g + G * i;
-      a[n2 * CW + c] = cmul(acc[i], w2[n2]);
-    }
-  }
-  __syncthreads();
-  // forward stage 1: thread (n2 = g, c); every input is read before the shared buffer is
-  // overwritten with the transposed result
-  {
-    C2<T> v[L1];
-    if (g < L2) {
-#pragma unroll
-      for (int n1 = 0; n1 < L1; n1++) v[n1] = a[(L2 * n1 + g) * CW + c];
-      Dft<T, L1, false>::run(v);
-    }
-    __syncthreads();
-    if (g < L2) {
-#pragma unroll
-      for (int k1 = 0; k1 < L1; k1++) y[(g * L1 + k1) * CW + c] = k1 == 0 ? v[0] : cmul(v[k1], wl[g * k1]);
-    }
-  }
-  __syncthreads();
-  // forward stage 2, product, inverse stage A: thread (k1 = g, c)
-  if (g < L1) {
-    C2<T> u[L2];
-#pragma unroll
-    for (int n2 = 0; n2 < L2; n2++) u[n2] = y[(n2 * L1 + g) * CW + c];
-    Dft<T, L2, false>::run(u);
-#pragma unroll
-    for (int k2 = 0; k2 < L2; k2++) {
-      const C2<T> f = Fmap[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c];
-      u[k2] = cscale(cmul(f, u[k2]), scale);
-    }
-    Dft<T, L2, true>::run(u);  // over k2 -> n2
-    // the thread rewrites exactly the entries of y it read above: no other thread's data
-#pragma unroll
-    for (int n2 = 0; n2 < L2; n2++) y[(n2 * L1 + g) * CW + c] = n2 == 0 ? u[0] : cmulc(u[n2], wl[g * n2]);
-  }
-  __syncthreads();
-  // inverse stage B: thread (n2 = g, c) over k1 -> rows n2 + L2 n1
-  if (g < L2) {
-    C2<T> v[L1];
-#pragma unroll
-    for (int k1 = 0; k1 < L1; k1++) v[k1] = y[(g * L1 + k1) * CW + c];
-    Dft<T, L1, true>::run(v);
-#pragma unroll
-    for (int n1 = 0; n1 < L1; n1++) {
-      const int n = g + L2 * n1;
-      out[((long)kk * N2 + n) * pitch + col0 + c] = cmulc(v[n1], w2[n]);
-    }
-  }
-}
-
-// ---------------------------------------------------------------- plain-path helpers
-
-template <typename T>
-__global__ void k_wrap_full(const double* __restrict__ prof, int N, int Nx, int Ny, T* __restrict__ out) {
-  const int h = N / 2;
-  const long total = (long)Nx * Ny;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const int y = (int)(i / Nx), x = (int)(i % Nx);
-    int pr = -1, pc = -1;
-    if (y < h) pr = h + y;
-    else if (y >= Ny - h) pr = y - (Ny - h);
-    if (x < h) pc = h + x;
-    else if (x >= Nx - h) pc = x - (Nx - h);
-    out[i] = (pr >= 0 && pc >= 0) ? (T)prof[(long)pr * N + pc] : (T)0;
-  }
-}
-
-// kernel_multiplyFFTs (gpu_functions.cu:571-577): Fk = Fmap * Fk / norm, in place.
-template <typename T>
-__global__ void k_multiply(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ Fk, long n, T scale) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    C2<T> m = cmul(Fmap[i], Fk[i]);
-    Fk[i] = C2<T>{m.x * scale, m.y * scale};
-  }
-}
-
-// ---------------------------------------------------------------- host orchestration
-
-template <typename T, typename Loader>
-static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, int nrows, void* out) {
-  if (nrows <= 0) return;
-  size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
-  auto kern = k_rows_r2c<T, Loader>;
-  set_max_smem((const void*)kern, smem);
-  {
-    MLC_KSCOPE(ctx, "fft_rows_r2c");
-    kern<<<nrows, 512, smem, ctx->stream>>>(ld, (C2<T>*)out, p.Wp, p.M, p.rlM, (const C2<T>*)p.twx);
-  }
-  MLC_CHECK_LAUNCH();
-}
-
-template <typename T>
-static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, void* out) {
-  {
-    using TO = typename RealOut<T>::type;
-    using K3 = void (*)(const C2<T>*, long, TO*, long, const C2<T>*);
-    K3 k3 = nullptr;
-    int J = 0;
-    switch (p.M) {
-      case 5000: k3 = k_rows_c2r3<T, 8, 25, 25>; J = 625; break;
-      case 4096: k3 = k_rows_c2r3<T, 16, 16, 16>; J = 256; break;
-      case 2000: k3 = k_rows_c2r3<T, 8, 10, 25>; J = 250; break;
-      case 1000: k3 = k_rows_c2r3<T, 10, 10, 10>; J = 100; break;
-      default: break;
-    }
-    if (k3) {
-      const size_t smem3 = ((size_t)p.M + J) * sizeof(C2<T>);
-      set_max_smem((const void*)k3, smem3);
-      {
-        MLC_KSCOPE(ctx, "fft_rows_c2r");
-        k3<<<p.Ny, 256, smem3, ctx->stream>>>((const C2<T>*)in, p.Wp, (TO*)out, p.Nx, (const C2<T>*)p.twx);
-      }
-      MLC_CHECK_LAUNCH();
-      return;
-    }
-  }
-  size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
-  auto kern = k_rows_c2r<T>;
-  set_max_smem((const void*)kern, smem);
-  {
-    MLC_KSCOPE(ctx, "fft_rows_c2r");
-    kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (typename RealOut<T>::type*)out, p.Nx, p.M, p.rlM,
-                                         (const C2<T>*)p.twx);
-  }
-  MLC_CHECK_LAUNCH();
-}
-
-// kind 'A': row sets {n2 + N2*j}, length N1; kind 'B': row blocks {k1*N2 + j}, length N2.
-template <typename T, bool INV>
-static void launch_colpass(mlc_ctx* ctx, const FftPlan2D& p, void* buf, char kind, int post_tw) {
-  constexpr int CW = sizeof(T) == 8 ? 8 : 16;
-  const int nstrips = ceil_div(p.Wc, CW);
-  int L, nsets, tw_stride;
-  long set_mul, j_mul;
-  RadixList rl;
-  if (kind == 'A') {
-    L = p.N1; nsets = p.N2; set_mul = 1; j_mul = p.N2; tw_stride = p.N2; rl = p.rlN1;
-  } else {
-    L = p.N2; nsets = p.N1; set_mul = p.N2; j_mul = 1; tw_stride = p.N1; rl = p.rlN2;
-  }
-  if (L == 1 && !post_tw) return;
-  // two-level register kernels for the lengths that split into two supported factors
-  using K2 = void (*)(C2<T>*, long, long, long, const C2<T>*, int, int);
-  K2 k2 = nullptr;
-  int nthr = 0;
-  switch (L) {
-    case 100: k2 = k_colpass2<T, CW, 10, 10, INV>; nthr = 10 * CW; break;
-    case 128: k2 = k_colpass2<T, CW, 8, 16, INV>; nthr = 16 * CW; break;
-    case 64: k2 = k_colpass2<T, CW, 8, 8, INV>; nthr = 8 * CW; break;
-    case 80: k2 = k_colpass2<T, CW, 8, 10, INV>; nthr = 10 * CW; break;
-    case 50: k2 = k_colpass2<T, CW, 5, 10, INV>; nthr = 10 * CW; break;
-    case 40: k2 = k_colpass2<T, CW, 5, 8, INV>; nthr = 8 * CW; break;
-    default: break;
-  }
-  if (k2) {
-    dim3 grid(nstrips, nsets);
-    {
-      MLC_KSCOPE(ctx, kind == 'A' ? "fft_col_A" : "fft_col_B");
-      k2<<<grid, nthr, 0, ctx->stream>>>((C2<T>*)buf, p.Wp, set_mul, j_mul, (const C2<T>*)p.twy, tw_stride, post_tw);
-    }
-    MLC_CHECK_LAUNCH();
-    return;
-  }
-  size_t smem = (2 * (size_t)L * CW + rl.tlen + L) * sizeof(C2<T>);
-  auto kern = k_colpass<T, CW, INV>;
-  set_max_smem((const void*)kern, smem);
-  dim3 grid(nstrips, nsets);
-  {
-    MLC_KSCOPE(ctx, kind == 'A' ? "fft_col_A" : "fft_col_B");
-    kern<<<grid, 256, smem, ctx->stream>>>((C2<T>*)buf, p.Wp, L, set_mul, j_mul, rl, (const C2<T>*)p.twy,
-                                         tw_stride, post_tw);
-  }
-  MLC_CHECK_LAUNCH();
-}
-
-template <typename T>
-static void forward_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec) {
-  if (in_dtype == MLC_F64)
-    launch_rows_r2c<T>(ctx, p, RealRows<T, double>{(const double*)in, p.Nx}, p.Ny, spec);
-  else
-    launch_rows_r2c<T>(ctx, p, RealRows<T, float>{(const float*)in, p.Nx}, p.Ny, spec);
-  launch_colpass<T, false>(ctx, p, spec, 'A', 1);
-  launch_colpass<T, false>(ctx, p, spec, 'B', 0);
-}
+// ---------------------------------------------------------------- dispatch by precision
 
 void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec) {
   if (p.prec == PREC_FF) forward_impl<ff>(ctx, p, in, in_dtype, spec);
   else if (p.prec == MLC_F64) forward_impl<double>(ctx, p, in, in_dtype, spec);
   else forward_impl<float>(ctx, p, in, in_dtype, spec);
-}
-
-// spec_out: stop after P2 and leave the inverse half-spectrum there (pitch Wp) instead of
-// running P3 into out.
-template <typename T>
-static void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
-                            void* out, void* spec_out = nullptr, int kx_slot = WS_KX) {
-  constexpr int CW = sizeof(T) == 8 ? 8 : 16;
-  const int h = pN / 2;
-  MLC_REQUIRE(pN % 2 == 0 && 2 * h <= p.Ny && 2 * h <= p.Nx, MLC_ERR_LIMIT,
-              "profile raster larger than the map");
-  void* kx = ws_get(ctx, kx_slot, (size_t)(2 * h > 0 ? 2 * h : 1) * p.Wp * sizeof(C2<T>));
-  void* tmp = spec_out ? spec_out : ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
-  launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
-  const int nstrips = ceil_div(p.Wc, CW);
-  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
-  {
-    // two-level register kernel where N2 splits into two supported factors
-    using K2 = void (*)(const C2<T>*, C2<T>*, long, const C2<T>*, int, int, int, const C2<T>*, T);
-    K2 k2 = nullptr;
-    int nthr = 0;
-    switch (p.N2) {
-      case 100: k2 = k_conv_fused2<T, CW, 10, 10>; nthr = 10 * CW; break;
-      case 128: k2 = k_conv_fused2<T, CW, 8, 16>; nthr = 16 * CW; break;
-      case 64: k2 = k_conv_fused2<T, CW, 8, 8>; nthr = 8 * CW; break;
-      case 80: k2 = k_conv_fused2<T, CW, 8, 10>; nthr = 10 * CW; break;
-      case 50: k2 = k_conv_fused2<T, CW, 5, 10>; nthr = 10 * CW; break;
-      case 40: k2 = k_conv_fused2<T, CW, 5, 8>; nthr = 8 * CW; break;
-      default: break;
-    }
-    if (k2) {
-      const size_t smem2 = ((size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
-      set_max_smem((const void*)k2, smem2);
-      {
-        MLC_KSCOPE(ctx, "conv_fused_spectrum");
-        k2<<<dim3(nstrips, p.N1), nthr, smem2, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp,
-                                                              (const C2<T>*)kx, h, p.Ny, p.N1,
-                                                              (const C2<T>*)p.twy, scale);
-      }
-      MLC_CHECK_LAUNCH();
-      launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
-      if (!spec_out) launch_rows_c2r<T>(ctx, p, tmp, out);
-      return;
-    }
-  }
-  size_t smem = (2 * (size_t)p.N2 * CW + p.N1 + p.N2 + p.rlN2.tlen) * sizeof(C2<T>);
-  auto kern = k_conv_fused<T, CW>;
-  set_max_smem((const void*)kern, smem);
-  dim3 grid(nstrips, p.N1);
-  {
-    MLC_KSCOPE(ctx, "conv_fused_spectrum");
-    kern<<<grid, 256, smem, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp, (const C2<T>*)kx, h, p.Ny,
-                                         p.N1, p.N2, p.rlN2, (const C2<T>*)p.twy, scale);
-  }
-  MLC_CHECK_LAUNCH();
-  launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
-  if (!spec_out) launch_rows_c2r<T>(ctx, p, tmp, out);
-}
-
-template <typename T>
-static void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
-                            void* out) {
-  MLC_REQUIRE(pN % 2 == 0 && pN <= p.Ny && pN <= p.Nx, MLC_ERR_LIMIT, "profile raster larger than the map");
-  void* kreal = ws_get(ctx, WS_KREAL, (size_t)p.Nx * p.Ny * sizeof(T));
-  void* kspec = ws_get(ctx, WS_KSPEC, p.spec_bytes());
-  const long total = (long)p.Nx * p.Ny;
-  int grid = (int)std::min<long>((total + 255) / 256, (long)ctx->sm_count * 16);
-  {
-    MLC_KSCOPE(ctx, "conv_plain_wrap");
-    k_wrap_full<T><<<grid, 256, 0, ctx->stream>>>(prof, pN, p.Nx, p.Ny, (T*)kreal);
-  }
-  MLC_CHECK_LAUNCH();
-  forward_impl<T>(ctx, p, kreal, sizeof(T) == 8 ? MLC_F64 : MLC_F32, kspec);
-  const long n = (long)p.Ny * p.Wp;
-  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
-  grid = (int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 16);
-  {
-    MLC_KSCOPE(ctx, "conv_plain_multiply");
-    k_multiply<T><<<grid, 256, 0, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)kspec, n, scale);
-  }
-  MLC_CHECK_LAUNCH();
-  launch_colpass<T, true>(ctx, p, kspec, 'B', 1);
-  launch_colpass<T, true>(ctx, p, kspec, 'A', 0);
-  launch_rows_c2r<T>(ctx, p, kspec, out);
 }
 
 void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
@@ -893,33 +207,6 @@ void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, con
   if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
   else if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
   else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
-}
-
-template <typename T>
-static bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
-                                void* out, unsigned planar) {
-  using TO = typename RealOut<T>::type;
-  using K = void (*)(const C2<T>*, long, long, int, TO*, int, const C2<T>*, unsigned);
-  K k = nullptr;
-  int J = 0;
-  switch (p.M) {
-    case 5000: k = k_rows_c2r3_il<T, 8, 25, 25>; J = 625; break;
-    case 4096: k = k_rows_c2r3_il<T, 16, 16, 16>; J = 256; break;
-    case 2000: k = k_rows_c2r3_il<T, 8, 10, 25>; J = 250; break;
-    case 1000: k = k_rows_c2r3_il<T, 10, 10, 10>; J = 100; break;
-    default: return false;
-  }
-  if (!rows_c2r_interleave_supported(p)) return false;
-  const size_t smem = ((size_t)p.M + J) * sizeof(C2<T>);
-  set_max_smem((const void*)k, smem);
-  const int quads = (nm + 3) / 4;
-  {
-    MLC_KSCOPE(ctx, "fft_rows_c2r_interleave");
-    k<<<dim3(4 * quads, p.Ny), 256, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (TO*)out, S,
-                                                          (const C2<T>*)p.twx, planar);
-  }
-  MLC_CHECK_LAUNCH();
-  return true;
 }
 
 bool rows_c2r_interleave_supported(const FftPlan2D& p) {

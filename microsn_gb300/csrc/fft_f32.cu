@@ -1,0 +1,11 @@
+// FP32 instantiations of the FFT and convolution passes of fft_impl.cuh.
+#include "fft_impl.cuh"
+
+namespace mlc {
+
+template void forward_impl<float>(mlc_ctx*, const FftPlan2D&, const void*, int, void*);
+template void conv_fused_impl<float>(mlc_ctx*, const FftPlan2D&, const void*, const double*, int, void*, void*, int);
+template void conv_plain_impl<float>(mlc_ctx*, const FftPlan2D&, const void*, const double*, int, void*);
+template bool c2r_interleave_impl<float>(mlc_ctx*, const FftPlan2D&, const void*, long, int, int, void*, unsigned);
+
+}  // namespace mlc

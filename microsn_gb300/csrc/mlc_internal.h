@@ -183,6 +183,18 @@ bool rows_c2r_interleave(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, lo
                          void* out, unsigned planar = 0);
 void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof_dev, int pN,
                 void* out_real);
+// Their per-precision forms (T = float, double, ff), defined in fft_impl.cuh and
+// instantiated explicitly in fft_f32.cu, fft_f64.cu and fft_ff_*.cu.
+template <typename T>
+void forward_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec);
+template <typename T>
+void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out,
+                     void* spec_out = nullptr, int kx_slot = WS_KX);
+template <typename T>
+void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out);
+template <typename T>
+bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
+                         void* out, unsigned planar);
 
 // Host profile rasters (profile.cpp)
 int profile_dims(const mlc_profile& p);
