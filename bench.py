@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-c5", action="store_true", help="skip the supernova multi-image workload")
     ap.add_argument("--n", type=int, default=None, help="map side (profiling cases only; not a bench number)")
     ap.add_argument("--tracks", type=int, default=None, help="track count (profiling cases only)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="FFT form for every profile (for ncu captures, under which the autotuner's first-call "
+                         "timings are distorted)")
     return ap.parse_args()
 
 
@@ -915,6 +918,8 @@ def main():
     torch.cuda.set_device(local)
     n, ntracks = sizes_for(args)
     ctx = mlc.Context(local)
+    if args.no_autotune:
+        ctx.set_autotune(False)
     stream = torch.cuda.current_stream(local)
 
     # ---- inputs resident in HBM
@@ -1028,19 +1033,24 @@ def main():
         e2e_ms = float(te.item())
     e2e_val = world * lc_per_step / (e2e_ms / 1000.0)
     # the host link itself: plain 1 GiB copies between pinned host memory and HBM on this machine
-    # (the light curves' download bounds the e2e step)
+    # (the light curves' download bounds the e2e step); the host memory is shared with other
+    # jobs, so three samples of three copies each, the best one reported
     link = {}
     nl = min(1 << 28, h_out.numel())  # up to 1 GiB
     dbuf = torch.empty(nl, dtype=torch.float32, device=dev)
     hbuf = h_out.view(-1)[:nl]
     for name, dst, src in (("d2h_gbs", hbuf, dbuf), ("h2d_gbs", dbuf, hbuf)):
         dst.copy_(src, non_blocking=True)
-        e0.record(stream)
+        samples = []
         for _ in range(3):
-            dst.copy_(src, non_blocking=True)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        link[name] = 3 * 4 * nl / (e0.elapsed_time(e1) / 1000.0) / 1e9
+            e0.record(stream)
+            for _ in range(3):
+                dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            samples.append(3 * 4 * nl / (e0.elapsed_time(e1) / 1000.0) / 1e9)
+        link[name] = max(samples)
+        link[name + "_samples"] = samples
     link["download_floor_ms"] = bo / (link["d2h_gbs"] * 1e9) * 1000.0
     del h_out, dbuf
 
