@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "mlc_internal.h"
 
@@ -45,11 +46,22 @@ struct ProfileRows {
 
 // ---------------------------------------------------------------- row kernels
 
+// Spectrum value k <= M of a real row from Z = FFT_M(x[2n] + i x[2n+1]):
+// X[k] = (Z[k] + conj Z[M-k]) / 2 - i W_Nx^k (Z[k] - conj Z[M-k]) / 2, Z[M] = Z[0].
+template <typename T>
+__device__ __forceinline__ C2<T> r2c_split(const C2<T>* Z, int M, const C2<T>* __restrict__ twx, int k) {
+  const C2<T> zk = Z[k == M ? 0 : k];
+  const C2<T> zc = cconj(Z[k == 0 ? 0 : M - k]);
+  const C2<T> s = cadd(zk, zc);
+  const C2<T> wd = cmul(ldc(twx + k), csub(zk, zc));  // W_Nx^k (Z - conj Z')
+  return C2<T>{(T)0.5 * (s.x + wd.y), (T)0.5 * (s.y - wd.x)};
+}
+
 // Real FFT of one row per CTA; writes Nx/2+1 complex values and zero padding up to Wp.
 template <typename T, typename Loader>
 __global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__ out, long pitch, int M,
                                                   RadixList rl, const C2<T>* __restrict__ twx) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + (M + 1);
   const int row = blockIdx.x;
@@ -57,14 +69,75 @@ __global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__
   __syncthreads();
   C2<T>* Z = fft_smem<T, false, 1>(a, b, rl, twx);
   C2<T>* o = out + (long)row * pitch;
-  for (int k = threadIdx.x; k <= M; k += blockDim.x) {
-    C2<T> zk = Z[k == M ? 0 : k];
-    C2<T> zc = cconj(Z[k == 0 ? 0 : M - k]);
-    C2<T> s = cadd(zk, zc);
-    C2<T> wd = cmul(ldc(twx + k), csub(zk, zc));  // W_Nx^k (Z - conj Z')
-    o[k] = C2<T>{(T)0.5 * (s.x + wd.y), (T)0.5 * (s.y - wd.x)};
-  }
+  for (int k = threadIdx.x; k <= M; k += blockDim.x) o[k] = r2c_split(Z, M, twx, k);
   for (int k = M + 1 + threadIdx.x; k < pitch; k += blockDim.x) o[k] = C2<T>{(T)0, (T)0};
+}
+
+// Real FFT of one row per CTA with M = L1 L2 L3 (J = L2 L3) in three register levels, the
+// forward counterpart of c2r3_row below (same item shapes, forward DFTs and twiddles):
+//   level 1, item j < J:        z[J a + j] (a < L1) from the loader, DFT_L1 over a,
+//                               twiddle W_M^(j k1)                    -> s[k1 J + j]
+//   level 2, item (k1, m < L3): DFT_L2 over b of s[k1 J + L3 b + m], twiddle W_J^(m k2)
+//                                                                      -> s[k1 J + k2 L3 + m]
+//   level 3, item (k1, k2):     DFT_L3 over m                      -> Z[k1 + L1 (k2 + L2 k3)]
+// then the split into Nx/2+1 spectrum values and the zero padding up to Wp.  Four CTAs per
+// SM (three for 16^3, whose 80 registers would spill at 64), like k_rows_c2r3.
+template <typename T, int L1, int L2, int L3, typename Loader>
+__global__ void __launch_bounds__(256, L1 == 16 ? 3 : 4) k_rows_r2c3(Loader ld, C2<T>* __restrict__ out, long pitch,
+                                                   const C2<T>* __restrict__ twx) {
+  constexpr int J = L2 * L3, M = L1 * J;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
+  C2<T>* wJ = s + M;  // W_J^e = W_Nx^(2 L1 e), e < J
+  const int tid = threadIdx.x, row = blockIdx.x;
+  for (int e = tid; e < J; e += blockDim.x) wJ[e] = ldc(twx + 2L * L1 * e);
+  for (int j = tid; j < J; j += blockDim.x) {
+    C2<T> v[L1];
+#pragma unroll
+    for (int a = 0; a < L1; a++) v[a] = ld.pair(row, J * a + j);
+    Dft<T, L1, false>::run(v);
+    s[j] = v[0];
+#pragma unroll
+    for (int k1 = 1; k1 < L1; k1++) s[k1 * J + j] = cmul(v[k1], ldc(twx + 2L * j * k1));  // W_M^(j k1)
+  }
+  __syncthreads();
+  {
+    const bool act = tid < L1 * L3;
+    const int k1 = tid / L3, m = tid - k1 * L3;
+    C2<T> u[L2];
+    if (act) {
+#pragma unroll
+      for (int b = 0; b < L2; b++) u[b] = s[k1 * J + L3 * b + m];
+      Dft<T, L2, false>::run(u);
+#pragma unroll
+      for (int k2 = 1; k2 < L2; k2++) u[k2] = cmul(u[k2], wJ[m * k2]);
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int k2 = 0; k2 < L2; k2++) s[k1 * J + k2 * L3 + m] = u[k2];
+    }
+  }
+  __syncthreads();
+  {
+    const bool act = tid < L1 * L2;
+    const int k2 = tid / L1, k1 = tid - k2 * L1;
+    C2<T> w[L3];
+    if (act) {
+#pragma unroll
+      for (int m = 0; m < L3; m++) w[m] = s[k1 * J + k2 * L3 + m];
+      Dft<T, L3, false>::run(w);
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int k3 = 0; k3 < L3; k3++) s[k1 + L1 * (k2 + L2 * k3)] = w[k3];
+    }
+  }
+  __syncthreads();
+  C2<T>* o = out + (long)row * pitch;
+  for (int k = tid; k <= M; k += blockDim.x) o[k] = r2c_split(s, M, twx, k);
+  for (int k = M + 1 + tid; k < pitch; k += blockDim.x) o[k] = C2<T>{(T)0, (T)0};
 }
 
 // Inverse real FFT (unnormalised, like cuFFT Z2D) of one spectrum row per CTA.
@@ -72,7 +145,7 @@ template <typename T>
 __global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, long pitch,
                                                   typename RealOut<T>::type* __restrict__ out, long ldo, int M,
                                                   RadixList rl, const C2<T>* __restrict__ twx) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + (M + 1);
   const int row = blockIdx.x;
@@ -168,7 +241,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in,
                                                    typename RealOut<T>::type* __restrict__ out, long ldo,
                                                    const C2<T>* __restrict__ twx) {
   constexpr int M = L1 * L2 * L3;
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
   const int row = blockIdx.x;
   c2r3_row<T, L1, L2, L3>(in + (long)row * pitch, twx, s);
@@ -195,7 +268,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
   constexpr int J = L2 * L3, M = L1 * J, NX = 2 * M;
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
   const int row = blockIdx.y;
   const int k = (int)cl.block_rank(), quad = blockIdx.x >> 2, q = 4 * quad + k;
@@ -246,7 +319,7 @@ template <typename T, int CW, bool INV>
 __global__ void __launch_bounds__(256) k_colpass(C2<T>* __restrict__ buf, long pitch, int L, long set_mul,
                                                  long j_mul, RadixList rl, const C2<T>* __restrict__ twy,
                                                  int tw_stride, int post_tw) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + L * CW;
   C2<T>* tab = b + L * CW;   // stage twiddles (rl.tlen)
@@ -324,7 +397,7 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
                                                     long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
                                                     int N1, int N2, RadixList rl2,
                                                     const C2<T>* __restrict__ twy, T scale) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
   C2<T>* b = a + N2 * CW;
   C2<T>* w1 = b + N2 * CW;   // W_N1^(n1 k1) for n1 < N1, this CTA's k1
@@ -376,13 +449,15 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
 // k = k1 + L1 k2, multiplies them by the map spectrum (read straight from global memory)
 // and 1/(Nx Ny), and starts the inverse as the transposed four-step on the same registers:
 // DFT^-1_L2 over k2, twiddle W_N2^-(k1 n2), transpose, thread (n2, c) DFT^-1_L1 over k1 ->
-// rows n2 + L2 n1, times W_Ny^-(n kk), stored.
+// rows n2 + L2 n1, times W_Ny^-(n kk), stored.  (Staging the map-spectrum tile in shared
+// memory with cp.async made this kernel 3 % faster alone but the two-chain step 3 % slower:
+// the extra 12.8 KB per CTA crowds out the other chain's P2 CTAs.)
 template <typename T, int CW, int L1, int L2>
 __global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
                                                      long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
                                                      int N1, const C2<T>* __restrict__ twy, T scale) {
   constexpr int N2 = L1 * L2;
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);  // [N2][CW] profile column sub-pass
   C2<T>* y = a;                                   // the transposes reuse it ([L2][L1][CW])
   C2<T>* w1 = y + N2 * CW;                        // W_N1^(n1 kk), n1 < N1
@@ -391,6 +466,11 @@ __global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ F
   const int kk = blockIdx.y;
   const long col0 = (long)blockIdx.x * CW;
   const int c = threadIdx.x % CW, g = threadIdx.x / CW;
+  // the map-spectrum tile (N2 rows of CW values, the only DRAM input) is needed in forward
+  // stage 2, after two L2 round trips and three barriers: start pulling it into L2 now
+  // (without registers or shared memory, which the other chain's P2 CTAs need)
+  for (int n = threadIdx.x; n < N2; n += blockDim.x)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + ((long)kk * N2 + n) * pitch + col0));
   for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * kk) % N1) * N2);
   for (int n = threadIdx.x; n < N2; n += blockDim.x) {
     w2[n] = ldc(twy + (long)n * kk);
@@ -403,36 +483,55 @@ __global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ F
   {
     constexpr int G = (L1 > L2 ? L1 : L2), NE = N2 / G;
     static_assert(N2 % G == 0, "rows per thread");
-    C2<T> acc[NE];
-#pragma unroll
-    for (int i = 0; i < NE; i++) acc[i] = C2<T>{(T)0, (T)0};
-    const int tlo = (h + N2 - 1) / N2;  // low rows: kernel rows n1 N2 + n2 < h
-    for (int n1 = 0; n1 < tlo; n1++) {
-      const C2<T> w = w1[n1];
-#pragma unroll
-      for (int i = 0; i < NE; i++) {
-        const int n2 = g + G * i, j = n1 * N2 + n2;
-        if (j < h) acc[i] = cadd(acc[i], cmul(Kx[(long)j * pitch + col0 + c], w));
-      }
-    }
-    // high rows: kernel rows >= Ny - h, in the last thi values of n1 (increasing)
-    const int thi = (h + N2 - 1) / N2 + 1;
-    for (int t = 0; t < thi; t++) {
-      const int n1 = N1 - thi + t;
-      if (n1 < 0) continue;
-      const C2<T> w = w1[n1];
+    if (h <= N2) {
+      // Profiles of at most 2 N2 rows: kernel rows [0, h) lie in n1 = 0 (weight 1) and rows
+      // [Ny - h, Ny) in n1 = N1 - 1 (weight W_N1^((N1-1) kk)), so row n2 sums at most one
+      // low term (n2 < h) and one high term (n2 >= N2 - h, compacted row n2 - (N2 - h) + h):
+      // the general loop below with its zero terms and its unit weight left out (the same
+      // values: multiplying by the table's exact 1 and adding zeros round nothing).
+      const C2<T> wh = w1[N1 - 1];
+      const C2<T>* kx = Kx + col0 + c;
+      const int hb = N2 - h;
 #pragma unroll
       for (int i = 0; i < NE; i++) {
         const int n2 = g + G * i;
-        const long jr = (long)n1 * N2 + n2;  // kernel row
-        if (jr >= (long)Ny - h && jr < Ny && (n1 > 0 || jr >= h))
-          acc[i] = cadd(acc[i], cmul(Kx[(jr - (Ny - 2L * h)) * pitch + col0 + c], w));
+        C2<T> acc = C2<T>{(T)0, (T)0};
+        if (n2 < h) acc = kx[(long)n2 * pitch];
+        if (n2 >= hb) acc = cadd(acc, cmul(kx[(long)(n2 - hb + h) * pitch], wh));
+        a[n2 * CW + c] = cmul(acc, w2[n2]);
       }
-    }
+    } else {
+      C2<T> acc[NE];
 #pragma unroll
-    for (int i = 0; i < NE; i++) {
-      const int n2 = g + G * i;
-      a[n2 * CW + c] = cmul(acc[i], w2[n2]);
+      for (int i = 0; i < NE; i++) acc[i] = C2<T>{(T)0, (T)0};
+      const int tlo = (h + N2 - 1) / N2;  // low rows: kernel rows n1 N2 + n2 < h
+      for (int n1 = 0; n1 < tlo; n1++) {
+        const C2<T> w = w1[n1];
+#pragma unroll
+        for (int i = 0; i < NE; i++) {
+          const int n2 = g + G * i, j = n1 * N2 + n2;
+          if (j < h) acc[i] = cadd(acc[i], cmul(Kx[(long)j * pitch + col0 + c], w));
+        }
+      }
+      // high rows: kernel rows >= Ny - h, in the last thi values of n1 (increasing)
+      const int thi = (h + N2 - 1) / N2 + 1;
+      for (int t = 0; t < thi; t++) {
+        const int n1 = N1 - thi + t;
+        if (n1 < 0) continue;
+        const C2<T> w = w1[n1];
+#pragma unroll
+        for (int i = 0; i < NE; i++) {
+          const int n2 = g + G * i;
+          const long jr = (long)n1 * N2 + n2;  // kernel row
+          if (jr >= (long)Ny - h && jr < Ny && (n1 > 0 || jr >= h))
+            acc[i] = cadd(acc[i], cmul(Kx[(jr - (Ny - 2L * h)) * pitch + col0 + c], w));
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < NE; i++) {
+        const int n2 = g + G * i;
+        a[n2 * CW + c] = cmul(acc[i], w2[n2]);
+      }
     }
   }
   __syncthreads();
@@ -514,6 +613,32 @@ __global__ void k_multiply(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ F
 template <typename T, typename Loader>
 static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, int nrows, void* out) {
   if (nrows <= 0) return;
+  {
+    using K3 = void (*)(Loader, C2<T>*, long, const C2<T>*);
+    K3 k3 = nullptr;
+    int J = 0;
+    // FP32 and FP64 only: the float-float forward pass runs once per map, and its register
+    // kernels would double the float-float units' compile time
+    if constexpr (!std::is_same<T, ff>::value) {
+      switch (p.M) {
+        case 5000: k3 = k_rows_r2c3<T, 8, 25, 25, Loader>; J = 625; break;
+        case 4096: k3 = k_rows_r2c3<T, 16, 16, 16, Loader>; J = 256; break;
+        case 2000: k3 = k_rows_r2c3<T, 8, 10, 25, Loader>; J = 250; break;
+        case 1000: k3 = k_rows_r2c3<T, 10, 10, 10, Loader>; J = 100; break;
+        default: break;
+      }
+    }
+    if (k3) {
+      const size_t smem3 = ((size_t)p.M + J) * sizeof(C2<T>);
+      set_max_smem((const void*)k3, smem3);
+      {
+        MLC_KSCOPE(ctx, "fft_rows_r2c");
+        k3<<<nrows, 256, smem3, ctx->stream>>>(ld, (C2<T>*)out, p.Wp, (const C2<T>*)p.twx);
+      }
+      MLC_CHECK_LAUNCH();
+      return;
+    }
+  }
   size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
   auto kern = k_rows_r2c<T, Loader>;
   set_max_smem((const void*)kern, smem);
