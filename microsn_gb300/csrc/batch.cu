@@ -37,6 +37,10 @@ struct BatchIO {
   // second compute stream: the odd profiles' P0-P2 run on it, beside the even ones'
   cudaStream_t aux = nullptr;
   cudaEvent_t spec_ready = nullptr, aux_done = nullptr;
+  // third compute stream: the last pass of a group's first eight profiles, beside the
+  // remaining profiles' P0-P2
+  cudaStream_t tail = nullptr;
+  cudaEvent_t half_main = nullptr, half_aux = nullptr, half_done = nullptr;
   cudaEvent_t pix_free = nullptr;  // compute: the forward transform has read the map pixels
   cudaEvent_t pix_in = nullptr;    // h2d: pixels uploaded
   cudaEvent_t h2d_last = nullptr, d2h_last = nullptr;
@@ -75,8 +79,12 @@ static BatchIO* batch_get(mlc_ctx* ctx) {
   MLC_CUDA(cudaStreamCreateWithFlags(&b->d2h, cudaStreamNonBlocking));
   MLC_CUDA(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
   MLC_CUDA(cudaStreamCreateWithFlags(&b->aux, cudaStreamNonBlocking));
+  MLC_CUDA(cudaStreamCreateWithFlags(&b->tail, cudaStreamNonBlocking));
   ev_create(&b->spec_ready);
   ev_create(&b->aux_done);
+  ev_create(&b->half_main);
+  ev_create(&b->half_aux);
+  ev_create(&b->half_done);
   ev_create(&b->pix_free);
   ev_create(&b->pix_in);
   ev_create(&b->h2d_last);
@@ -96,6 +104,7 @@ static BatchIO* batch_get(mlc_ctx* ctx) {
 static void sync_all(mlc_ctx* ctx, BatchIO* b) {
   MLC_CUDA(cudaStreamSynchronize(ctx->stream));
   MLC_CUDA(cudaStreamSynchronize(b->aux));
+  MLC_CUDA(cudaStreamSynchronize(b->tail));
   MLC_CUDA(cudaStreamSynchronize(b->h2d));
   MLC_CUDA(cudaStreamSynchronize(b->d2h));
 }
@@ -124,9 +133,12 @@ void batch_release(mlc_ctx* ctx) {
       if (e) cudaEventDestroy(e);
   }
   if (b->aux) cudaStreamSynchronize(b->aux);
-  for (cudaEvent_t e : {b->pix_free, b->pix_in, b->h2d_last, b->d2h_last, b->spec_ready, b->aux_done})
+  if (b->tail) cudaStreamSynchronize(b->tail);
+  for (cudaEvent_t e : {b->pix_free, b->pix_in, b->h2d_last, b->d2h_last, b->spec_ready, b->aux_done, b->half_main,
+                        b->half_aux, b->half_done})
     if (e) cudaEventDestroy(e);
   if (b->aux) cudaStreamDestroy(b->aux);
+  if (b->tail) cudaStreamDestroy(b->tail);
   if (b->prof_dev) cudaFree(b->prof_dev);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->cap) cudaStreamDestroy(b->cap);
@@ -322,6 +334,11 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     // the odd profiles' P0-P2 on the second stream, after the map spectrum (not under the
     // per-kernel timing, whose event pairs would then span the other stream's kernels)
     const bool two = fuse_il && !ctx->timing;
+    // with more than eight profiles, the first eight's last pass (the first 32-byte sector of
+    // every 64-byte pixel, so its stores still fill whole sectors) starts on a third stream
+    // as soon as both chains are past them
+    const bool split = two && stride == 16 && nm > 8;
+    const long spec_stride = (long)(slot / (2 * es));
     if (two) {
       MLC_CUDA(cudaEventRecord(b->spec_ready, ctx->stream));
       MLC_CUDA(cudaStreamWaitEvent(b->aux, b->spec_ready, 0));
@@ -352,14 +369,36 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
       } else {
         conv_plain(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
       }
+      if (split && q == 7) {
+        MLC_CUDA(cudaEventRecord(b->half_main, ctx->stream));
+        MLC_CUDA(cudaEventRecord(b->half_aux, b->aux));
+        MLC_CUDA(cudaStreamWaitEvent(b->tail, b->half_main, 0));
+        MLC_CUDA(cudaStreamWaitEvent(b->tail, b->half_aux, 0));
+        cudaStream_t main = ctx->stream;
+        ctx->stream = b->tail;
+        try {
+          rows_c2r_interleave(ctx, *p, maps, spec_stride, 8, stride, imap, planar & 0xFFu);
+        } catch (...) {
+          ctx->stream = main;
+          throw;
+        }
+        ctx->stream = main;
+        MLC_CUDA(cudaEventRecord(b->half_done, b->tail));
+      }
     }
     if (two) {  // the last pass needs both chains
       MLC_CUDA(cudaEventRecord(b->aux_done, b->aux));
       MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->aux_done, 0));
     }
     if (ntr == 0) continue;
-    if (fuse_il) rows_c2r_interleave(ctx, *p, maps, (long)(slot / (2 * es)), nm, stride, imap, planar);
-    else interleave(ctx, mp, nm, npix, map->prec, stride, imap);
+    if (split) {
+      MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->half_done, 0));
+      rows_c2r_interleave(ctx, *p, maps + 8 * slot, spec_stride, nm - 8, stride, (char*)imap + 8 * es, planar >> 8);
+    } else if (fuse_il) {
+      rows_c2r_interleave(ctx, *p, maps, spec_stride, nm, stride, imap, planar);
+    } else {
+      interleave(ctx, mp, nm, npix, map->prec, stride, imap);
+    }
     if (!host) {
       sample_tracks_il(ctx, imap, stride, nm, Nx, Ny, map->prec, ntr, x0, y0, phi, v, off, t, mag,
                        (char*)out + (size_t)g0 * E * es, (long)E, 0);
