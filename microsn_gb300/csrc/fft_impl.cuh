@@ -451,9 +451,12 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
 // DFT^-1_L2 over k2, twiddle W_N2^-(k1 n2), transpose, thread (n2, c) DFT^-1_L1 over k1 ->
 // rows n2 + L2 n1, times W_Ny^-(n kk), stored.  (Staging the map-spectrum tile in shared
 // memory with cp.async made this kernel 3 % faster alone but the two-chain step 3 % slower:
-// the extra 12.8 KB per CTA crowds out the other chain's P2 CTAs.)
+// the extra 12.8 KB per CTA crowds out the other chain's P2 CTAs.)  The FP32 kernels of at
+// most 160 threads are held to 40 registers (ten CTAs per SM instead of seven for 10 x 10,
+// 8 bytes of spills): this pass waits on latency, and the extra CTAs hide more of it
+// (4.31 -> 4.13 ms per 16 profiles at 10000^2).
 template <typename T, int CW, int L1, int L2>
-__global__ void __launch_bounds__(256) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
+__global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) ? 6 : 0) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
                                                      long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
                                                      int N1, const C2<T>* __restrict__ twy, T scale) {
   constexpr int N2 = L1 * L2;
