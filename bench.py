@@ -776,6 +776,7 @@ def algorithmic_bytes(name, n, E, nprof, e=4):
     real = n * n * e
     table = {
         "fft_rows_r2c": real + spec,           # read a real map, write its row spectra
+        "fft_profile_rows": None,              # a profile's 2h rows: L2-resident, a few MB
         "fft_rows_c2r": spec + real,           # read row spectra, write a real map
         "fft_col_A": 2 * spec,                 # in-place column sub-pass: read + write
         "fft_col_B": 2 * spec,

@@ -616,6 +616,8 @@ __global__ void k_multiply(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ F
 template <typename T, typename Loader>
 static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, int nrows, void* out) {
   if (nrows <= 0) return;
+  // the profile's 2h rows (P0) timed apart from the map's rows
+  const char* name = std::is_same<Loader, ProfileRows<T>>::value ? "fft_profile_rows" : "fft_rows_r2c";
   {
     using K3 = void (*)(Loader, C2<T>*, long, const C2<T>*);
     K3 k3 = nullptr;
@@ -635,7 +637,7 @@ static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, 
       const size_t smem3 = ((size_t)p.M + J) * sizeof(C2<T>);
       set_max_smem((const void*)k3, smem3);
       {
-        MLC_KSCOPE(ctx, "fft_rows_r2c");
+        MLC_KSCOPE(ctx, name);
         k3<<<nrows, 256, smem3, ctx->stream>>>(ld, (C2<T>*)out, p.Wp, (const C2<T>*)p.twx);
       }
       MLC_CHECK_LAUNCH();
@@ -646,7 +648,7 @@ static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, 
   auto kern = k_rows_r2c<T, Loader>;
   set_max_smem((const void*)kern, smem);
   {
-    MLC_KSCOPE(ctx, "fft_rows_r2c");
+    MLC_KSCOPE(ctx, name);
     kern<<<nrows, 512, smem, ctx->stream>>>(ld, (C2<T>*)out, p.Wp, p.M, p.rlM, (const C2<T>*)p.twx);
   }
   MLC_CHECK_LAUNCH();
