@@ -470,7 +470,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
   const long col0 = (long)blockIdx.x * CW;
   const int c = threadIdx.x % CW, g = threadIdx.x / CW;
   // the map-spectrum tile (N2 rows of CW values, the only DRAM input) is needed in forward
-  // stage 2, after two L2 round trips and three barriers: start pulling it into L2 now
+  // stage 2, after two L2 round trips and four barriers: start pulling it into L2 now
   // (without registers or shared memory, which the other chain's P2 CTAs need)
   for (int n = threadIdx.x; n < N2; n += blockDim.x)
     asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + ((long)kk * N2 + n) * pitch + col0));
