@@ -76,7 +76,8 @@ def workload_config(args):
                 else f"profiling case {n}^2 x {nt} tracks (not the bench workload)", map=f"{n}x{n} ray-shot kappa*={KAPPA} gamma={GAMMA} width={WIDTH} R_E seed {MAP_SEED}",
                 profiles=f"{SHAPES} x rhalf {RHALF_PX} px", tracks=nt,
                 epochs=f"U{{{EPOCHS[0]}..{EPOCHS[1]}}} in {SEASONS} seasons", velocity_px_per_day=list(V_RANGE),
-                l2="inputs larger than L2: every map is 400 MB (FP32), L2 is 129 MB", n=n)
+                l2=(f"inputs larger than L2: every map is {n * n * 4 / 1e6:.0f} MB (FP32), L2 is 129 MB"
+                    if n * n * 4 > 129e6 else f"maps of {n * n * 4 / 1e6:.0f} MB (FP32) fit in the 129 MB L2"), n=n)
 
 
 # ----------------------------------------------------------------------------- tracks on the device
