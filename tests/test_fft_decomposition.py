@@ -1,0 +1,83 @@
+"""The register-level row transforms' decompositions, restated in numpy on the CPU.
+
+`k_rows_r2c3` (forward) and `c2r3_row` (inverse) in csrc/fft_impl.cuh split a row of
+M = L1 L2 L3 complex points (J = L2 L3) into three register levels:
+  level 1, item j < J:        z[J a + j] (a < L1), DFT_L1 over a, twiddle W_M^(j k1)
+  level 2, item (k1, m < L3): DFT_L2 over b of s[k1 J + L3 b + m], twiddle W_J^(m k2)
+  level 3, item (k1, k2):     DFT_L3 over m -> Z[k1 + L1 (k2 + L2 k3)]
+with the twiddles read from the row's Nx-entry table exp(-2 pi i e / Nx) at e = 2 j k1
+and e = 2 L1 m k2.  These tests run exactly that index arithmetic with numpy DFTs and
+compare it, and the split into Nx/2 + 1 spectrum values (and its inverse), with numpy's
+FFT for every row length that has a register kernel.  The GPU tests check the kernels.
+"""
+import numpy as np
+import pytest
+
+SIZES = [(8, 25, 25), (16, 16, 16), (8, 10, 25), (10, 10, 10)]  # M = 5000, 4096, 2000, 1000
+
+
+def _dft(x, inv=False):
+    return np.fft.ifft(x, axis=-1) * x.shape[-1] if inv else np.fft.fft(x, axis=-1)
+
+
+def three_level(z, L1, L2, L3, twx, inv=False):
+    """The three register levels over one row z (length M), in the kernels' index order."""
+    J, M = L2 * L3, L1 * L2 * L3
+    conj = np.conj if inv else (lambda v: v)
+    s = np.empty(M, complex)
+    for j in range(J):  # level 1
+        v = _dft(z[J * np.arange(L1) + j], inv)
+        for k1 in range(L1):
+            s[k1 * J + j] = v[k1] * conj(twx[2 * j * k1])
+    wJ = twx[2 * L1 * np.arange(J)]
+    t = np.empty(M, complex)
+    for k1 in range(L1):  # level 2
+        for m in range(L3):
+            u = _dft(s[k1 * J + L3 * np.arange(L2) + m], inv)
+            for k2 in range(L2):
+                t[k1 * J + k2 * L3 + m] = u[k2] * conj(wJ[m * k2])
+    out = np.empty(M, complex)
+    for k2 in range(L2):  # level 3
+        for k1 in range(L1):
+            w = _dft(t[k1 * J + k2 * L3 + np.arange(L3)], inv)
+            for k3 in range(L3):
+                out[k1 + L1 * (k2 + L2 * k3)] = w[k3]
+    return out
+
+
+def r2c_split(Z, twx):
+    """X[k] = (Z[k] + conj Z[M-k]) / 2 - i W^k (Z[k] - conj Z[M-k]) / 2, k <= M."""
+    M = Z.shape[0]
+    k = np.arange(M + 1)
+    zk, zc = Z[k % M], np.conj(Z[(M - k) % M])
+    return 0.5 * (zk + zc) - 0.5j * twx[k] * (zk - zc)
+
+
+@pytest.mark.parametrize("L1,L2,L3", SIZES)
+def test_forward_row_decomposition_matches_rfft(L1, L2, L3):
+    M = L1 * L2 * L3
+    Nx = 2 * M
+    twx = np.exp(-2j * np.pi * np.arange(Nx) / Nx)
+    x = np.random.default_rng(M).lognormal(0.0, 0.5, Nx)
+    Z = three_level(x[0::2] + 1j * x[1::2], L1, L2, L3, twx)
+    np.testing.assert_allclose(Z, np.fft.fft(x[0::2] + 1j * x[1::2]), rtol=0, atol=1e-9 * np.abs(x).sum())
+    X = r2c_split(Z, twx)
+    np.testing.assert_allclose(X, np.fft.rfft(x), rtol=0, atol=1e-9 * np.abs(x).sum())
+
+
+@pytest.mark.parametrize("L1,L2,L3", SIZES)
+def test_inverse_row_decomposition_matches_irfft(L1, L2, L3):
+    """c2r3_row: b[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W^-k, the three levels
+    inverted (conjugate twiddles), real row (z.re, z.im) interleaved, unnormalised."""
+    M = L1 * L2 * L3
+    Nx = 2 * M
+    twx = np.exp(-2j * np.pi * np.arange(Nx) / Nx)
+    x = np.random.default_rng(M + 1).lognormal(0.0, 0.5, Nx)
+    X = np.fft.rfft(x)
+    k = np.arange(M)
+    xk, xm = X[k], np.conj(X[M - k])
+    b = (xk + xm) + 1j * (xk - xm) * np.conj(twx[k])
+    z = three_level(b, L1, L2, L3, twx, inv=True)
+    row = np.empty(Nx)
+    row[0::2], row[1::2] = z.real, z.imag
+    np.testing.assert_allclose(row, Nx * x, rtol=0, atol=1e-9 * Nx * np.abs(x).sum())
