@@ -8,7 +8,11 @@ M = L1 L2 L3 complex points (J = L2 L3) into three register levels:
 with the twiddles read from the row's Nx-entry table exp(-2 pi i e / Nx) at e = 2 j k1
 and e = 2 L1 m k2.  These tests run exactly that index arithmetic with numpy DFTs and
 compare it, and the split into Nx/2 + 1 spectrum values (and its inverse), with numpy's
-FFT for every row length that has a register kernel.  The GPU tests check the kernels.
+FFT for every row length that has a register kernel.  The fused convolution (P0-P3) is
+restated the same way: the map's column passes A and B leaving the spectrum in the
+digit-transposed row order, P1's profile column sub-pass per kk (the two-term form for
+profiles of at most 2 N2 rows and the general loop), and P2, against the oracle's FFT
+convolution.  The GPU tests check the kernels themselves.
 """
 import numpy as np
 import pytest
@@ -81,3 +85,73 @@ def test_inverse_row_decomposition_matches_irfft(L1, L2, L3):
     row = np.empty(Nx)
     row[0::2], row[1::2] = z.real, z.imag
     np.testing.assert_allclose(row, Nx * x, rtol=0, atol=1e-9 * Nx * np.abs(x).sum())
+
+
+def _profile_rows(prof, Ny, Nx):
+    """ProfileRows: the 2h non-zero rows of the wrapped kernel, compacted (rows j < h are
+    kernel rows j, rows j >= h kernel rows Ny - 2h + j), columns wrapped the same way."""
+    N = prof.shape[0]
+    h = N // 2
+    rows = np.zeros((2 * h, Nx))
+    for j in range(2 * h):
+        pr = h + j if j < h else j - h
+        rows[j, :h] = prof[pr, h:]
+        rows[j, Nx - h:] = prof[pr, :h]
+    return rows
+
+
+def fused_convolution(mp, prof, N1, N2):
+    """P0-P3 of the fused convolution in the kernels' order, with the spectrum rows in the
+    digit-transposed order (row k1 N2 + k2 holds column frequency k1 + N1 k2)."""
+    Ny, Nx = mp.shape
+    assert Ny == N1 * N2
+    Wy = lambda e: np.exp(-2j * np.pi * np.asarray(e) / Ny)
+    h = prof.shape[0] // 2
+    # map forward: rows, column pass A (length N1 over rows n1 N2 + n2, twiddle W^(n2 k1)),
+    # column pass B (length N2 over the block of k1)
+    R = np.fft.rfft(mp, axis=1)
+    spec = np.empty_like(R)
+    for n2 in range(N2):
+        a = np.fft.fft(R[n2::N2], axis=0)  # rows n1 N2 + n2, n1 < N1 -> k1
+        spec[n2::N2] = a * Wy(n2 * np.arange(N1))[:, None]
+    for k1 in range(N1):
+        spec[k1 * N2:(k1 + 1) * N2] = np.fft.fft(spec[k1 * N2:(k1 + 1) * N2], axis=0)
+    # P0: the profile's 2h rows
+    kx = np.fft.rfft(_profile_rows(prof, Ny, Nx), axis=1)
+    out = np.empty_like(spec)
+    W1 = lambda e: np.exp(-2j * np.pi * np.asarray(e) / N1)
+    for kk in range(N1):
+        # P1, profile column sub-pass A at k1 = kk restricted to the non-zero rows
+        a = np.zeros((N2, kx.shape[1]), complex)
+        if h <= N2:  # the kernels' two-term form: low row n2 < h (weight 1), high row n2 >= N2 - h
+            for n2 in range(N2):
+                if n2 < h:
+                    a[n2] += kx[n2]
+                if n2 >= N2 - h:
+                    a[n2] += kx[n2 - (N2 - h) + h] * W1((N1 - 1) * kk)
+        else:
+            for j in range(2 * h):
+                r = j if j < h else Ny - 2 * h + j  # kernel row
+                a[r % N2] += kx[j] * W1((r // N2) * kk)
+        a *= Wy(np.arange(N2) * kk)[:, None]
+        K = np.fft.fft(a, axis=0)  # k2
+        P = K * spec[kk * N2:(kk + 1) * N2] / (Nx * Ny)
+        out[kk * N2:(kk + 1) * N2] = np.fft.ifft(P, axis=0) * N2 * np.conj(Wy(np.arange(N2) * kk))[:, None]
+    # P2: inverse column pass A (length N1 over k1 -> n1) per n2; P3: inverse rows
+    col = np.empty_like(out)
+    for n2 in range(N2):
+        col[n2::N2] = np.fft.ifft(out[n2::N2], axis=0) * N1
+    return np.fft.irfft(col, n=Nx, axis=1) * Nx
+
+
+@pytest.mark.parametrize("N", [6, 22])  # h = 3 <= N2 (two-term form) and h = 11 > N2 (general)
+def test_fused_convolution_decomposition_matches_oracle(N):
+    import oracle
+    N1, N2, Nx = 4, 10, 24
+    rng = np.random.default_rng(N)
+    mp = rng.lognormal(0.0, 0.5, (N1 * N2, Nx))
+    prof = rng.random((N, N))
+    prof /= prof.sum()
+    got = fused_convolution(mp, prof, N1, N2)
+    ref = oracle.conv_fft(mp, prof)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
