@@ -104,7 +104,7 @@ __device__ __forceinline__ uint16_t bf16_of_small_int(int v) {
   return (uint16_t)(__float_as_uint(f) >> 16);
 }
 
-// Per row: step exponent e = ceil(log2(rowmax / QMAX)) (clamped to [-100, 100]), integers
+// Per row: step exponent e = ceil(log2(rowmax / QMAX)) (clamped to [PD_EMIN, PD_EMAX]), integers
 // q = rint(v 2^-e) (|q| <= QMAX), split q = s0*65536 + s1*256 + s2 with balanced digits in
 // [-128, 127], slices written to the operand row [slice 0 | slice 1 | slice 2] (Kp = padded T
 // each, zeros beyond T), the exact squared norm sum q^2 and its float-float copy.  Rows
