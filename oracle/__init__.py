@@ -106,6 +106,10 @@ def lib():
 
 
 def ref_available() -> bool:
+    """The reference's CPU code is here: compiled on first use where its sources exist (a
+    failed build raises instead of skipping the tests that pin the oracle to it)."""
+    if not os.path.exists(REF_PATH) and os.path.isdir(REFERENCE_SRC):
+        build()
     return os.path.exists(REF_PATH)
 
 
