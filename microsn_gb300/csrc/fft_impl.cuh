@@ -80,10 +80,12 @@ __global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__
 //   level 2, item (k1, m < L3): DFT_L2 over b of s[k1 J + L3 b + m], twiddle W_J^(m k2)
 //                                                                      -> s[k1 J + k2 L3 + m]
 //   level 3, item (k1, k2):     DFT_L3 over m                      -> Z[k1 + L1 (k2 + L2 k3)]
-// then the split into Nx/2+1 spectrum values and the zero padding up to Wp.  Four CTAs per
-// SM (three for 16^3, whose 80 registers would spill at 64), like k_rows_c2r3.
+// then the split into Nx/2+1 spectrum values and the zero padding up to Wp.  FP32: four
+// CTAs per SM (three for 16^3, whose 80 registers would spill at 64), like k_rows_c2r3;
+// FP64 keeps the compiler's allocation (its 90 KB rows fit two CTAs per SM anyway).
 template <typename T, int L1, int L2, int L3, typename Loader>
-__global__ void __launch_bounds__(256, L1 == 16 ? 3 : 4) k_rows_r2c3(Loader ld, C2<T>* __restrict__ out, long pitch,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? (L1 == 16 ? 3 : 4) : 0)
+    k_rows_r2c3(Loader ld, C2<T>* __restrict__ out, long pitch,
                                                    const C2<T>* __restrict__ twx) {
   constexpr int J = L2 * L3, M = L1 * J;
   extern __shared__ __align__(16) unsigned char smem_raw[];
