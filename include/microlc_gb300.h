@@ -137,13 +137,19 @@ int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map);
  * rewritten through mlc_map_data). */
 int mlc_map_refresh(mlc_ctx* ctx, mlc_map* map);
 
-/* Arithmetic of an FP64 map's Fourier transforms (no reference counterpart).  GB300 runs
- * FP64 at a small fraction of its FP32 rate; with MLC_FFT_F32X2 the map's forward
- * transform and its fused convolutions run in float-float arithmetic (pairs of FP32
- * values, about 48 significant bits: convolved maps within about 1e-13 relative of FP64
- * transforms) while pixels, convolved maps, light curves and everything after them stay
- * FP64.  The plain form (MLC_CONV_PLAIN) keeps native FP64 and refuses such a map.
- * Changing the mode drops the cached spectrum.  FP32 maps accept MLC_FFT_NATIVE only. */
+/* Arithmetic of a map's Fourier transforms (no reference counterpart).  With
+ * MLC_FFT_F32X2 the map's forward transform and its fused convolutions run in float-float
+ * arithmetic (pairs of FP32 values, about 48 significant bits) while pixels, convolved
+ * maps, light curves and everything after them keep the map's precision.
+ *  - FP64 maps: GB300 runs FP64 at a small fraction of its FP32 rate; float-float
+ *    transforms give convolved maps within about 1e-13 relative of FP64 transforms.
+ *  - FP32 maps: FP32 transforms carry an absolute error of a few 1e-7 of the map's rms,
+ *    which is up to ~1e-5 relative in the faint pixels of a ray-shot map and moves the
+ *    offset-minimised chi2 of a light curve by up to ~3e-4 relative; float-float transforms
+ *    leave only the FP32 rounding of the convolved pixels (about 1e-7 relative).  The
+ *    spectrum takes 16 bytes per complex value instead of 8.
+ * The plain form (MLC_CONV_PLAIN) keeps the map's own precision and refuses such a map;
+ * the direct tiled form is not used for it.  Changing the mode drops the cached spectrum. */
 #define MLC_FFT_NATIVE 0
 #define MLC_FFT_F32X2 1
 int mlc_map_set_fft(mlc_map* map, int mode);
@@ -453,16 +459,17 @@ int mlc_histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double l
 
 /* The histogram above without any device allocation.  No counterpart in the reference
  * (its binning allocates with thrust on every call).  For callers that cannot allocate
- * device memory -- inside a framework that owns the whole device pool, in plugins or
- * callbacks that may only use memory they are given, or in call sequences later replayed
- * from a captured stream.  The per-bin counters live in a fixed array compiled into the
+ * device memory -- code running inside a framework that has reserved the whole device pool
+ * for its own allocator, and plugins or callbacks that may only use the buffers they are
+ * handed.  The per-bin counters live in a fixed array compiled into the
  * library (96 KB on every device that loads it, held until the process exits), so no
  * cudaMalloc, cudaFree or allocating library routine is called.  nbins is limited to
  * 12000; larger requests return MLC_ERR_LIMIT.  The first call on a device resolves the
  * array's device address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  Every call clears the counters it uses, but all calls
  * on a device share the one array: calls that overlap on the GPU (other streams, other
- * contexts, other host threads) race and must be serialised by the caller. */
+ * contexts, other host threads) race and must be serialised by the caller.  The call copies
+ * the counts to counts_host and waits for its stream before it returns. */
 int mlc_histogram_f64_noalloc(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, double hi, int logscale,
                               uint64_t* counts_host);
 

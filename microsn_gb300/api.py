@@ -190,7 +190,8 @@ class Map:
         self.ctx.check(self.ctx.L.mlc_map_prepare(self.ctx.h, self.h))
 
     def set_fft(self, mode: str):
-        """Transforms of an FP64 map in "native" FP64 or "f32x2" (float-float) arithmetic."""
+        """Transforms in the map's own precision ("native") or in float-float arithmetic ("f32x2");
+        pixels and outputs keep the map's precision either way."""
         self.ctx.check(self.ctx.L.mlc_map_set_fft(self.h, {"native": 0, "f32x2": 1}[mode]))
 
     def refresh(self):

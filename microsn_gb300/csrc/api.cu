@@ -297,7 +297,7 @@ extern "C++" {
 void mlc::map_prepare(mlc_ctx* ctx, mlc_map* map) {
   if (map->spec_valid) return;
   FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map_fft_prec(map));
-  if (!map->spec) MLC_CUDA(cudaMalloc(&map->spec, p->spec_bytes()));
+  map_spec_buffer(map, p->spec_bytes());
   fft2_forward(ctx, *p, map->data, map->prec, map->spec);
   map->spec_valid = true;
 }
@@ -311,11 +311,9 @@ int mlc_map_prepare(mlc_ctx* ctx, mlc_map* map) {
 int mlc_map_set_fft(mlc_map* map, int mode) {
   if (!map) return MLC_ERR_ARG;
   if (mode != MLC_FFT_NATIVE && mode != MLC_FFT_F32X2) return fail(map->ctx, MLC_ERR_ARG, "unknown FFT mode");
-  if (mode == MLC_FFT_F32X2 && map->prec != MLC_F64)
-    return fail(map->ctx, MLC_ERR_ARG, "float-float transforms are for FP64 maps");
   if (map->fft != mode) {
     map->fft = mode;
-    map->spec_valid = false;  // the spectrum's element type changes (same size)
+    map->spec_valid = false;  // the spectrum's element type changes (and for FP32 maps its size)
   }
   return MLC_OK;
 }

@@ -262,7 +262,7 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     map->spec_valid = false;
   }
   if (!map->spec_valid) {
-    if (!map->spec) MLC_CUDA(cudaMalloc(&map->spec, p->spec_bytes()));
+    map_spec_buffer(map, p->spec_bytes());
     fft2_forward(ctx, *p, map->data, map->prec, map->spec);
     map->spec_valid = true;
   }
@@ -338,7 +338,9 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     // every 64-byte pixel, so its stores still fill whole sectors) starts on a third stream
     // as soon as both chains are past them
     const bool split = two && stride == 16 && nm > 8;
-    const long spec_stride = (long)(slot / (2 * es));
+    // slot stride in spectrum elements (C2 of the transform's type: 16 bytes for float-float
+    // spectra, also of FP32 maps) -- a planar slot is read through the same pointer type
+    const long spec_stride = (long)(slot / p->elem);
     if (two) {
       MLC_CUDA(cudaEventRecord(b->spec_ready, ctx->stream));
       MLC_CUDA(cudaStreamWaitEvent(b->aux, b->spec_ready, 0));

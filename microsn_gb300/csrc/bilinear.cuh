@@ -50,4 +50,122 @@ __device__ __forceinline__ Bilin<T> bilin_weights(long bx, T fx, long by, T fy, 
   return B;
 }
 
+// sin and cos of an FP32 angle as float-float pairs, our own evaluation: Cody-Waite
+// reduction by pi/2 (split into P1 + P2 + P3, the first two of 12 significant bits so that
+// k P1 and k P2 are exact products; every step a float-float sum), then the Taylor series of
+// sin and cos on |r| <= pi/4 (nine and ten terms, the first omitted term below 1e-16), in
+// float-float arithmetic.  About 1e-14 absolute for |phi| < 2^12 pi/2; larger angles take
+// the FP32 library values (about 1e-7).
+__device__ __forceinline__ void sincos_ff(float phi, ff* sn, ff* cs) {
+  if (!(fabsf(phi) < 6433.0f)) {
+    float s_, c_;
+    sincosf(phi, &s_, &c_);
+    *sn = ff(s_, 0.f);
+    *cs = ff(c_, 0.f);
+    return;
+  }
+  const float kf = rintf(__fmul_rn(phi, 0.636619772367581343f));  // nearest multiple of pi/2
+  const float P1 = 1.5703125f, P2 = 4.837512969970703125e-4f, P3 = 7.549790126404332e-08f;
+  const float kp3 = __fmul_rn(kf, P3);
+  ff r = ff(phi, 0.f) - ff(__fmul_rn(kf, P1), 0.f);  // k P1, k P2: exact products
+  r = r - ff(__fmul_rn(kf, P2), 0.f);
+  r = r - ff(kp3, __fmaf_rn(kf, P3, -kp3));            // k P3 as an exact two-product
+  r = ff_norm(r);
+  const ff z = r * r;
+  // sin r = r (1 - z/3! + z^2/5! - ...), cos r = 1 - z/2! + z^2/4! - ...: the
+  // coefficients (-1)^n / (2n+1)! and (-1)^n / (2n)! as float-float pairs
+  ff p = ff(2.8114573589663704e-15f, -1.0462084739763658e-22f);  // 1/17!
+  p = ff(-7.647163609812713e-13f, -1.2200710471178288e-20f) + z * p;
+  p = ff(1.6059044372074283e-10f, -5.352526511562726e-18f) + z * p;
+  p = ff(-2.5052107943679403e-08f, -4.4176230446483665e-16f) + z * p;
+  p = ff(2.7557318844628753e-06f, 3.793571224297229e-14f) + z * p;
+  p = ff(-0.00019841270113829523f, 2.725596874933456e-12f) + z * p;
+  p = ff(0.008333333767950535f, -4.34617203337595e-10f) + z * p;
+  p = ff(-0.1666666716337204f, 4.967053879312289e-09f) + z * p;  // -1/3!
+  p = ff(1.0f, 0.f) + z * p;
+  const ff s = ff_norm(r * p);
+  ff q = ff(-1.5619206814541513e-16f, -1.5404471465941993e-24f);  // -1/18!
+  q = ff(4.7794772561329454e-14f, 7.62544404448643e-22f) + z * q;
+  q = ff(-1.147074536050896e-11f, -2.372207689231238e-19f) + z * q;
+  q = ff(2.0876755879584152e-09f, 1.1082839147459852e-16f) + z * q;
+  q = ff(-2.755731998149713e-07f, 7.575112209051195e-15f) + z * q;
+  q = ff(2.4801587642286904e-05f, -3.40699609366682e-13f) + z * q;
+  q = ff(-0.0013888889225199819f, 3.3631094437103215e-11f) + z * q;
+  q = ff(0.0416666679084301f, -1.2417634698280722e-09f) + z * q;
+  q = ff(-0.5f, 0.f) + z * q;
+  q = ff(1.0f, 0.f) + z * q;
+  const ff c = ff_norm(q);
+  switch (((int)kf) & 3) {
+    case 0: *sn = s; *cs = c; break;
+    case 1: *sn = c; *cs = -s; break;
+    case 2: *sn = -s; *cs = -c; break;
+    default: *sn = -c; *cs = s; break;
+  }
+}
+
+// Offset f0 + V t c of a track epoch from the track's pixel base, returned as whole pixels
+// *d and a fraction in [0, 1) rounded to FP32 (6e-8 px).  The displacement V t c runs to
+// thousands of pixels, where an FP32 sum would be off by up to 5e-4 px: V t is formed
+// exactly (FMA two-product) and the sum in float-float arithmetic.
+__device__ __forceinline__ float track_offset(float f0, float V, float t, ff c, long* d) {
+  const float vh = __fmul_rn(V, t);
+  const ff x = ff(f0, 0.f) + ff(vh, __fmaf_rn(V, t, -vh)) * c;
+  const float fl = floorf(x.hi);
+  float r = __fadd_rn(__fsub_rn(x.hi, fl), x.lo);
+  long dd = (long)fl;
+  if (r < 0.f) {
+    r = __fadd_rn(r, 1.f);
+    dd -= 1;
+  } else if (r >= 1.f) {
+    r = __fsub_rn(r, 1.f);
+    dd += 1;
+  }
+  *d = dd;
+  return r;
+}
+
+// A straight track x0 + V t (cos phi, sin phi): the bilinear weights at epoch t.  The start
+// is split into an exact integer pixel base and an offset in [0, 1).  FP64 tracks form the
+// position in FP64; FP32 tracks in float-float (sincos_ff, track_offset), so that FP32 light
+// curves are limited by the maps' FP32 values, not by the position arithmetic.
+template <typename T>
+struct TrackGeom;
+
+template <>
+struct TrackGeom<double> {
+  long bx, by;
+  double fx0, fy0, V, c, s;
+  __device__ __forceinline__ TrackGeom(double X0, double Y0, double phi, double V_) : V(V_) {
+    sincos(phi, &s, &c);
+    bx = (long)floor(X0);
+    by = (long)floor(Y0);
+    fx0 = X0 - (double)bx;
+    fy0 = Y0 - (double)by;
+  }
+  __device__ __forceinline__ Bilin<double> at(double t, int Nx, int Ny) const {
+    const double vt = V * t;
+    return bilin_weights<double>(bx, fx0 + vt * c, by, fy0 + vt * s, Nx, Ny);
+  }
+};
+
+template <>
+struct TrackGeom<float> {
+  long bx, by;
+  float fx0, fy0, V;
+  ff c, s;
+  __device__ __forceinline__ TrackGeom(float X0, float Y0, float phi, float V_) : V(V_) {
+    sincos_ff(phi, &s, &c);
+    bx = (long)floorf(X0);
+    by = (long)floorf(Y0);
+    fx0 = X0 - (float)bx;  // exact
+    fy0 = Y0 - (float)by;
+  }
+  __device__ __forceinline__ Bilin<float> at(float t, int Nx, int Ny) const {
+    long dx, dy;
+    const float rx = track_offset(fx0, V, t, c, &dx);
+    const float ry = track_offset(fy0, V, t, s, &dy);
+    return bilin_weights<float>(bx + dx, rx, by + dy, ry, Nx, Ny);
+  }
+};
+
 }  // namespace mlc

@@ -25,6 +25,7 @@
 // kernels and launch sequences are in fft_impl.cuh.
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <mutex>
 #include <unordered_map>
 
@@ -74,14 +75,19 @@ RadixList factor_radices(int L, int tw_stride) {
   return rl;
 }
 
+// The attribute belongs to the function on the current device: a process holding contexts
+// on several GPUs sets it once per (device, function).
 void set_max_smem(const void* func, size_t bytes) {
   static std::mutex mu;
-  static std::unordered_map<const void*, size_t> done;
+  static std::map<std::pair<int, const void*>, size_t> done;
+  int dev = 0;
+  MLC_CUDA(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> g(mu);
-  auto it = done.find(func);
+  const auto key = std::make_pair(dev, func);
+  auto it = done.find(key);
   if (it != done.end() && it->second >= bytes) return;
   MLC_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  done[func] = bytes;
+  done[key] = bytes;
 }
 
 FftPlan2D::~FftPlan2D() {
@@ -161,7 +167,7 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
   p->M = Nx / 2;
   p->Wc = Nx / 2 + 1;
   p->Wp = (int)round_up(p->Wc, 16);
-  p->elem = prec == MLC_F64 ? sizeof(C2<double>) : prec == PREC_FF ? sizeof(C2<ff>) : sizeof(C2<float>);
+  p->elem = prec == MLC_F64 ? sizeof(C2<double>) : prec_is_ff(prec) ? sizeof(C2<ff>) : sizeof(C2<float>);
   p->CW = prec == MLC_F32 ? 16 : 8;
   split_columns(Ny, p->N1, p->N2);
   p->rlM = factor_radices(p->M, 2);
@@ -176,7 +182,7 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
   if (prec == MLC_F64) {
     p->twx = upload_twiddles<double>(Nx);
     p->twy = upload_twiddles<double>(Ny);
-  } else if (prec == PREC_FF) {
+  } else if (prec_is_ff(prec)) {
     p->twx = upload_twiddles<ff>(Nx);
     p->twy = upload_twiddles<ff>(Ny);
   } else {
@@ -191,20 +197,24 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
 // ---------------------------------------------------------------- dispatch by precision
 
 void fft2_forward(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype, void* spec) {
-  if (p.prec == PREC_FF) forward_impl<ff>(ctx, p, in, in_dtype, spec);
+  if (prec_is_ff(p.prec)) forward_impl<ff>(ctx, p, in, in_dtype, spec);
   else if (p.prec == MLC_F64) forward_impl<double>(ctx, p, in, in_dtype, spec);
   else forward_impl<float>(ctx, p, in, in_dtype, spec);
 }
 
 void conv_fused(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
-  if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, out);
+  if (p.prec == PREC_FFS) {  // P0-P2 to the half-spectrum, then P3 into FP32 pixels
+    void* tmp = ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
+    conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, nullptr, tmp, WS_KX);
+    rows_c2r_impl<ff, float>(ctx, p, tmp, out);
+  } else if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, out);
   else if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, out);
   else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, out);
 }
 
 void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
                          void* spec_out, int kx_slot) {
-  if (p.prec == PREC_FF) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
+  if (prec_is_ff(p.prec)) conv_fused_impl<ff>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
   else if (p.prec == MLC_F64) conv_fused_impl<double>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
   else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
 }
@@ -215,13 +225,14 @@ bool rows_c2r_interleave_supported(const FftPlan2D& p) {
 
 bool rows_c2r_interleave(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
                          void* out, unsigned planar) {
+  if (p.prec == PREC_FFS) return c2r_interleave_impl<ff, float>(ctx, p, specs, spec_stride, nm, S, out, planar);
   if (p.prec == PREC_FF) return c2r_interleave_impl<ff>(ctx, p, specs, spec_stride, nm, S, out, planar);
   if (p.prec == MLC_F64) return c2r_interleave_impl<double>(ctx, p, specs, spec_stride, nm, S, out, planar);
   return c2r_interleave_impl<float>(ctx, p, specs, spec_stride, nm, S, out, planar);
 }
 
 void conv_plain(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out) {
-  MLC_REQUIRE(p.prec != PREC_FF, MLC_ERR_ARG, "the plain form runs native FP64 transforms (map in float-float mode)");
+  MLC_REQUIRE(!prec_is_ff(p.prec), MLC_ERR_ARG, "the plain form runs the map's own precision (map in float-float mode)");
   if (p.prec == MLC_F64) conv_plain_impl<double>(ctx, p, Fmap, prof, pN, out);
   else conv_plain_impl<float>(ctx, p, Fmap, prof, pN, out);
 }

@@ -6,6 +6,6 @@ namespace mlc {
 template void forward_impl<double>(mlc_ctx*, const FftPlan2D&, const void*, int, void*);
 template void conv_fused_impl<double>(mlc_ctx*, const FftPlan2D&, const void*, const double*, int, void*, void*, int);
 template void conv_plain_impl<double>(mlc_ctx*, const FftPlan2D&, const void*, const double*, int, void*);
-template bool c2r_interleave_impl<double>(mlc_ctx*, const FftPlan2D&, const void*, long, int, int, void*, unsigned);
+template bool c2r_interleave_impl<double, double>(mlc_ctx*, const FftPlan2D&, const void*, long, int, int, void*, unsigned);
 
 }  // namespace mlc

@@ -7,6 +7,6 @@
 namespace mlc {
 
 template void forward_impl<ff>(mlc_ctx*, const FftPlan2D&, const void*, int, void*);
-template bool c2r_interleave_impl<ff>(mlc_ctx*, const FftPlan2D&, const void*, long, int, int, void*, unsigned);
+template bool c2r_interleave_impl<ff, double>(mlc_ctx*, const FftPlan2D&, const void*, long, int, int, void*, unsigned);
 
 }  // namespace mlc

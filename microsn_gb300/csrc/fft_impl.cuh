@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(512) k_rows_r2c(Loader ld, C2<T>* __restrict__
   __syncthreads();
   C2<T>* Z = fft_smem<T, false, 1>(a, b, rl, twx);
   C2<T>* o = out + (long)row * pitch;
-  for (int k = threadIdx.x; k <= M; k += blockDim.x) o[k] = r2c_split(Z, M, twx, k);
+  for (int k = threadIdx.x; k <= M; k += blockDim.x) o[k] = cfin(r2c_split(Z, M, twx, k));
   for (int k = M + 1 + threadIdx.x; k < pitch; k += blockDim.x) o[k] = C2<T>{(T)0, (T)0};
 }
 
@@ -138,14 +138,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? (L1 == 16 ? 3 : 4) : 0)
   }
   __syncthreads();
   C2<T>* o = out + (long)row * pitch;
-  for (int k = tid; k <= M; k += blockDim.x) o[k] = r2c_split(s, M, twx, k);
+  for (int k = tid; k <= M; k += blockDim.x) o[k] = cfin(r2c_split(s, M, twx, k));
   for (int k = M + 1 + tid; k < pitch; k += blockDim.x) o[k] = C2<T>{(T)0, (T)0};
 }
 
 // Inverse real FFT (unnormalised, like cuFFT Z2D) of one spectrum row per CTA.
-template <typename T>
+template <typename T, typename TO>
 __global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, long pitch,
-                                                  typename RealOut<T>::type* __restrict__ out, long ldo, int M,
+                                                  TO* __restrict__ out, long ldo, int M,
                                                   RadixList rl, const C2<T>* __restrict__ twx) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);
@@ -163,9 +163,8 @@ __global__ void __launch_bounds__(512) k_rows_c2r(const C2<T>* __restrict__ in, 
   }
   __syncthreads();
   C2<T>* z = fft_smem<T, true, 1>(b, a, rl, twx);
-  using TO = typename RealOut<T>::type;
   C2<TO>* dst = reinterpret_cast<C2<TO>*>(out + (long)row * ldo);
-  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{RealOut<T>::cvt(z[n].x), RealOut<T>::cvt(z[n].y)};
+  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{out_cvt<TO>(z[n].x), out_cvt<TO>(z[n].y)};
 }
 
 // Inverse real FFT of one spectrum row per CTA with M = L1 L2 L3 (J = L2 L3) in three
@@ -238,18 +237,17 @@ __device__ __forceinline__ void c2r3_row(const C2<T>* __restrict__ a, const C2<T
   __syncthreads();
 }
 
-template <typename T, int L1, int L2, int L3>
+template <typename T, int L1, int L2, int L3, typename TO>
 __global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in, long pitch,
-                                                   typename RealOut<T>::type* __restrict__ out, long ldo,
+                                                   TO* __restrict__ out, long ldo,
                                                    const C2<T>* __restrict__ twx) {
   constexpr int M = L1 * L2 * L3;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
   const int row = blockIdx.x;
   c2r3_row<T, L1, L2, L3>(in + (long)row * pitch, twx, s);
-  using TO = typename RealOut<T>::type;
   C2<TO>* dst = reinterpret_cast<C2<TO>*>(out + (long)row * ldo);
-  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{RealOut<T>::cvt(s[n].x), RealOut<T>::cvt(s[n].y)};
+  for (int n = threadIdx.x; n < M; n += blockDim.x) dst[n] = C2<TO>{out_cvt<TO>(s[n].x), out_cvt<TO>(s[n].y)};
 }
 
 // P3 of four profiles with the interleave fused in.  A cluster of four CTAs takes one row
@@ -262,11 +260,10 @@ __global__ void __launch_bounds__(256) k_rows_c2r3(const C2<T>* __restrict__ in,
 // written back.  No planar maps and no separate interleave pass; the arithmetic is
 // k_rows_c2r3's.  (Measured at 10000^2, 16 profiles: clusters of 4 6.0 ms, of 8 6.1 ms,
 // of 2 or 1 (8- or 4-byte strided stores) 9.8 ms.)
-template <typename T, int L1, int L2, int L3>
+template <typename T, int L1, int L2, int L3, typename TO>
 __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
     k_rows_c2r3_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm,
-                   typename RealOut<T>::type* __restrict__ out, int S, const C2<T>* __restrict__ twx, unsigned planar) {
-  using TO = typename RealOut<T>::type;
+                   TO* __restrict__ out, int S, const C2<T>* __restrict__ twx, unsigned planar) {
   constexpr int J = L2 * L3, M = L1 * J, NX = 2 * M;
   namespace cg = cooperative_groups;
   cg::cluster_group cl = cg::this_cluster();
@@ -295,7 +292,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
     for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
       TO v[4];
 #pragma unroll
-      for (int r = 0; r < 4; r++) v[r] = RealOut<T>::cvt(src[r][x]);
+      for (int r = 0; r < 4; r++) v[r] = out_cvt<TO>(src[r][x]);
       float4* d = reinterpret_cast<float4*>(dst + (long)x * S);
       const float4* w = reinterpret_cast<const float4*>(v);
 #pragma unroll
@@ -304,7 +301,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
   } else {
     for (int r = 0; r < W; r++) {
       const T* sr = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
-      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = RealOut<T>::cvt(sr[x]);
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = out_cvt<TO>(sr[x]);
     }
   }
   // no CTA leaves while the others still read its shared memory.  Execution order is all
@@ -342,7 +339,7 @@ __global__ void __launch_bounds__(256) k_colpass(C2<T>* __restrict__ buf, long p
     int j = idx / CW, c = idx % CW;
     C2<T> v = r[idx];
     if (post_tw) v = INV ? cmulc(v, pw[j]) : cmul(v, pw[j]);
-    buf[(base + j * j_mul) * pitch + col0 + c] = v;
+    buf[(base + j * j_mul) * pitch + col0 + c] = cfin(v);
   }
 }
 
@@ -388,7 +385,7 @@ __global__ void __launch_bounds__(256) k_colpass2(C2<T>* __restrict__ buf, long 
       const int j = g + L1 * k2;
       C2<T> val = u[k2];
       if (post_tw) val = INV ? cmulc(val, pw[j]) : cmul(val, pw[j]);
-      buf[(base + (long)j * j_mul) * pitch + col0 + c] = val;
+      buf[(base + (long)j * j_mul) * pitch + col0 + c] = cfin(val);
     }
   }
 }
@@ -441,7 +438,7 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
   for (int idx = threadIdx.x; idx < N2 * CW; idx += blockDim.x) {
     const int n2 = idx / CW, c = idx % CW;
     C2<T> v = cmulc(U[idx], w2[n2]);
-    out[((long)k1 * N2 + n2) * pitch + col0 + c] = v;
+    out[((long)k1 * N2 + n2) * pitch + col0 + c] = cfin(v);
   }
 }
 
@@ -582,7 +579,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
 #pragma unroll
     for (int n1 = 0; n1 < L1; n1++) {
       const int n = g + L2 * n1;
-      out[((long)kk * N2 + n) * pitch + col0 + c] = cmulc(v[n1], w2[n]);
+      out[((long)kk * N2 + n) * pitch + col0 + c] = cfin(cmulc(v[n1], w2[n]));
     }
   }
 }
@@ -656,18 +653,17 @@ static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, 
   MLC_CHECK_LAUNCH();
 }
 
-template <typename T>
+template <typename T, typename TO = typename RealOut<T>::type>
 static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, void* out) {
   {
-    using TO = typename RealOut<T>::type;
     using K3 = void (*)(const C2<T>*, long, TO*, long, const C2<T>*);
     K3 k3 = nullptr;
     int J = 0;
     switch (p.M) {
-      case 5000: k3 = k_rows_c2r3<T, 8, 25, 25>; J = 625; break;
-      case 4096: k3 = k_rows_c2r3<T, 16, 16, 16>; J = 256; break;
-      case 2000: k3 = k_rows_c2r3<T, 8, 10, 25>; J = 250; break;
-      case 1000: k3 = k_rows_c2r3<T, 10, 10, 10>; J = 100; break;
+      case 5000: k3 = k_rows_c2r3<T, 8, 25, 25, TO>; J = 625; break;
+      case 4096: k3 = k_rows_c2r3<T, 16, 16, 16, TO>; J = 256; break;
+      case 2000: k3 = k_rows_c2r3<T, 8, 10, 25, TO>; J = 250; break;
+      case 1000: k3 = k_rows_c2r3<T, 10, 10, 10, TO>; J = 100; break;
       default: break;
     }
     if (k3) {
@@ -682,11 +678,11 @@ static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, vo
     }
   }
   size_t smem = 2 * (size_t)(p.M + 1) * sizeof(C2<T>);
-  auto kern = k_rows_c2r<T>;
+  auto kern = k_rows_c2r<T, TO>;
   set_max_smem((const void*)kern, smem);
   {
     MLC_KSCOPE(ctx, "fft_rows_c2r");
-    kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (typename RealOut<T>::type*)out, p.Nx, p.M, p.rlM,
+    kern<<<p.Ny, 512, smem, ctx->stream>>>((const C2<T>*)in, p.Wp, (TO*)out, p.Nx, p.M, p.rlM,
                                          (const C2<T>*)p.twx);
   }
   MLC_CHECK_LAUNCH();
@@ -836,18 +832,23 @@ void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const d
   launch_rows_c2r<T>(ctx, p, kspec, out);
 }
 
-template <typename T>
+// P3 alone: the inverse real row transform of a half-spectrum into a real map of TO.
+template <typename T, typename TO>
+void rows_c2r_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* spec, void* out) {
+  launch_rows_c2r<T, TO>(ctx, p, spec, out);
+}
+
+template <typename T, typename TO>
 bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
                          void* out, unsigned planar) {
-  using TO = typename RealOut<T>::type;
   using K = void (*)(const C2<T>*, long, long, int, TO*, int, const C2<T>*, unsigned);
   K k = nullptr;
   int J = 0;
   switch (p.M) {
-    case 5000: k = k_rows_c2r3_il<T, 8, 25, 25>; J = 625; break;
-    case 4096: k = k_rows_c2r3_il<T, 16, 16, 16>; J = 256; break;
-    case 2000: k = k_rows_c2r3_il<T, 8, 10, 25>; J = 250; break;
-    case 1000: k = k_rows_c2r3_il<T, 10, 10, 10>; J = 100; break;
+    case 5000: k = k_rows_c2r3_il<T, 8, 25, 25, TO>; J = 625; break;
+    case 4096: k = k_rows_c2r3_il<T, 16, 16, 16, TO>; J = 256; break;
+    case 2000: k = k_rows_c2r3_il<T, 8, 10, 25, TO>; J = 250; break;
+    case 1000: k = k_rows_c2r3_il<T, 10, 10, 10, TO>; J = 100; break;
     default: return false;
   }
   if (!rows_c2r_interleave_supported(p)) return false;

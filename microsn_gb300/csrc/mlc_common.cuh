@@ -40,14 +40,16 @@ struct alignas(2 * sizeof(T)) C2 {
   T x, y;
 };
 
-// Float-float number: hi + lo with |lo| <= ulp(hi)/2, about 48 significant bits.  GB300
-// issues FP32 about sixty times faster than FP64, and one float-float operation costs
-// 7 (product) to 11 (sum) FP32 operations, so FFTs of FP64 maps run several times faster
-// in it at about 1e-14 relative accuracy.  Every step uses explicitly rounded intrinsics
-// (no contraction or reassociation can break the error-free transforms).  The sum is the
-// two-sum of the high parts plus the low parts, renormalised (error below 2^-47 of
-// |a| + |b|: the bound the FFT's error analysis needs); the product is the FMA two-product
-// plus the cross terms.
+// Float-float number: hi + lo, about 48 significant bits.  GB300 issues FP32 about sixty
+// times faster than FP64, so FFTs run several times faster in it than in FP64 at about
+// 1e-14 relative accuracy.  Every step uses explicitly rounded intrinsics (no contraction or
+// reassociation can break the error-free transforms).  The sum is the two-sum of the high
+// parts plus the low parts (8 FP32 operations), the product the FMA two-product plus the
+// cross terms (4 operations).  Neither renormalises its result: the pair stays an exact
+// two-term representation, |lo| grows to at most a few ulp(hi) over a chain of butterflies,
+// and the error of every operation stays below a few 2^-47 of its operands' magnitude --
+// the bound the FFT's norm-wise error analysis needs.  ff_norm restores |lo| <= ulp(hi)/2
+// where a caller needs hi alone (divisions, values stored between passes).
 struct ff {
   float hi, lo;
   ff() = default;
@@ -60,12 +62,12 @@ __device__ __forceinline__ ff ff_renorm(float s, float e) {
   const float h = __fadd_rn(s, e);
   return ff(h, __fsub_rn(e, __fsub_rn(h, s)));
 }
+__device__ __forceinline__ ff ff_norm(ff a) { return ff_renorm(a.hi, a.lo); }
 __device__ __forceinline__ ff operator+(ff a, ff b) {
   const float s = __fadd_rn(a.hi, b.hi);
   const float bb = __fsub_rn(s, a.hi);
-  float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-  return ff_renorm(s, e);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return ff(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
 }
 __device__ __forceinline__ ff operator-(ff a) { return ff(-a.hi, -a.lo); }
 __device__ __forceinline__ ff operator-(ff a, ff b) { return a + (-b); }
@@ -74,18 +76,26 @@ __device__ __forceinline__ ff operator*(ff a, ff b) {
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
-  return ff_renorm(p, e);
+  return ff(p, e);
 }
 __device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
 __device__ __forceinline__ double ff_to_double(ff a) { return __dadd_rn((double)a.hi, (double)a.lo); }
 
-// a / b to float-float accuracy: the FP32 quotient, then one correction from the
-// float-float residual.
+// a / b to float-float accuracy: the FP32 quotient of the normalised operands, then one
+// correction from the float-float residual.
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
+  a = ff_norm(a);
+  b = ff_norm(b);
   const float q1 = __fdiv_rn(a.hi, b.hi);
-  const ff r = a - ff(q1, 0.f) * b;
+  const ff r = ff_norm(a - ff(q1, 0.f) * b);
   return ff_renorm(q1, __fdiv_rn(r.hi, b.hi));
 }
+
+// Values stored between passes are renormalised (3 operations per value) so that the low
+// parts cannot keep growing from pass to pass; FP32 and FP64 values pass unchanged.
+template <typename T>
+__device__ __forceinline__ T fin(T v) { return v; }
+__device__ __forceinline__ ff fin(ff v) { return ff_norm(v); }
 
 // log10 of an FP64 value in float-float arithmetic (our own evaluation, from the series
 // log m = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...), s = (m - 1)/(m + 1)): x = 2^e m with m
@@ -129,18 +139,28 @@ __device__ __forceinline__ double log10_f32x2(double x) {
   return __dadd_rn((double)r.hi, (double)r.lo);
 }
 
-// The element type a real transform writes: FP32 and FP64 transforms their own, float-float
-// transforms FP64.
+// The element type a real transform writes by default: FP32 and FP64 transforms their own,
+// float-float transforms FP64 (FP64 maps); FP32 maps with float-float transforms instantiate
+// the inverse row passes with float output instead.
 template <typename T>
 struct RealOut {
   using type = T;
-  static __device__ __forceinline__ T cvt(T v) { return v; }
 };
 template <>
 struct RealOut<ff> {
   using type = double;
-  static __device__ __forceinline__ double cvt(ff v) { return ff_to_double(v); }
 };
+// One transform value rounded to the output element type.
+template <typename TO>
+__device__ __forceinline__ TO out_cvt(float v) { return (TO)v; }
+template <typename TO>
+__device__ __forceinline__ TO out_cvt(double v) { return (TO)v; }
+template <typename TO>
+__device__ __forceinline__ TO out_cvt(ff v);
+template <>
+__device__ __forceinline__ double out_cvt<double>(ff v) { return ff_to_double(v); }
+template <>
+__device__ __forceinline__ float out_cvt<float>(ff v) { return __fadd_rn(v.hi, v.lo); }
 
 // read-only (non-coherent) load of a complex value
 __device__ __forceinline__ C2<float> ldc(const C2<float>* p) {
@@ -180,6 +200,10 @@ __host__ __device__ __forceinline__ C2<T> cscale(C2<T> a, T s) {
 template <typename T>
 __host__ __device__ __forceinline__ C2<T> cconj(C2<T> a) {
   return C2<T>{a.x, -a.y};
+}
+template <typename T>
+__device__ __forceinline__ C2<T> cfin(C2<T> a) {
+  return C2<T>{fin(a.x), fin(a.y)};
 }
 // multiply by -i (forward) or +i (inverse)
 template <typename T, bool INV>

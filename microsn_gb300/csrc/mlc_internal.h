@@ -30,8 +30,11 @@ struct FftPlan2D {
   ~FftPlan2D();
 };
 
-// Internal plan precision: FFTs of FP64 maps in float-float arithmetic (mlc_map_set_fft).
+// Internal plan precisions (mlc_map_set_fft): FFTs in float-float arithmetic of FP64 maps
+// (FP64 outputs), and of FP32 maps (float-float spectra, FP32 outputs).
 constexpr int PREC_FF = 2;
+constexpr int PREC_FFS = 3;
+inline bool prec_is_ff(int prec) { return prec == PREC_FF || prec == PREC_FFS; }
 
 enum WsSlot {
   WS_SPEC_TMP = 0,
@@ -101,12 +104,28 @@ struct mlc_map {
   void* data = nullptr;  // Ny x Nx real
   void* spec = nullptr;  // forward spectrum, digit-transposed row order
   bool spec_valid = false;
-  int fft = 0;  // FP64 maps: 0 native FP64 transforms, 1 float-float (MLC_FFT_F32X2)
+  int fft = 0;  // 0 transforms in the map's precision, 1 float-float (MLC_FFT_F32X2)
+  size_t spec_cap = 0;  // bytes allocated at spec
 };
 
 namespace mlc {
-// Precision of a map's transforms: PREC_FF for FP64 maps with float-float FFTs.
-inline int map_fft_prec(const mlc_map* m) { return (m->prec == MLC_F64 && m->fft == 1) ? PREC_FF : m->prec; }
+// The map's spectrum buffer with room for `bytes` (a float-float spectrum of an FP32 map is
+// twice its FP32 one).  Growing it frees the old buffer, which waits for the device.
+inline void* map_spec_buffer(mlc_map* m, size_t bytes) {
+  if (m->spec_cap < bytes) {
+    if (m->spec) MLC_CUDA(cudaFree(m->spec));
+    m->spec = nullptr;
+    m->spec_cap = 0;
+    MLC_CUDA(cudaMalloc(&m->spec, bytes));
+    m->spec_cap = bytes;
+  }
+  return m->spec;
+}
+// Precision of a map's transforms: PREC_FF / PREC_FFS for FP64 / FP32 maps with float-float FFTs.
+inline int map_fft_prec(const mlc_map* m) {
+  if (m->fft == 1) return m->prec == MLC_F64 ? PREC_FF : PREC_FFS;
+  return m->prec;
+}
 }  // namespace mlc
 
 namespace mlc {
@@ -192,9 +211,11 @@ void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const d
                      void* spec_out = nullptr, int kx_slot = WS_KX);
 template <typename T>
 void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out);
-template <typename T>
+template <typename T, typename TO = typename RealOut<T>::type>
 bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, long spec_stride, int nm, int S,
                          void* out, unsigned planar);
+template <typename T, typename TO>
+void rows_c2r_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* spec, void* out);
 
 // Host profile rasters (profile.cpp)
 int profile_dims(const mlc_profile& p);

@@ -7,17 +7,25 @@
 
 namespace mlc {
 
+// Every operation is an explicitly rounded FP32 (or FP64) intrinsic in a fixed order --
+// no contraction into FMAs the compiler might choose -- so that a CPU program doing the
+// same IEEE operations in the same order reproduces the counts exactly:
+//   x1 = fp32(x0 + dx * i),  u = x1 - lx,  q = 1 / fma(u, u, v * v),  a1 = fma(u, q, a1)
+// over the lenses in index order, y1 = (1 - kappa_c - gamma) * x1 - a1, and the pixel
+// floor((y1 + w/2) * (N / w)).
 __global__ void __launch_bounds__(256) k_rayshoot(const float2* __restrict__ lenses, int nl, float kappa_c,
                                                   float gamma, double x0, double y0, double dx, long nrx, long nry,
                                                   float half_w, int N, int* __restrict__ counts) {
   __shared__ float2 ls[1024];
   const long total = nrx * nry;
-  const float scale = N / (2.0f * half_w);
+  const float scale = __fdiv_rn((float)N, __fmul_rn(2.0f, half_w));
+  const float c1 = __fsub_rn(__fsub_rn(1.f, kappa_c), gamma);
+  const float c2 = __fadd_rn(__fsub_rn(1.f, kappa_c), gamma);
   for (long base = (long)blockIdx.x * blockDim.x; base < total; base += (long)gridDim.x * blockDim.x) {
     const long r = base + threadIdx.x;
     const bool ok = r < total;
-    const float x1 = (float)(x0 + dx * (double)(ok ? r % nrx : 0));
-    const float x2 = (float)(y0 + dx * (double)(ok ? r / nrx : 0));
+    const float x1 = (float)__dadd_rn(x0, __dmul_rn(dx, (double)(ok ? r % nrx : 0)));
+    const float x2 = (float)__dadd_rn(y0, __dmul_rn(dx, (double)(ok ? r / nrx : 0)));
     float a1 = 0.f, a2 = 0.f;
     for (int t = 0; t < nl; t += 1024) {
       const int m = min(1024, nl - t);
@@ -26,17 +34,17 @@ __global__ void __launch_bounds__(256) k_rayshoot(const float2* __restrict__ len
       __syncthreads();
 #pragma unroll 8
       for (int i = 0; i < m; i++) {
-        const float u = x1 - ls[i].x, v = x2 - ls[i].y;
-        const float q = __frcp_rn(u * u + v * v);
-        a1 = fmaf(u, q, a1);
-        a2 = fmaf(v, q, a2);
+        const float u = __fsub_rn(x1, ls[i].x), v = __fsub_rn(x2, ls[i].y);
+        const float q = __frcp_rn(__fmaf_rn(u, u, __fmul_rn(v, v)));
+        a1 = __fmaf_rn(u, q, a1);
+        a2 = __fmaf_rn(v, q, a2);
       }
     }
     if (ok) {
-      const float y1 = (1.f - kappa_c - gamma) * x1 - a1;
-      const float y2 = (1.f - kappa_c + gamma) * x2 - a2;
-      const int j = (int)floorf((y1 + half_w) * scale);
-      const int i = (int)floorf((y2 + half_w) * scale);
+      const float y1 = __fsub_rn(__fmul_rn(c1, x1), a1);
+      const float y2 = __fsub_rn(__fmul_rn(c2, x2), a2);
+      const int j = (int)floorf(__fmul_rn(__fadd_rn(y1, half_w), scale));
+      const int i = (int)floorf(__fmul_rn(__fadd_rn(y2, half_w), scale));
       if (i >= 0 && i < N && j >= 0 && j < N) atomicAdd(counts + (long)i * N + j, 1);
     }
   }

@@ -59,26 +59,10 @@ __global__ void __launch_bounds__(256) k_sample_tracks(MapList<T> maps, int nm, 
   const int lane = threadIdx.x & 31;
   const long track = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (track >= ntracks) return;
-  const T X0 = x0[track], Y0 = y0[track], V = v[track];
-  T sn, cs;
-  if (sizeof(T) == 8) {
-    double s_, c_;
-    sincos((double)phi[track], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  } else {
-    float s_, c_;
-    sincosf((float)phi[track], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  }
-  const long bx = (long)floor(X0), by = (long)floor(Y0);
-  const T fx0 = X0 - (T)bx, fy0 = Y0 - (T)by;
+  const TrackGeom<T> g(x0[track], y0[track], phi[track], v[track]);
   const int64_t e0 = off[track], e1 = off[track + 1];
   for (int64_t e = e0 + lane; e < e1; e += 32) {
-    const T vt = V * t[e];
-    const T fx = fx0 + vt * cs, fy = fy0 + vt * sn;
-    const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
+    const Bilin<T> B = g.at(t[e], Nx, Ny);
     for (int q = 0; q < nm; q++) {
       T mu = B.inside ? bilin_read<T>(maps.m[q], B, Nx) : (T)0;
       out[(long)(m_base + q) * E + e] = mag ? (T)-2.5 * mlc_log10(mu) : mu;
@@ -170,15 +154,11 @@ __device__ __forceinline__ void load_pix(const T* __restrict__ p, T* v) {
   }
 }
 
-// One epoch of one track on an interleaved map: bilinear weights at (bx + fx, by + fy),
-// fx = fx0 + vt cos phi, fy = fy0 + vt sin phi, then every map's value (or magnitude)
-// into out[q * E + o].
+// One epoch of one track on an interleaved map: with the bilinear weights of its position
+// (TrackGeom::at), every map's value (or magnitude) into out[q * E + o].
 template <typename T, int NM>
-__device__ __forceinline__ void sample_epoch(const T* __restrict__ imap, int Nx, int Ny, long bx, long by, T fx0, T fy0,
-                                             T cs, T sn, T vt, int mag, T* __restrict__ out, long E, int nm_out,
-                                             int64_t o) {
-  const T fx = fx0 + vt * cs, fy = fy0 + vt * sn;
-  const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
+__device__ __forceinline__ void sample_epoch(const T* __restrict__ imap, int Nx, const Bilin<T>& B, int mag,
+                                             T* __restrict__ out, long E, int nm_out, int64_t o) {
   // 16 bytes of maps at a time (4 FP32 / 2 FP64): the four corners of one chunk in
   // registers, not all NM maps of all four corners (which needed 100 registers and left
   // 2 CTAs per SM, too few warps to hide the gather latency)
@@ -214,21 +194,6 @@ __device__ __forceinline__ void sample_epoch(const T* __restrict__ imap, int Nx,
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void sincos_t(T phi, T* sn, T* cs) {
-  if (sizeof(T) == 8) {
-    double s_, c_;
-    sincos((double)phi, &s_, &c_);
-    *sn = (T)s_;
-    *cs = (T)c_;
-  } else {
-    float s_, c_;
-    sincosf((float)phi, &s_, &c_);
-    *sn = (T)s_;
-    *cs = (T)c_;
-  }
-}
-
 // One warp per track, lanes over epochs; each epoch reads 4 corners x NM interleaved
 // values and writes nm_out light-curve values out[q*E + e].
 template <typename T, int NM>
@@ -241,14 +206,10 @@ __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ 
   const int lane = threadIdx.x & 31;
   const long track = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (track >= ntracks) return;
-  const T X0 = x0[track], Y0 = y0[track], V = v[track];
-  T sn, cs;
-  sincos_t<T>(phi[track], &sn, &cs);
-  const long bx = (long)floor(X0), by = (long)floor(Y0);
-  const T fx0 = X0 - (T)bx, fy0 = Y0 - (T)by;
+  const TrackGeom<T> g(x0[track], y0[track], phi[track], v[track]);
   const int64_t e0 = off[track], e1 = off[track + 1];
   for (int64_t e = e0 + lane; e < e1; e += 32)
-    sample_epoch<T, NM>(imap, Nx, Ny, bx, by, fx0, fy0, cs, sn, V * t[e], mag, out, E, nm_out, e - ebase);
+    sample_epoch<T, NM>(imap, Nx, g.at(t[e], Nx, Ny), mag, out, E, nm_out, e - ebase);
 }
 
 // FP32 with a contiguous output (width == S, off == 0, W in {4, 8, 16}), npix % 4 == 0 and
@@ -365,22 +326,7 @@ __global__ void __launch_bounds__(256) k_sample_expanding(const T* __restrict__ 
   if (idx >= (long)ntracks * nep) return;
   const long tr = idx / nep;
   const int e = (int)(idx - tr * nep);
-  const T X0 = x0[tr], Y0 = y0[tr];
-  T sn, cs;
-  if (sizeof(T) == 8) {
-    double s_, c_;
-    sincos((double)phi[tr], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  } else {
-    float s_, c_;
-    sincosf((float)phi[tr], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  }
-  const long bx = (long)floor(X0), by = (long)floor(Y0);
-  const T vt = v[tr] * t[e];
-  const Bilin<T> B = bilin_weights<T>(bx, X0 - (T)bx + vt * cs, by, Y0 - (T)by + vt * sn, Nx, Ny);
+  const Bilin<T> B = TrackGeom<T>(x0[tr], y0[tr], phi[tr], v[tr]).at(t[e], Nx, Ny);
   T* o = out + idx * nbands;
   for (int b = 0; b < nbands; b++) {
     const T mu = B.inside ? bilin_read<T>(maps + (long)(e * nbands + b) * npix, B, Nx) : (T)0;
@@ -416,9 +362,7 @@ void sample_expanding(mlc_ctx* ctx, const void* maps, int Nx, int Ny, int prec, 
 // from the cancellation-prone single-pass form.  An epoch outside the hull samples 0
 // (magnitude +inf) and makes that map's chi2 +inf, as the light curve would.
 template <typename T, int NM>
-__device__ __forceinline__ void sample_mags(const T* __restrict__ imap, int Nx, int Ny, long bx, T fx, long by, T fy,
-                                            T* m) {
-  const Bilin<T> B = bilin_weights<T>(bx, fx, by, fy, Nx, Ny);
+__device__ __forceinline__ void sample_mags(const T* __restrict__ imap, int Nx, const Bilin<T>& B, T* m) {
   if (!B.inside) {
 #pragma unroll
     for (int q = 0; q < NM; q++) m[q] = (T)INFINITY;
@@ -450,28 +394,13 @@ __global__ void __launch_bounds__(256) k_track_chi2_offset(const T* __restrict__
   const int lane = threadIdx.x & 31;
   const long tr = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (tr >= ntracks) return;
-  const T X0 = x0[tr], Y0 = y0[tr], V = v[tr];
-  T sn, cs;
-  if (sizeof(T) == 8) {
-    double s_, c_;
-    sincos((double)phi[tr], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  } else {
-    float s_, c_;
-    sincosf((float)phi[tr], &s_, &c_);
-    sn = (T)s_;
-    cs = (T)c_;
-  }
-  const long bx = (long)floor(X0), by = (long)floor(Y0);
-  const T fx0 = X0 - (T)bx, fy0 = Y0 - (T)by;
+  const TrackGeom<T> g(x0[tr], y0[tr], phi[tr], v[tr]);
   double s1[NM], s2[NM], W = 0.0;
 #pragma unroll
   for (int q = 0; q < NM; q++) s1[q] = s2[q] = 0.0;
   for (int e = lane; e < Tn; e += 32) {
-    const T vt = V * t[e];
     T m[NM];
-    sample_mags<T, NM>(imap, Nx, Ny, bx, fx0 + vt * cs, by, fy0 + vt * sn, m);
+    sample_mags<T, NM>(imap, Nx, g.at(t[e], Nx, Ny), m);
     const double we = __ldg(w + e), oe = __ldg(obs + e);
     W += we;
 #pragma unroll
@@ -486,9 +415,8 @@ __global__ void __launch_bounds__(256) k_track_chi2_offset(const T* __restrict__
     s1[q] /= W;  // the offset
   }
   for (int e = lane; e < Tn; e += 32) {
-    const T vt = V * t[e];
     T m[NM];
-    sample_mags<T, NM>(imap, Nx, Ny, bx, fx0 + vt * cs, by, fy0 + vt * sn, m);
+    sample_mags<T, NM>(imap, Nx, g.at(t[e], Nx, Ny), m);
     const double we = __ldg(w + e), oe = __ldg(obs + e);
 #pragma unroll
     for (int q = 0; q < NM; q++) {

@@ -326,9 +326,9 @@ void histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, 
 // ---------------------------------------------------------------- histogram without allocation
 //
 // For callers that must not allocate device memory: code running while another
-// framework owns the whole device memory pool, host callbacks and plugins that may only
-// use memory they were handed, or a sequence that is later replayed from a captured
-// stream.  The per-bin counters live in a fixed file-scope device array instead of the
+// framework has reserved the whole device memory pool for its own allocator, and host
+// callbacks and plugins that may only use the buffers they were handed.  The per-bin
+// counters live in a fixed file-scope device array instead of the
 // context's workspace, so this entry point calls no cudaMalloc, cudaFree or allocating
 // library routine.  The array is loaded with the library and stays allocated on every
 // device that loads it until the process exits.

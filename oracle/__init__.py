@@ -25,7 +25,20 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_bin", "libmlc_oracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libmlcref.so")
-REFERENCE_SRC = "/root/reference/simulating_lcurves"
+
+def _reference_src():
+    """The reference's simulating_lcurves directory: $MLC_REFERENCE (the checkout's root),
+    else a checkout named "reference" beside this repository; None when neither exists
+    (on machines without the reference the golden vectors in tests/golden pin the oracle)."""
+    root = os.environ.get("MLC_REFERENCE") or os.path.join(os.path.dirname(HERE), "..", "reference")
+    d = os.path.normpath(os.path.join(root, "simulating_lcurves"))
+    return d if os.path.isdir(os.path.join(d, "src")) else None
+
+
+REFERENCE_SRC = _reference_src()
+REFCUDA_MK = os.path.join(HERE, "refcuda.mk")
+REFCUDA_DIR = os.path.join(os.path.dirname(HERE), "baseline", "_ref")
+REFCUDA_PATH = os.path.join(REFCUDA_DIR, "libmlcref_cuda.so")
 
 SHAPES = {
     "uniform": 0,
@@ -51,9 +64,12 @@ def build(force: bool = False) -> None:
     os.makedirs(os.path.join(HERE, "_bin"), exist_ok=True)
     src = os.path.join(HERE, "mlc_oracle.c")
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
-        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm"])
-    if os.path.isdir(REFERENCE_SRC):
+        subprocess.check_call(["gcc", "-O3", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm"])
+    if REFERENCE_SRC:
         subprocess.check_call(["make", "-s", "-C", HERE, "-j8", f"REF={REFERENCE_SRC}"])
+        # the reference's CUDA sources, staged where they travel with the repository
+        subprocess.check_call(["make", "-s", "-f", REFCUDA_MK, "stage", f"REF={REFERENCE_SRC}"],
+                              stdout=subprocess.DEVNULL)
 
 
 _lib = None
@@ -101,6 +117,8 @@ def lib():
         L.orc_histogram.argtypes = [C.c_long, _dp, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double,
                                     _u64p, _u64p]
         L.orc_topk_smallest.argtypes = [C.c_long, _dp, C.c_long, _lp]
+        L.orc_rayshoot.argtypes = [_fp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.c_long, C.c_long, C.c_double, C.c_int, C.c_long, C.c_long, _ip]
         _lib = L
     return _lib
 
@@ -108,7 +126,7 @@ def lib():
 def ref_available() -> bool:
     """The reference's CPU code is here: compiled on first use where its sources exist (a
     failed build raises instead of skipping the tests that pin the oracle to it)."""
-    if not os.path.exists(REF_PATH) and os.path.isdir(REFERENCE_SRC):
+    if not os.path.exists(REF_PATH) and REFERENCE_SRC:
         build()
     return os.path.exists(REF_PATH)
 
@@ -404,3 +422,116 @@ def topk_smallest(v, k):
     idx = np.zeros(min(k, v.size), np.int64)
     lib().orc_topk_smallest(v.size, v, k, idx)
     return idx
+
+
+# ----------------------------------------------------------------------------- synthetic maps
+
+def lens_field(kappa_star, gamma, width, seed, margin=2.0):
+    """Equal-mass point lenses (unit Einstein radius) uniformly in a disc that covers the
+    image-plane region mapping into the source square: the same seeded draws as the
+    library's map generator, so both shoot through the same lenses."""
+    import math
+    rng = np.random.default_rng(seed)
+    half = width / 2 + margin
+    l1 = half / abs(1 - kappa_star - gamma)
+    l2 = half / abs(1 - kappa_star + gamma)
+    R = math.hypot(l1, l2) + 5.0
+    n = int(round(kappa_star * R * R))
+    r = R * np.sqrt(rng.random(n))
+    th = 2 * np.pi * rng.random(n)
+    return np.stack([r * np.cos(th), r * np.sin(th)], axis=1), (l1, l2)
+
+
+def rayshoot(N, width, kappa_star, gamma, seed, rays_per_pixel=4.0, threads=None):
+    """Inverse ray shooting on the host cores (orc_rayshoot, threads over ray ranges):
+    int32 counts (N, N) equal to the library's mlc_rayshoot for the same inputs, and the
+    map in the reference's normalisation (magnification_map.cpp:33-38): counts / avgN."""
+    import concurrent.futures as cf
+    import math
+    lenses, (l1, l2) = lens_field(kappa_star, gamma, width, seed)
+    mu_th = 1.0 / abs((1 - kappa_star) ** 2 - gamma ** 2)
+    dx = 1.0 / math.sqrt(rays_per_pixel / (mu_th * (width / N) ** 2))
+    nrx, nry = int(2 * l1 / dx) + 1, int(2 * l2 / dx) + 1
+    lz = np.ascontiguousarray(lenses.astype(np.float32).ravel())
+    counts = np.zeros(N * N, np.int32)
+    total = nrx * nry
+    threads = threads or os.cpu_count() or 1
+    parts = max(threads * 8, 1)
+    bounds = [total * i // parts for i in range(parts + 1)]
+    L = lib()
+
+    def run(i):
+        L.orc_rayshoot(lz, len(lenses), 0.0, gamma, -l1, -l2, dx, nrx, nry, width, N, bounds[i], bounds[i + 1],
+                       counts)
+
+    with cf.ThreadPoolExecutor(threads) as ex:
+        list(ex.map(run, range(parts)))
+    counts = counts.reshape(N, N)
+    avgN = float(counts.mean())
+    return counts, counts / avgN
+
+
+# ----------------------------------------------------------------------------- the reference's CUDA build
+
+_refc = None
+
+
+def refcuda_available() -> bool:
+    """The reference's CUDA sources are staged beside the repository (baseline/_ref)."""
+    return os.path.isdir(os.path.join(REFCUDA_DIR, "microlc", "src"))
+
+
+def refcuda():
+    """The reference's own CUDA path (expanding_source, setup_integral_GPU, calculate_chi2_GPU,
+    bin_chi2_GPU) built unchanged for sm_103a by oracle/refcuda.mk (compiled on first use),
+    behind the C entry points of oracle/ref_cuda_harness.cu; None when its sources are not
+    staged.  Runs on the GPU: only -m gpu tests and bench.py's GPU leg call it."""
+    global _refc
+    if _refc is None:
+        if not refcuda_available():
+            return None
+        subprocess.check_call(["make", "-s", "-f", REFCUDA_MK, "-j8"], stdout=subprocess.DEVNULL)
+        L = C.CDLL(REFCUDA_PATH)
+        L.refc_expanding_source.argtypes = [_dp, C.c_int, C.c_int, C.c_double, C.c_double, _dp, C.c_int, C.c_char_p,
+                                            C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_int]
+        L.refc_pair_path.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int, _ip, _ip, _dp, _dp, _dp, _dp,
+                                     C.c_int, _dp, C.c_void_p, _up, _up, _dp, _dp, _dp, C.c_int]
+        _refc = L
+    return _refc
+
+
+def refcuda_expanding_source(mp, sizes, shape, lx, ly, pix_phys, width):
+    """expanding_source of the reference's CUDA build on a 10000 x 10000 FP64 map (the only
+    size its fixed multiply grid covers): (LC, DLC, ms)."""
+    L = refcuda()
+    mp = np.ascontiguousarray(mp, np.float64)
+    Ny, Nx = mp.shape
+    sizes = np.ascontiguousarray(sizes, np.float64)
+    lx = np.ascontiguousarray(lx, np.int32); ly = np.ascontiguousarray(ly, np.int32)
+    Nloc, Nprof = lx.size, sizes.size
+    LC = np.zeros(Nloc * Nprof); DLC = np.zeros(max(Nloc * (Nprof - 1), 1)); ms = np.zeros(1)
+    st = L.refc_expanding_source(mp, Nx, Ny, width, pix_phys, sizes, Nprof, shape.encode(), Nloc, lx, ly, LC, DLC, ms,
+                                 1)
+    if st != 0:
+        raise RuntimeError(f"refc_expanding_source: status {st}")
+    return LC.reshape(Nloc, Nprof), DLC[: Nloc * (Nprof - 1)].reshape(Nloc, Nprof - 1), float(ms[0])
+
+
+def refcuda_pair_path(LCA, DLCA, LCB, DLCB, v, edges, want_rank=True):
+    """setup_integral_GPU + calculate_chi2_GPU + bin_chi2_GPU of the reference's CUDA build:
+    dict(rank, lower, nper, bchi2, bexp, ms=[setup, chi2, bin])."""
+    L = refcuda()
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    LCA, DLCA, LCB, DLCB = f(LCA), f(DLCA), f(LCB), f(DLCB)
+    Nloc, Nprof = LCA.shape
+    edges = f(edges)
+    nb = edges.size
+    rank = np.zeros(Nloc * Nloc, np.uint32) if want_rank else None
+    lower = np.zeros(nb, np.uint32); nper = np.zeros(nb, np.uint32)
+    bc = np.zeros(nb); be = np.zeros(nb); ms = np.zeros(3)
+    st = L.refc_pair_path(Nloc, Nprof, LCA, DLCA, LCB, DLCB, int(v["Njp"]), np.ascontiguousarray(v["indA"], np.int32),
+                          np.ascontiguousarray(v["indB"], np.int32), f(v["facA"]), f(v["facB"]), f(v["d"]), f(v["s"]),
+                          nb, edges, rank.ctypes.data_as(C.c_void_p) if want_rank else None, lower, nper, bc, be, ms, 1)
+    if st != 0:
+        raise RuntimeError(f"refc_pair_path: status {st}")
+    return dict(rank=rank, lower=lower, nper=nper, bchi2=bc, bexp=be, ms=[float(x) for x in ms])

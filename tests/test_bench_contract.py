@@ -13,7 +13,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 KEYS = {"impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
         "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"}
-ARGS = ["bench.py", "--impl", "reference", "--small", "--steps", "3", "--warmup", "3"]
+ARGS = ["bench.py", "--impl", "reference", "--side", "400", "--tracks", "2000", "--steps", "3", "--warmup", "3"]
 
 
 def _lines(stdout):
@@ -27,7 +27,8 @@ def _check(d, n_gpus):
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
-    assert d["config"]["workload"] and d["config"]["n"] == 2000
+    assert d["config"]["workload"] and d["config"]["n"] == 400
+    assert len(d["step_ms"]) == 3 and abs(sum(d["step_ms"]) / 3 - d["ms_per_step"]) < 1e-6 * d["ms_per_step"]
 
 
 def test_reference_arm_prints_one_contract_line():
