@@ -519,6 +519,17 @@ def c5_workload(args, ctx, dev, rank):
     conv_graph = e[0].elapsed_time(e[1])
     npairs = len(pairs) * float(ntr) * ntr
     total = t_curves + t_pairs
+    # the pair stage against FP64 on a fixed subset (images 0 and 1, 1000 x 1000 curves):
+    # the tensor-core chi2 matrix against the FP64 plain kernel on the same curves
+    sa = torch.randperm(ntr, generator=torch.Generator().manual_seed(4))[:1000].to(dev)
+    sb = torch.randperm(ntr, generator=torch.Generator().manual_seed(5))[:1000].to(dev)
+    As, Bs = lcs[0][sa].contiguous(), lcs[1][sb].contiguous()
+    mt = mlc.pair_chi2_magdiff(ctx, As, Bs, w, None, True, method="tensor", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                               want_matrix=True)["matrix"].double()
+    mp_ = mlc.pair_chi2_magdiff(ctx, As, Bs, w, None, True, method="plain", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                                want_matrix=True)["matrix"].double()
+    pair_rel = ((mt - mp_).abs() / mp_.abs().clamp_min(1e-30)).max().item()
+    del mt, mp_, As, Bs
     out = {"workload": f"supernova: {len(maps)} x {N}^2 FP32 maps, {len(profs)} limb-darkened expanding-photosphere "
                        f"profiles per map ({C5_EPOCHS} epochs x {nb} bands), {ntr} tracks per image, offset "
                        f"magnitude-difference chi2 of all track pairs of {len(pairs)} image pairs (T = {T})",
@@ -528,7 +539,14 @@ def c5_workload(args, ctx, dev, rank):
            "convolutions_per_s": len(maps) * len(profs) / (t_curves / 1000.0),
            "conv_ms_graph": conv_graph, "conv_ms_eager": conv_eager,
            "refined_pairs": int(sum(r["stats"]["refined"] for r in res)),
-           "histogram_total": float(sum(float(r["hist"].sum()) for r in res))}
+           "histogram_total": float(sum(float(r["hist"].sum()) for r in res)),
+           "histogram_below_range": int(sum(r["stats"]["below"] for r in res)),
+           "histogram_above_range": int(sum(r["stats"]["above"] for r in res)),
+           "pairs_total": npairs,
+           "max_rel_err_vs_fp64": pair_rel,
+           "parity_subset": {"pairs": 1000 * 1000, "max_rel_err_vs_fp64": pair_rel, "tolerance": 1e-5,
+                             "what": "tensor-core pair chi2 vs the FP64 plain kernel on the same FP32 light curves "
+                                     "(images 0 and 1, 1000 x 1000 fixed curves)"}}
     for m in maps:
         m.close()
     del conv
@@ -561,6 +579,8 @@ def ratio_pair_workload(args, ctx, m, dev, rank):
     Nloc = RATIO_NLOC if not args.small else 1024
     mA = mlc.Map(ctx, m.tensor().double(), "f64")
     mB = mlc.Map(ctx, torch.flip(m.tensor(), [0, 1]).double().contiguous(), "f64")  # image B: the map turned 180 deg
+    mA_host = mA.tensor().cpu().numpy() if oracle.refcuda_available() else None
+    mB_host = mB.tensor().cpu().numpy() if oracle.refcuda_available() else None
     Noff = int(np.ceil((n / WIDTH) * RATIO_SIZES[-1]))
     lx, ly = mlc.locations_random(Nloc, n, Noff, RATIO_SEED + rank)
     base = mlc.profile("gaussian", 0.0, WIDTH / n)
@@ -610,7 +630,40 @@ def ratio_pair_workload(args, ctx, m, dev, rank):
         dt = time.perf_counter() - t0
         cpu = {"kind": "port", "cores": 1, "pairs_per_s": sub_n * sub_n / dt,
                "sample": f"{sub_n}^2 pairs of the same curves (calculate_chi2 + bin_chi2 restated in C)"}
+    # the reference's own CUDA build on the same inputs and GPU (compiled unchanged for sm_103a
+    # from the staged sources): its expanding_source on both maps (cuFFT, host rasters and a
+    # host-built full-size kernel per profile, as it is written) and its pair path, timed
+    # around each call, with its outputs compared with the library's
+    refc = None
+    if rank == 0 and oracle.refcuda_available() and n == 10000:
+        try:
+            mpA = mA_host
+            mpB = mB_host
+            pixr = WIDTH / n
+            LCr_A, DLCr_A, msA = oracle.refcuda_expanding_source(mpA, RATIO_SIZES, "gaussian", lx, ly, pixr, WIDTH)
+            LCr_B, DLCr_B, msB = oracle.refcuda_expanding_source(mpB, RATIO_SIZES, "gaussian", lx, ly, pixr, WIDTH)
+            ov = dict(Njp=v.Njp, indA=v.indA, indB=v.indB, facA=v.facA, facB=v.facB, d=v.d, s=v.s)
+            rp = oracle.refcuda_pair_path(LCr_A, DLCr_A, LCr_B, DLCr_B, ov, edges, want_rank=False)
+            lA = LCA.cpu().numpy()
+            rel_lc = float(np.max(np.abs(lA - LCr_A) / np.maximum(np.abs(LCr_A), 1e-3 * np.mean(LCr_A))))
+            fullr = rp["nper"] > 0
+            refc = {"what": "the reference's gpu_functions.cu / data_structs.cu built unchanged for sm_103a "
+                            "(cuFFT, thrust), on the same maps, locations, sizes and bins",
+                    "expanding_source_ms_two_maps": msA + msB,
+                    "expanding_source_over_library": (msA + msB) / es_ms,
+                    "setup_integral_ms": rp["ms"][0], "calculate_chi2_ms": rp["ms"][1], "bin_chi2_ms": rp["ms"][2],
+                    "pairs_per_s": pairs / ((rp["ms"][1] + rp["ms"][2]) / 1000.0),
+                    "library_reference_form_over_it": (rp["ms"][1] + rp["ms"][2]) / ref_ms,
+                    "library_fused_over_it": (rp["ms"][1] + rp["ms"][2]) / fused_ms,
+                    "LC_max_rel_vs_library": rel_lc,
+                    "bins_equal": bool(np.array_equal(rp["nper"], nper) and np.array_equal(rp["lower"], lower)),
+                    "binned_chi2_max_rel_vs_library": float(np.max(np.abs(rp["bchi2"][fullr] - bc[fullr]) /
+                                                                   np.abs(bc[fullr]))) if fullr.any() else None,
+                    "timing": "wall clock around each call (each synchronises internally)"}
+        except Exception as ex:  # report, do not fail the bench
+            refc = {"error": str(ex)[:200]}
     return {"metric": "pair-chi2/s (reference ratio form)", "unit": "pair-chi2/s",
+            "reference_cuda": refc,
             "config": {"workload": f"two {n}^2 FP64 maps (the bench map and its 180-degree turn), {Nloc} random "
                                    f"locations, sizes {RATIO_SIZES} R_E gaussian, 300 log z-bins, Nd = 5",
                        "pairs_per_evaluation": pairs},

@@ -421,6 +421,8 @@ typedef struct {
   long long refined;   /* near-identical pairs recomputed in FP64 (tensor form) */
   long long candidates;
   int passes;          /* passes over the pairs (1 unless the threshold had to move) */
+  long long below;     /* pairs whose chi2 lies below 10^lo_log10 (zero included): not in hist */
+  long long above;     /* pairs whose chi2 lies at or above 10^hi_log10: not in hist */
 } mlc_pair_stats;
 
 /* Pairwise magnitude-difference chi2 between NA curves A and NB curves B (device FP32,

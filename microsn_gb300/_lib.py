@@ -34,7 +34,8 @@ MLC_IO_HOST, MLC_ASYNC, MLC_GRAPH = 1, 2, 4
 
 class MlcPairStats(C.Structure):
     _fields_ = [("delta", C.c_double), ("threshold", C.c_double), ("refined", C.c_longlong),
-                ("candidates", C.c_longlong), ("passes", C.c_int)]
+                ("candidates", C.c_longlong), ("passes", C.c_int), ("below", C.c_longlong),
+                ("above", C.c_longlong)]
 
 
 class MlcError(RuntimeError):

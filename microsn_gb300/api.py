@@ -609,7 +609,7 @@ def pair_chi2_magdiff(ctx: Context, A: torch.Tensor, B: torch.Tensor, w, d=None,
                                           _ptr(hist), k, _ptr(tv), _ptr(ti), _ptr(tj), _ptr(mat), C.byref(st)))
     return dict(hist=hist, topk_val=tv[:k], topk_i=ti[:k], topk_j=tj[:k], matrix=mat,
                 stats=dict(delta=st.delta, threshold=st.threshold, refined=st.refined, candidates=st.candidates,
-                           passes=st.passes))
+                           passes=st.passes, below=st.below, above=st.above))
 
 
 def pair_chi2_magdiff_list(ctx: Context, A: torch.Tensor, B: torch.Tensor, w, ia, ib, d=None, offset=False):

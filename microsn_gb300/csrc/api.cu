@@ -648,6 +648,8 @@ int mlc_pair_chi2_magdiff(mlc_ctx* ctx, int method, int NA, int NB, int T, const
       stats->refined = r.nrefined;
       stats->candidates = r.ncand;
       stats->passes = r.passes;
+      stats->below = r.below;
+      stats->above = r.above;
     }
   });
 }

@@ -103,13 +103,13 @@ __device__ __forceinline__ void sincos_ff(float phi, ff* sn, ff* cs) {
   }
 }
 
-// Offset f0 + V t c of a track epoch from the track's pixel base, returned as whole pixels
-// *d and a fraction in [0, 1) rounded to FP32 (6e-8 px).  The displacement V t c runs to
-// thousands of pixels, where an FP32 sum would be off by up to 5e-4 px: V t is formed
-// exactly (FMA two-product) and the sum in float-float arithmetic.
-__device__ __forceinline__ float track_offset(float f0, float V, float t, ff c, long* d) {
-  const float vh = __fmul_rn(V, t);
-  const ff x = ff(f0, 0.f) + ff(vh, __fmaf_rn(V, t, -vh)) * c;
+// Offset f0 + t vc of a track epoch from the track's pixel base (vc = V cos phi or V sin phi
+// as a float-float pair), returned as whole pixels *d and a fraction in [0, 1) rounded to
+// FP32 (6e-8 px).  The displacement runs to thousands of pixels, where an FP32 sum would be
+// off by up to 5e-4 px, so it is formed in float-float arithmetic.
+__device__ __forceinline__ float track_offset(float f0, float t, ff vc, long* d) {
+  const float ph = __fmul_rn(t, vc.hi);
+  const ff x = ff(f0, 0.f) + ff(ph, __fmaf_rn(t, vc.lo, __fmaf_rn(t, vc.hi, -ph)));
   const float fl = floorf(x.hi);
   float r = __fadd_rn(__fsub_rn(x.hi, fl), x.lo);
   long dd = (long)fl;
@@ -151,10 +151,13 @@ struct TrackGeom<double> {
 template <>
 struct TrackGeom<float> {
   long bx, by;
-  float fx0, fy0, V;
-  ff c, s;
-  __device__ __forceinline__ TrackGeom(float X0, float Y0, float phi, float V_) : V(V_) {
+  float fx0, fy0;
+  ff vc, vs;  // V cos phi, V sin phi
+  __device__ __forceinline__ TrackGeom(float X0, float Y0, float phi, float V) {
+    ff c, s;
     sincos_ff(phi, &s, &c);
+    vc = ff_norm(ff(V, 0.f) * c);
+    vs = ff_norm(ff(V, 0.f) * s);
     bx = (long)floorf(X0);
     by = (long)floorf(Y0);
     fx0 = X0 - (float)bx;  // exact
@@ -162,8 +165,8 @@ struct TrackGeom<float> {
   }
   __device__ __forceinline__ Bilin<float> at(float t, int Nx, int Ny) const {
     long dx, dy;
-    const float rx = track_offset(fx0, V, t, c, &dx);
-    const float ry = track_offset(fy0, V, t, s, &dy);
+    const float rx = track_offset(fx0, t, vc, &dx);
+    const float ry = track_offset(fy0, t, vs, &dy);
     return bilin_weights<float>(bx + dx, rx, by + dy, ry, Nx, Ny);
   }
 };

@@ -168,7 +168,7 @@ FftPlan2D* plan_get(mlc_ctx* ctx, int Nx, int Ny, int prec) {
   p->Wc = Nx / 2 + 1;
   p->Wp = (int)round_up(p->Wc, 16);
   p->elem = prec == MLC_F64 ? sizeof(C2<double>) : prec_is_ff(prec) ? sizeof(C2<ff>) : sizeof(C2<float>);
-  p->CW = prec == MLC_F32 ? 16 : 8;
+  p->CW = prec == MLC_F64 ? 8 : 16;  // as strip_width<T>() in fft_impl.cuh
   split_columns(Ny, p->N1, p->N2);
   p->rlM = factor_radices(p->M, 2);
   p->rlN1 = factor_radices(p->N1, p->N2);

@@ -125,8 +125,10 @@ __device__ __forceinline__ void dft_split2(C2<T>* v, const T* wr, const T* wi) {
   }
   Dft<T, H, INV>::run(e);
   Dft<T, H, INV>::run(o);
+  v[0] = cadd(e[0], o[0]);  // W^0 = 1
+  v[H] = csub(e[0], o[0]);
 #pragma unroll
-  for (int k = 0; k < H; k++) {
+  for (int k = 1; k < H; k++) {
     // W^k o with W^k = (wr, -wi) forward, (wr, wi) inverse
     const T sr = INV ? -wi[k] : wi[k];
     const C2<T> t = C2<T>{wr[k] * o[k].x + sr * o[k].y, wr[k] * o[k].y - sr * o[k].x};
@@ -135,15 +137,27 @@ __device__ __forceinline__ void dft_split2(C2<T>* v, const T* wr, const T* wi) {
   }
 }
 
+// 10 points by the prime-factor (Good-Thomas) split 10 = 2 x 5, which needs no twiddles:
+// with n = (5 n1 + 2 n2) mod 10 and k = (5 k1 + 6 k2) mod 10, W10^(n k) = W2^(n1 k1) W5^(n2 k2),
+// so five DFT2 over n1, then two DFT5 over n2 (84 real additions and 32 multiplications,
+// against 94 and 52 for the radix-2 split with its twiddles).
 template <typename T, bool INV>
 struct Dft<T, 10, INV> {
   static __device__ __forceinline__ void run(C2<T>* v) {
-    // cos, sin(2 pi k / 10), k = 0..4
-    const T wr[5] = {(T)1, (T)0.80901699437494742410229341718282, (T)0.30901699437494742410229341718282,
-                     (T)-0.30901699437494742410229341718282, (T)-0.80901699437494742410229341718282};
-    const T wi[5] = {(T)0, (T)0.58778525229247312916870595463907, (T)0.95105651629515357211643933337938,
-                     (T)0.95105651629515357211643933337938, (T)0.58778525229247312916870595463907};
-    dft_split2<T, 5, INV>(v, wr, wi);
+    C2<T> a[5], b[5];
+#pragma unroll
+    for (int n2 = 0; n2 < 5; n2++) {
+      const C2<T> x0 = v[(2 * n2) % 10], x1 = v[(5 + 2 * n2) % 10];
+      a[n2] = cadd(x0, x1);  // k1 = 0
+      b[n2] = csub(x0, x1);  // k1 = 1
+    }
+    Dft<T, 5, INV>::run(a);
+    Dft<T, 5, INV>::run(b);
+#pragma unroll
+    for (int k2 = 0; k2 < 5; k2++) {
+      v[(6 * k2) % 10] = a[k2];
+      v[(5 + 6 * k2) % 10] = b[k2];
+    }
   }
 };
 

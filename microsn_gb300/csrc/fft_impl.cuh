@@ -310,6 +310,134 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
   asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
 }
 
+// The same last pass for float-float rows of M = 5000 = 8 x 5^4 points, with levels small
+// enough for 64 registers: a float-float DFT25 item of the three-level form holds 100
+// registers of data alone, which left two CTAs of 256 threads (16 warps) per SM, waiting
+// on its barriers.  Here level 1 is the three-level form's (DFT8 over stride 625 from global
+// memory, twiddle W_M^-(j n1)); then in-place decimation-in-frequency radix-5 levels on
+// blocks of 625, 125, 25 (item (block, m < J'/5): DFT5 over stride J'/5, twiddle
+// W_J'^-(m r), written back to the slots it read, so a thread takes its items one after
+// another with no barrier between them); the last radix-5 level on blocks of 5 reads its
+// items, waits, and writes them in natural order: output r of item
+// it = 125 k1 + 25 a + 5 b + c is z[k1 + 8 (a + 5 (b + 5 (c + 5 r)))] = z[n0 + 1000 r].  512 threads, two
+// CTAs (32 warps) per SM, the same number of barriers as the three-level form.
+template <typename T, int JP>
+__device__ __forceinline__ void c2r5_level(C2<T>* s, const C2<T>* w) {
+  constexpr int SP = JP / 5, WS = 625 / JP;
+  for (int it = threadIdx.x; it < 1000; it += blockDim.x) {
+    const int blk = it / SP, m = it - blk * SP;
+    C2<T>* b = s + blk * JP + m;
+    C2<T> u[5];
+#pragma unroll
+    for (int r = 0; r < 5; r++) u[r] = b[r * SP];
+    Dft<T, 5, true>::run(u);
+    b[0] = u[0];
+#pragma unroll
+    for (int r = 1; r < 5; r++) b[r * SP] = cmulc(u[r], w[m * r * WS]);
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a, const C2<T>* __restrict__ twx, C2<T>* s) {
+  constexpr int M = 5000, J = 625;
+  C2<T>* w = s + M;  // W_625^e = W_Nx^(16 e), e < 625
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < J; e += nt) w[e] = ldc(twx + 16L * e);
+  for (int j = tid; j < J; j += nt) {
+    C2<T> v[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int k = J * q + j;
+      const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
+      const C2<T> e = cadd(xk, xm);
+      const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
+      v[q] = C2<T>{e.x - o.y, e.y + o.x};
+    }
+    Dft<T, 8, true>::run(v);
+    s[j] = v[0];
+#pragma unroll
+    for (int n1 = 1; n1 < 8; n1++) s[n1 * J + j] = cmulc(v[n1], ldc(twx + 2L * j * n1));  // W_M^-(j n1)
+  }
+  __syncthreads();
+  c2r5_level<T, 625>(s, w);
+  c2r5_level<T, 125>(s, w);
+  c2r5_level<T, 25>(s, w);
+  // blocks of 5: every item read (two per thread at most: blockDim >= 500), then written
+  // in natural order.  Thread t takes the item whose outputs land at n0 = t (and t + nt),
+  // n0 + 1000 r: consecutive threads write consecutive slots (taking items in their own
+  // order instead put a warp's writes 200 slots apart, all in one shared-memory bank)
+  C2<T> u[2][5];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int n0 = tid + h * nt;
+    if (n0 < 1000) {
+      const int it = 125 * (n0 % 8) + 25 * ((n0 / 8) % 5) + 5 * ((n0 / 40) % 5) + n0 / 200;
+#pragma unroll
+      for (int r = 0; r < 5; r++) u[h][r] = s[5 * it + r];
+      Dft<T, 5, true>::run(u[h]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int n0 = tid + h * nt;
+    if (n0 < 1000) {
+#pragma unroll
+      for (int r = 0; r < 5; r++) s[n0 + 1000 * r] = u[h][r];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, typename TO>
+__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
+    k_rows_c2r5_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm, TO* __restrict__ out,
+                   int S, const C2<T>* __restrict__ twx, unsigned planar) {
+  constexpr int NX = 10000;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
+  const int row = blockIdx.y;
+  const int k = (int)cl.block_rank(), quad = blockIdx.x >> 2, q = 4 * quad + k;
+  if (q < nm && ((planar >> q) & 1u)) {  // the direct form's real map: copy its row
+    const TO* src = reinterpret_cast<const TO*>(specs + (long)q * spec_stride) + (long)row * NX;
+    T* d = reinterpret_cast<T*>(s);
+    for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = T(src[n]);
+  } else if (q < nm) {
+    c2r5_row<T>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
+  } else {
+    for (int n = threadIdx.x; n < NX / 2; n += blockDim.x) s[n] = C2<T>{T(0), T(0)};
+  }
+  cl.sync();  // every row of the cluster is in its CTA's shared memory
+  const int W = S - 4 * quad < 4 ? S - 4 * quad : 4;
+  constexpr int CH = NX / 4;
+  const int x0 = k * CH, x1 = x0 + CH;
+  TO* dst = out + (long)row * NX * S + 4 * quad;
+  if (W == 4) {
+    const T* src[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) src[r] = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
+    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+      TO v[4];
+#pragma unroll
+      for (int r = 0; r < 4; r++) v[r] = out_cvt<TO>(src[r][x]);
+      float4* d = reinterpret_cast<float4*>(dst + (long)x * S);
+      const float4* wv = reinterpret_cast<const float4*>(v);
+#pragma unroll
+      for (int i = 0; i < (int)(4 * sizeof(TO) / 16); i++) d[i] = wv[i];
+    }
+  } else {
+    for (int r = 0; r < W; r++) {
+      const T* sr = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = out_cvt<TO>(sr[x]);
+    }
+  }
+  // no CTA leaves while the others still read its shared memory (relaxed: see k_rows_c2r3_il)
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
+}
+
 // ---------------------------------------------------------------- column kernels
 
 // In-place sub-pass over the row set {set*set_mul + j*j_mul : j < L} of one strip of CW
@@ -471,8 +599,10 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
   // the map-spectrum tile (N2 rows of CW values, the only DRAM input) is needed in forward
   // stage 2, after two L2 round trips and four barriers: start pulling it into L2 now
   // (without registers or shared memory, which the other chain's P2 CTAs need)
-  for (int n = threadIdx.x; n < N2; n += blockDim.x)
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + ((long)kk * N2 + n) * pitch + col0));
+  constexpr int LINES = (int)(CW * sizeof(C2<T>) / 128);  // 128-byte lines per strip row
+  for (int n = threadIdx.x; n < N2 * LINES; n += blockDim.x)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + ((long)kk * N2 + n / LINES) * pitch + col0 +
+                                                    (n % LINES) * (128 / (int)sizeof(C2<T>))));
   for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * kk) % N1) * N2);
   for (int n = threadIdx.x; n < N2; n += blockDim.x) {
     w2[n] = ldc(twy + (long)n * kk);
@@ -688,10 +818,19 @@ static void launch_rows_c2r(mlc_ctx* ctx, const FftPlan2D& p, const void* in, vo
   MLC_CHECK_LAUNCH();
 }
 
+// Columns per CTA of the column passes: 128 bytes of complex values for FP32 and FP64;
+// float-float (16-byte values) takes 16 columns, as FP32 does, so that its arithmetic-bound
+// CTAs are whole warps (10 x 16 = 160 threads for a 10 x 10 pass, where 8 columns left the
+// third of 80 threads' warps half empty).
+template <typename T>
+constexpr int strip_width() {
+  return (sizeof(T) == 8 && !std::is_same<T, ff>::value) ? 8 : 16;
+}
+
 // kind 'A': row sets {n2 + N2*j}, length N1; kind 'B': row blocks {k1*N2 + j}, length N2.
 template <typename T, bool INV>
 static void launch_colpass(mlc_ctx* ctx, const FftPlan2D& p, void* buf, char kind, int post_tw) {
-  constexpr int CW = sizeof(T) == 8 ? 8 : 16;
+  constexpr int CW = strip_width<T>();
   const int nstrips = ceil_div(p.Wc, CW);
   int L, nsets, tw_stride;
   long set_mul, j_mul;
@@ -753,7 +892,7 @@ void forward_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype
 template <typename T>
 void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
                      void* out, void* spec_out, int kx_slot) {
-  constexpr int CW = sizeof(T) == 8 ? 8 : 16;
+  constexpr int CW = strip_width<T>();
   const int h = pN / 2;
   MLC_REQUIRE(pN % 2 == 0 && 2 * h <= p.Ny && 2 * h <= p.Nx, MLC_ERR_LIMIT,
               "profile raster larger than the map");
@@ -843,9 +982,17 @@ bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, lo
                          void* out, unsigned planar) {
   using K = void (*)(const C2<T>*, long, long, int, TO*, int, const C2<T>*, unsigned);
   K k = nullptr;
-  int J = 0;
+  int J = 0, nthr = 256;
   switch (p.M) {
-    case 5000: k = k_rows_c2r3_il<T, 8, 25, 25, TO>; J = 625; break;
+    case 5000:
+      if constexpr (std::is_same<T, ff>::value) {
+        k = k_rows_c2r5_il<T, TO>;
+        nthr = 512;
+      } else {
+        k = k_rows_c2r3_il<T, 8, 25, 25, TO>;
+      }
+      J = 625;
+      break;
     case 4096: k = k_rows_c2r3_il<T, 16, 16, 16, TO>; J = 256; break;
     case 2000: k = k_rows_c2r3_il<T, 8, 10, 25, TO>; J = 250; break;
     case 1000: k = k_rows_c2r3_il<T, 10, 10, 10, TO>; J = 100; break;
@@ -857,8 +1004,8 @@ bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, lo
   const int quads = (nm + 3) / 4;
   {
     MLC_KSCOPE(ctx, "fft_rows_c2r_interleave");
-    k<<<dim3(4 * quads, p.Ny), 256, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (TO*)out, S,
-                                                          (const C2<T>*)p.twx, planar);
+    k<<<dim3(4 * quads, p.Ny), nthr, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (TO*)out, S,
+                                                           (const C2<T>*)p.twx, planar);
   }
   MLC_CHECK_LAUNCH();
   return true;

@@ -33,6 +33,7 @@ struct PdResult {
   double delta = 0, thr = 0;
   long long nrefined = 0, ncand = 0;
   int passes = 0;
+  long long below = 0, above = 0;  // chi2 below lo / at or above hi of the histogram
 };
 
 void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int NA, int NB, int T,

@@ -82,7 +82,7 @@ struct PdParams {
 
 size_t smem_bytes(int nkb, int nbins) {
   return 1024 + (size_t)3 * nkb * A_BOX + (size_t)NSTAGE * 3 * nkb * B_BOX + 16 * 8 + 16 +
-         sizeof(uint32_t) * ((nbins + 3) & ~3) + (size_t)EPI_WARPS * 16 * sizeof(float4);
+         sizeof(uint32_t) * ((nbins + 2 + 3) & ~3) + (size_t)EPI_WARPS * 16 * sizeof(float4);
 }
 
 // 2^k for k in [-126, 127]; 0 below (the terms it scales are then negligible)
@@ -127,7 +127,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
   uint32_t* tmem_slot = (uint32_t*)(bars + 16);
   volatile int* abort_s = (volatile int*)(tmem_slot + 1);
   uint32_t* hist_s = tmem_slot + 4;
-  float4* colv = (float4*)(hist_s + ((P.nbins + 3) & ~3));  // [EPI_WARPS][16] column constants
+  // nbins counters, then the two out-of-range counters (below lo, at or above hi)
+  float4* colv = (float4*)(hist_s + ((P.nbins + 2 + 3) & ~3));  // [EPI_WARPS][16] column constants
   const uint32_t hist_sa = tc::smem_u32(hist_s);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
     *abort_s = 0;
     tc::fence_barrier_init();
   }
-  for (int i = threadIdx.x; i < P.nbins; i += NTHREADS) hist_s[i] = 0;
+  for (int i = threadIdx.x; i < P.nbins + 2; i += NTHREADS) hist_s[i] = 0;
   if (warp == 2) tc::tmem_alloc(tmem_slot, TMEM_COLS);
   tc::fence_before_sync();
   __syncthreads();
@@ -314,8 +315,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
             float lg;
             asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(lg) : "f"(chi2));
             const int bin = __float2int_rd(fmaf(lg, P.hscale, P.hoff));
-            if ((unsigned)bin < (unsigned)P.nbins)
-              asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(hist_sa + 4u * (uint32_t)bin) : "memory");
+            const uint32_t slot = (unsigned)bin < (unsigned)P.nbins ? (uint32_t)bin
+                                  : (bin < 0 ? (uint32_t)P.nbins : (uint32_t)P.nbins + 1u);
+            asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(hist_sa + 4u * slot) : "memory");
           }
         }
         tc::fence_before_sync();
@@ -324,7 +326,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
       }
       // flush this item's histogram (per item, so the 32-bit shared counters cannot overflow)
       epi_sync();
-      for (int b = (int)threadIdx.x - 128; b < P.nbins; b += EPI_WARPS * 32) {
+      for (int b = (int)threadIdx.x - 128; b < P.nbins + 2; b += EPI_WARPS * 32) {
         const uint32_t v = hist_s[b];
         if (v) {
           atomicAdd(P.hist + b, (unsigned long long)v);
@@ -362,7 +364,9 @@ __global__ void __launch_bounds__(256) k_pd_refine(const double* __restrict__ ce
     if (out) out[(long)i * NB + j] = chi2;
     if (s > 0) {
       const int bin = (int)floor((log10(s) - lo) / width);
-      if (bin >= 0 && bin < nbins) atomicAdd(hist + bin, 1ull);
+      atomicAdd(hist + (bin < 0 ? nbins : (bin < nbins ? bin : nbins + 1)), 1ull);
+    } else if (s == 0) {
+      atomicAdd(hist + nbins, 1ull);  // below every edge
     }
     if (chi2 < thr) {
       const unsigned k = atomicAdd(ncand, 1u);
@@ -405,13 +409,15 @@ __global__ void __launch_bounds__(256) k_pd_hist_cand(const double* __restrict__
                                                       unsigned* __restrict__ ncand, float* __restrict__ cval,
                                                       int* __restrict__ ci, int* __restrict__ cj) {
   extern __shared__ uint32_t hs[];
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x) hs[b] = 0;
+  for (int b = threadIdx.x; b < nbins + 2; b += blockDim.x) hs[b] = 0;
   __syncthreads();
   for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
     const double s = chi2[q];
     if (s > 0) {
       const int bin = (int)floor((log10(s) - lo) / width);
-      if (bin >= 0 && bin < nbins) atomicAdd(hs + bin, 1u);
+      atomicAdd(hs + (bin < 0 ? nbins : (bin < nbins ? bin : nbins + 1)), 1u);
+    } else if (s == 0) {
+      atomicAdd(hs + nbins, 1u);  // below every edge
     }
     if ((float)s < thr) {
       const unsigned k = atomicAdd(ncand, 1u);
@@ -423,7 +429,7 @@ __global__ void __launch_bounds__(256) k_pd_hist_cand(const double* __restrict__
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < nbins; b += blockDim.x)
+  for (int b = threadIdx.x; b < nbins + 2; b += blockDim.x)
     if (hs[b]) atomicAdd(hist + b, (unsigned long long)hs[b]);
 }
 
@@ -519,7 +525,7 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
   }
   // ---- buffers: candidates, refinement list, counters, histogram
   const unsigned rcap = 1u << 22;
-  char* buf = (char*)ws_get(ctx, WS_PAIR_CAND, (size_t)cap * 12 + (size_t)rcap * 8 + 64 + 8 * (size_t)nbins + 64);
+  char* buf = (char*)ws_get(ctx, WS_PAIR_CAND, (size_t)cap * 12 + (size_t)rcap * 8 + 64 + 8 * (size_t)(nbins + 2) + 64);
   float* cval = (float*)buf;
   int* ci = (int*)(cval + cap);
   int* cj = ci + cap;
@@ -590,7 +596,7 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
     res.passes = pass + 1;
     prm.thr = (float)std::min(thr, 3.0e38);  // -1: no candidates
     MLC_CUDA(cudaMemsetAsync(counters, 0, 16, ctx->stream));
-    MLC_CUDA(cudaMemsetAsync(hist, 0, 8 * (size_t)nbins, ctx->stream));
+    MLC_CUDA(cudaMemsetAsync(hist, 0, 8 * (size_t)(nbins + 2), ctx->stream));
     if (method == 1) {
       MLC_KSCOPE(ctx, "pairdiff_tc");
       kern<<<grid, NTHREADS, smem, ctx->stream>>>(tmA, tmB, prm);
@@ -608,7 +614,7 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
           MLC_CUDA(cudaMemcpy(out + r0 * NB, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice));
         }
         const long n = nr * NB;
-        const size_t hsm = sizeof(uint32_t) * nbins;
+        const size_t hsm = sizeof(uint32_t) * (nbins + 2);
         set_max_smem((const void*)k_pd_hist_cand, hsm);
         MLC_KSCOPE(ctx, "pd_hist_cand");
         k_pd_hist_cand<<<(int)std::min<long>((n + 255) / 256, (long)ctx->sm_count * 8), 256, hsm, ctx->stream>>>(
@@ -650,6 +656,12 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
     break;
   }
   if (hist_host) MLC_CUDA(cudaMemcpy(hist_host, hist, 8 * (size_t)nbins, cudaMemcpyDeviceToHost));
+  {
+    unsigned long long oor[2];
+    MLC_CUDA(cudaMemcpy(oor, hist + nbins, sizeof oor, cudaMemcpyDeviceToHost));
+    res.below = (long long)oor[0];
+    res.above = (long long)oor[1];
+  }
   // ---- top-k from the candidates: sort by value (stable by candidate order), then order
   // ties by pair index on the host
   if (k > 0) {

@@ -87,6 +87,63 @@ def test_inverse_row_decomposition_matches_irfft(L1, L2, L3):
     np.testing.assert_allclose(row, Nx * x, rtol=0, atol=1e-9 * Nx * np.abs(x).sum())
 
 
+def radix5_levels(b, twx):
+    """c2r5_row (float-float rows of M = 5000 = 8 x 5^4): level 1 as in three_level
+    (inverse DFT8 over stride 625, twiddle W_M^-(j n1)), then in-place decimation-in-frequency
+    radix-5 levels on blocks of 625, 125, 25 (item (block, m): inverse DFT5 over stride J'/5,
+    twiddle W_J'^-(m r), written back to the slots it read) and blocks of 5, whose outputs go
+    to natural order: output r of item it = 125 k1 + 25 a + 5 b + c is z[n0 + 1000 r] with
+    n0 = k1 + 8 (a + 5 (b + 5 c))."""
+    M, J = 5000, 625
+    s = np.empty(M, complex)
+    for j in range(J):
+        v = _dft(b[J * np.arange(8) + j], True)
+        for n1 in range(8):
+            s[n1 * J + j] = v[n1] * np.conj(twx[2 * j * n1])
+    w = twx[16 * np.arange(J)]  # W_625^e
+    for Jp in (625, 125, 25):
+        Sp, ws = Jp // 5, 625 // Jp
+        for it in range(1000):
+            blk, m = divmod(it, Sp)
+            idx = blk * Jp + m + Sp * np.arange(5)
+            u = _dft(s[idx], True)
+            s[idx] = u * np.conj(w[m * np.arange(5) * ws])
+    z = np.empty(M, complex)
+    for it in range(1000):
+        u = _dft(s[5 * it + np.arange(5)], True)
+        k1, a5, b5, c5 = it // 125, (it // 25) % 5, (it // 5) % 5, it % 5
+        z[k1 + 8 * (a5 + 5 * (b5 + 5 * c5)) + 1000 * np.arange(5)] = u
+    return z
+
+
+def test_radix5_last_pass_decomposition_matches_irfft():
+    M = 5000
+    Nx = 2 * M
+    twx = np.exp(-2j * np.pi * np.arange(Nx) / Nx)
+    x = np.random.default_rng(7).lognormal(0.0, 0.5, Nx)
+    X = np.fft.rfft(x)
+    k = np.arange(M)
+    xk, xm = X[k], np.conj(X[M - k])
+    b = (xk + xm) + 1j * (xk - xm) * np.conj(twx[k])
+    z = radix5_levels(b, twx)
+    row = np.empty(Nx)
+    row[0::2], row[1::2] = z.real, z.imag
+    np.testing.assert_allclose(row, Nx * x, rtol=0, atol=1e-9 * Nx * np.abs(x).sum())
+
+
+def test_prime_factor_dft10_matches_fft():
+    """Dft<T, 10>: DFT2 over x[(5 n1 + 2 n2) mod 10], DFT5 over n2, X[(5 k1 + 6 k2) mod 10]."""
+    x = np.random.default_rng(3).normal(size=10) + 1j * np.random.default_rng(4).normal(size=10)
+    for inv in (False, True):
+        a = np.array([x[(2 * n2) % 10] + x[(5 + 2 * n2) % 10] for n2 in range(5)])
+        b = np.array([x[(2 * n2) % 10] - x[(5 + 2 * n2) % 10] for n2 in range(5)])
+        A, B = _dft(a, inv), _dft(b, inv)
+        X = np.empty(10, complex)
+        for k2 in range(5):
+            X[(6 * k2) % 10], X[(5 + 6 * k2) % 10] = A[k2], B[k2]
+        np.testing.assert_allclose(X, _dft(x, inv), rtol=0, atol=1e-12)
+
+
 def _profile_rows(prof, Ny, Nx):
     """ProfileRows: the 2h non-zero rows of the wrapped kernel, compacted (rows j < h are
     kernel rows j, rows j >= h kernel rows Ny - 2h + j), columns wrapped the same way."""

@@ -39,6 +39,11 @@ def test_matrix_matches_oracle(ctx, method, offset, NA, NB, T):
         assert r["stats"]["refined"] < 0.5 * NA * NB  # most values come from the tensor-core path
     counts, near = oracle.histogram(ref, 200, -6, 8, log=True, rel_tol=1e-5)
     assert np.abs(r["hist"].astype(np.int64) - counts.astype(np.int64)).sum() <= 2 * near
+    # every pair is counted once: in a bin, below 10^lo or at/above 10^hi
+    st = r["stats"]
+    assert int(r["hist"].sum()) + st["below"] + st["above"] == NA * NB
+    below = int((ref < 10.0 ** -6).sum()); above = int((ref >= 1e8).sum())
+    assert abs(st["below"] - below) <= near and abs(st["above"] - above) <= near
     idx = oracle.topk_smallest(ref, 20)
     np.testing.assert_allclose(r["topk_val"], ref[idx], rtol=1e-5)
     got_pairs = r["topk_i"] * NB + r["topk_j"]
@@ -58,6 +63,7 @@ def test_tensor_large_with_sampled_threshold(ctx, offset):
     ref = oracle.pair_chi2_magdiff(A, B, w, d, offset)
     counts, near = oracle.histogram(ref, 1000, -4, 8, log=True, rel_tol=1e-5)
     assert int(r["hist"].sum()) == int(counts.sum())
+    assert int(r["hist"].sum()) + r["stats"]["below"] + r["stats"]["above"] == NA * NB
     assert np.abs(r["hist"].astype(np.int64) - counts.astype(np.int64)).sum() <= 2 * near
     idx = oracle.topk_smallest(ref, k)
     np.testing.assert_allclose(r["topk_val"], ref[idx], rtol=1e-5)
