@@ -227,7 +227,7 @@ typedef struct {
 
 #define MLC_IO_HOST 1 /* pixels, the track arrays and out are host memory */
 #define MLC_ASYNC 2   /* return once queued (see below) */
-#define MLC_GRAPH 4   /* mlc_convolve_many: capture / replay the kernel sequence as a CUDA graph */
+#define MLC_GRAPH 4   /* capture / replay the call's kernel sequence as a CUDA graph (device buffers) */
 
 /* The light-curve step of one lensed image in one call -- expanding_source
  * (gpu_functions.cu:82-225) with straight tracks in place of fixed locations:
@@ -249,7 +249,14 @@ typedef struct {
  * computed on host threads and uploaded once per profile list: a call with the same list
  * and map size as the previous call reuses them.  Device memory held: the
  * group's convolved maps and their interleaved copy (2 x min(nprof,16) maps), two track
- * buffers and an output ring of about twice one call's light curves (4 to 64 chunks). */
+ * buffers and an output ring of about twice one call's light curves (4 to 64 chunks).
+ * MLC_GRAPH (device buffers only) runs the call eagerly the first time and then captures
+ * the whole step -- forward spectrum (when pixels is given), both convolution chains, the
+ * last passes, sampling -- into one CUDA graph on an internal stream; later calls with the
+ * same map, pixel, track and output pointers, sizes, profile raster sizes and workspace
+ * replay it with one launch on the context's stream.  The contents of pixels, the track
+ * arrays and the profile values may change between calls; any other change recaptures.
+ * Per-kernel timing (mlc_ctx_set_timing) runs the call eagerly instead. */
 int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof,
                                const mlc_profile* profiles_host, const mlc_tracks* tracks, int mode,
                                int mag, void* out, int flags);
@@ -446,6 +453,38 @@ int mlc_pair_chi2_magdiff(mlc_ctx* ctx, int method, int NA, int NB, int T, const
 int mlc_pair_chi2_magdiff_list(mlc_ctx* ctx, int NA, int NB, int T, const float* A, const float* B,
                                const double* w_host, const double* d_host, int offset, long npairs,
                                const int64_t* ia, const int64_t* ib, double* chi2);
+
+/* Pair sides: one image's curves made ready for the tensor-core pair stage once (centred,
+ * weighted, quantised to sliced integers, with norms and steps) and then paired with any
+ * number of other sides, so that an image taking part in many pairs is prepared once and
+ * an expanding source's curves need never be stored.  No reference counterpart: the
+ * reference stores each image's light curves (expanding_source, gpu_functions.cu:82-225)
+ * and reads both sets for every pair in kernel_chi2 (gpu_functions.cu:700-750).
+ * A side owns one device allocation, made when it is built and freed by
+ * mlc_pair_side_destroy.  The statistic is that of mlc_pair_chi2_magdiff with the same
+ * w and offset; d_host (nullable) enters the side used as B.  T <= 128. */
+typedef struct mlc_pair_side mlc_pair_side;
+
+/* A side from N FP32 curves X (device, N x T row-major). */
+int mlc_pair_side_curves(mlc_ctx* ctx, int N, int T, const float* X, const double* w_host, const double* d_host,
+                         int offset, mlc_pair_side** side);
+
+/* A side straight from an expanding source's convolved FP32 maps (layout as in
+ * mlc_sample_expanding; track arrays FP32): curve r is the magnitudes of track r at the nep
+ * shared epochs t, band-minor (T = nep*nbands), sampled, converted, centred and weighted in
+ * one pass -- the values mlc_sample_expanding with mag != 0 followed by mlc_pair_side_curves
+ * give, bit for bit, without the N x T light curves in memory. */
+int mlc_pair_side_expanding(mlc_ctx* ctx, const float* maps, int Nx, int Ny, int nep, int nbands, int ntracks,
+                            const float* x0, const float* y0, const float* phi, const float* v, const float* t,
+                            const double* w_host, const double* d_host, int offset, mlc_pair_side** side);
+
+int mlc_pair_side_destroy(mlc_pair_side* side);
+
+/* mlc_pair_chi2_magdiff (MLC_PAIR_TENSOR) between two sides built with the same T, w and
+ * offset; A must have been built without d.  Same outputs and statistics. */
+int mlc_pair_chi2_sides(mlc_ctx* ctx, const mlc_pair_side* A, const mlc_pair_side* B, int nbins, double lo_log10,
+                        double hi_log10, uint64_t* hist_host, int k, double* topk_val_host, int64_t* topk_i_host,
+                        int64_t* topk_j_host, float* chi2_out, mlc_pair_stats* stats);
 
 /* ======================================================================= sort / histogram */
 

@@ -432,7 +432,7 @@ TRACK_KEYS = ("x0", "y0", "phi", "v", "off", "t")
 
 
 def convolve_sample_tracks(ctx: Context, m: Map, profiles, tracks: dict, mag=True, pixels=None, out=None,
-                           mode="fused", async_=False):
+                           mode="fused", async_=False, graph=False):
     """The light-curve step of one image in one library call (mlc_convolve_sample_tracks).
 
     tracks: dict of x0, y0, phi, v (map precision), off (int64, ntracks + 1) and t (map
@@ -442,6 +442,9 @@ def convolve_sample_tracks(ctx: Context, m: Map, profiles, tracks: dict, mag=Tru
     location as the tracks) or None to keep the map's.  Returns out[nprof, nepochs].
     Device buffers: stream-ordered on the context's stream.  Host buffers: the call returns
     with out filled, or with async_=True once queued (out valid after ctx.synchronize()).
+    graph=True (device buffers): the step is captured as one CUDA graph after its first
+    eager run and replayed by later calls with the same buffers, sizes and profile raster
+    sizes (contents and profile values may change).
     """
     tr = {k: tracks[k] for k in TRACK_KEYS}
     first = tr["x0"]
@@ -472,7 +475,7 @@ def convolve_sample_tracks(ctx: Context, m: Map, profiles, tracks: dict, mag=Tru
             out = torch.empty((nprof, E), dtype=m.dtype, pin_memory=torch.cuda.is_available())
         else:
             out = torch.empty((nprof, E), dtype=m.dtype, device=first.device)
-    flags = (_lib.MLC_IO_HOST if host else 0) | (_lib.MLC_ASYNC if async_ else 0)
+    flags = (_lib.MLC_IO_HOST if host else 0) | (_lib.MLC_ASYNC if async_ else 0) | (_lib.MLC_GRAPH if graph else 0)
     T = _lib.MlcTracks(ntr, E, *[_ptr(tr[k]) for k in TRACK_KEYS])
     P = (_lib.MlcProfile * nprof)(*profiles)
     md = _MODES[mode]
@@ -607,6 +610,79 @@ def pair_chi2_magdiff(ctx: Context, A: torch.Tensor, B: torch.Tensor, w, d=None,
     ctx.check(ctx.L.mlc_pair_chi2_magdiff(ctx.h, 1 if method == "tensor" else 0, NA, NB, T, _ptr(A.contiguous()),
                                           _ptr(B.contiguous()), _ptr(w), _ptr(dd), int(offset), nbins, lo, hi,
                                           _ptr(hist), k, _ptr(tv), _ptr(ti), _ptr(tj), _ptr(mat), C.byref(st)))
+    return dict(hist=hist, topk_val=tv[:k], topk_i=ti[:k], topk_j=tj[:k], matrix=mat,
+                stats=dict(delta=st.delta, threshold=st.threshold, refined=st.refined, candidates=st.candidates,
+                           passes=st.passes, below=st.below, above=st.above))
+
+
+class PairSide:
+    """One image's curves made ready for the tensor-core pair stage once (centred, weighted,
+    quantised), then paired with any number of sides by pair_chi2_sides.  Built from FP32
+    curves (PairSide.curves) or straight from an expanding source's convolved FP32 maps and
+    tracks (PairSide.expanding), in which case no light curve is stored."""
+
+    def __init__(self, ctx: Context, h, N: int, T: int):
+        self.ctx = ctx
+        self.h = h
+        self.N, self.T = N, T
+        ctx._maps.add(self)
+
+    @classmethod
+    def curves(cls, ctx: Context, X: torch.Tensor, w, d=None, offset: bool = False):
+        if X.dtype != torch.float32 or not X.is_cuda:
+            raise ValueError("pair side curves: a device FP32 tensor")
+        X = X.contiguous()
+        N, T = X.shape
+        w = _np(w, np.float64)
+        dd = None if d is None else _np(d, np.float64)
+        h = C.c_void_p()
+        ctx.check(ctx.L.mlc_pair_side_curves(ctx.h, N, T, _ptr(X), _ptr(w), _ptr(dd), int(offset), C.byref(h)))
+        return cls(ctx, h, N, T)
+
+    @classmethod
+    def expanding(cls, ctx: Context, maps: torch.Tensor, nep: int, nbands: int, x0, y0, phi, v, t, w, d=None,
+                  offset: bool = False):
+        """maps: nep*nbands FP32 planes (Ny x Nx) on the device, plane e*nbands + b for epoch e,
+        band b; track arrays FP32 device tensors; t: the nep shared epochs."""
+        if maps.dtype != torch.float32 or not maps.is_cuda:
+            raise ValueError("pair side maps: a device FP32 tensor")
+        maps = maps.contiguous()
+        Ny, Nx = maps.shape[-2:]
+        if maps.numel() != nep * nbands * Nx * Ny:
+            raise ValueError("pair side maps: nep*nbands planes")
+        trk = [a.contiguous() for a in (x0, y0, phi, v, t)]
+        if any(a.dtype != torch.float32 or not a.is_cuda for a in trk):
+            raise ValueError("pair side tracks: device FP32 tensors")
+        w = _np(w, np.float64)
+        dd = None if d is None else _np(d, np.float64)
+        h = C.c_void_p()
+        ctx.check(ctx.L.mlc_pair_side_expanding(ctx.h, _ptr(maps), Nx, Ny, nep, nbands, trk[0].numel(),
+                                                *[_ptr(a) for a in trk], _ptr(w), _ptr(dd), int(offset),
+                                                C.byref(h)))
+        return cls(ctx, h, trk[0].numel(), nep * nbands)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.mlc_pair_side_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pair_chi2_sides(ctx: Context, A: PairSide, B: PairSide, nbins: int = 1000, lo: float = -2.0, hi: float = 8.0,
+                    k: int = 0, want_matrix: bool = False):
+    """pair_chi2_magdiff (tensor form) between two prepared sides; same dict of results."""
+    from ._lib import MlcPairStats
+    hist = np.zeros(nbins, np.uint64)
+    tv = np.zeros(max(k, 1)); ti = np.zeros(max(k, 1), np.int64); tj = np.zeros(max(k, 1), np.int64)
+    mat = torch.empty((A.N, B.N), dtype=torch.float32, device=f"cuda:{ctx.device}") if want_matrix else None
+    st = MlcPairStats()
+    ctx.check(ctx.L.mlc_pair_chi2_sides(ctx.h, A.h, B.h, nbins, lo, hi, _ptr(hist), k, _ptr(tv), _ptr(ti), _ptr(tj),
+                                        _ptr(mat), C.byref(st)))
     return dict(hist=hist, topk_val=tv[:k], topk_i=ti[:k], topk_j=tj[:k], matrix=mat,
                 stats=dict(delta=st.delta, threshold=st.threshold, refined=st.refined, candidates=st.candidates,
                            passes=st.passes, below=st.below, above=st.above))

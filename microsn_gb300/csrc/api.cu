@@ -4,6 +4,7 @@
 #include <cmath>
 #include <algorithm>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "mlc_internal.h"
@@ -443,7 +444,8 @@ int mlc_convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, i
   if (!ctx || !map || !profiles_host || !tracks) return fail(ctx, MLC_ERR_ARG, "null argument");
   if (nprof < 1) return fail(ctx, MLC_ERR_ARG, "need at least one profile");
   if (mode != MLC_CONV_FUSED && mode != MLC_CONV_PLAIN) return fail(ctx, MLC_ERR_ARG, "unknown convolution mode");
-  if (flags & ~(MLC_IO_HOST | MLC_ASYNC)) return fail(ctx, MLC_ERR_ARG, "unknown flags");
+  if (flags & ~(MLC_IO_HOST | MLC_ASYNC | MLC_GRAPH)) return fail(ctx, MLC_ERR_ARG, "unknown flags");
+  if ((flags & MLC_GRAPH) && (flags & MLC_IO_HOST)) return fail(ctx, MLC_ERR_ARG, "MLC_GRAPH takes device buffers only");
   const mlc_tracks& tr = *tracks;
   if (tr.ntracks < 0 || tr.nepochs < 0) return fail(ctx, MLC_ERR_ARG, "negative track or epoch count");
   if (tr.ntracks > 0 && (!tr.x0 || !tr.y0 || !tr.phi || !tr.v || !tr.off || (tr.nepochs > 0 && !tr.t) || !out))
@@ -669,6 +671,83 @@ int mlc_pair_chi2_magdiff_list(mlc_ctx* ctx, int NA, int NB, int T, const float*
     if (d_host) MLC_CUDA(cudaMemcpy(buf + T, d_host, sizeof(double) * T, cudaMemcpyHostToDevice));
     pairdiff_plain(ctx, A, B, NA, NB, T, buf, d_host ? buf + T : nullptr, W, offset, npairs, (const long*)ia,
                    (const long*)ib, chi2);
+  });
+}
+
+struct mlc_pair_side {
+  int device = 0;
+  PdSide s;
+};
+
+namespace {
+int side_new(mlc_ctx* ctx, mlc_pair_side** out, const std::function<void(PdSide&)>& build) {
+  mlc_pair_side* sd = new mlc_pair_side;
+  sd->device = ctx->device;
+  const int st = guarded(ctx, [&] { build(sd->s); });
+  if (st != MLC_OK) {
+    delete sd;
+    return st;
+  }
+  *out = sd;
+  return MLC_OK;
+}
+}  // namespace
+
+int mlc_pair_side_curves(mlc_ctx* ctx, int N, int T, const float* X, const double* w_host, const double* d_host,
+                         int offset, mlc_pair_side** side) {
+  if (!ctx || !X || !w_host || !side) return fail(ctx, MLC_ERR_ARG, "null argument");
+  *side = nullptr;
+  if (N < 1 || T < 1) return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  if (T > 128) return fail(ctx, MLC_ERR_LIMIT, "pair sides support T <= 128 epochs");
+  return side_new(ctx, side, [&](PdSide& s) { pd_side_from_curves(ctx, X, N, T, w_host, d_host, offset, s); });
+}
+
+int mlc_pair_side_expanding(mlc_ctx* ctx, const float* maps, int Nx, int Ny, int nep, int nbands, int ntracks,
+                            const float* x0, const float* y0, const float* phi, const float* v, const float* t,
+                            const double* w_host, const double* d_host, int offset, mlc_pair_side** side) {
+  if (!ctx || !maps || !x0 || !y0 || !phi || !v || !t || !w_host || !side)
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  *side = nullptr;
+  if (Nx < 2 || Ny < 2 || nep < 1 || nbands < 1 || ntracks < 1) return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  if ((long)nep * nbands > 128) return fail(ctx, MLC_ERR_LIMIT, "pair sides support nep*nbands <= 128");
+  return side_new(ctx, side, [&](PdSide& s) {
+    pd_side_from_expanding(ctx, maps, Nx, Ny, nep, nbands, ntracks, x0, y0, phi, v, t, w_host, d_host, offset, s);
+  });
+}
+
+int mlc_pair_side_destroy(mlc_pair_side* side) {
+  if (!side) return MLC_ERR_ARG;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(side->device);
+  pd_side_free(side->s);
+  if (prev >= 0) cudaSetDevice(prev);
+  delete side;
+  return MLC_OK;
+}
+
+int mlc_pair_chi2_sides(mlc_ctx* ctx, const mlc_pair_side* A, const mlc_pair_side* B, int nbins, double lo_log10,
+                        double hi_log10, uint64_t* hist_host, int k, double* topk_val_host, int64_t* topk_i_host,
+                        int64_t* topk_j_host, float* chi2_out, mlc_pair_stats* stats) {
+  if (!ctx || !A || !B || (k > 0 && (!topk_val_host || !topk_i_host || !topk_j_host)))
+    return fail(ctx, MLC_ERR_ARG, "null argument");
+  if (A->device != ctx->device || B->device != ctx->device)
+    return fail(ctx, MLC_ERR_ARG, "pair side built on another device");
+  if (k < 0 || nbins < 1 || !(hi_log10 > lo_log10)) return fail(ctx, MLC_ERR_ARG, "bad sizes");
+  if ((long long)A->s.N * B->s.N > (1LL << 40)) return fail(ctx, MLC_ERR_LIMIT, "more than 2^40 pairs");
+  return guarded(ctx, [&] {
+    PdResult r;
+    pairdiff_sides(ctx, A->s, B->s, nbins, lo_log10, hi_log10, hist_host, k, topk_val_host, topk_i_host, topk_j_host,
+                   chi2_out, r);
+    if (stats) {
+      stats->delta = r.delta;
+      stats->threshold = r.thr;
+      stats->refined = r.nrefined;
+      stats->candidates = r.ncand;
+      stats->passes = r.passes;
+      stats->below = r.below;
+      stats->above = r.above;
+    }
   });
 }
 

@@ -26,6 +26,14 @@
 
 namespace mlc {
 
+// One captured kernel sequence: the key of pointers and sizes it was captured with, the
+// executable graph and the number of our kernels in it.
+struct GraphSlot {
+  std::vector<uint64_t> key;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long launches = 0;
+};
+
 struct BatchIO {
   // Output ring: enough slots for about two calls' light curves (4 to 64 slots), so that
   // the sampling of one call never waits for its own downloads and the next call's
@@ -61,12 +69,10 @@ struct BatchIO {
   std::vector<int> prof_N;
   std::vector<size_t> prof_off;
   int parity = 0;
-  // the kernel sequence of the last mlc_convolve_many call with MLC_GRAPH, replayed while
-  // every pointer and size it baked in stays the same
+  // the kernel sequences of the last mlc_convolve_many and mlc_convolve_sample_tracks calls
+  // with MLC_GRAPH, each replayed while every pointer and size it baked in stays the same
   cudaStream_t cap = nullptr;
-  std::vector<uint64_t> graph_key;
-  cudaGraphExec_t graph = nullptr;
-  unsigned long long graph_launches = 0;  // kernels in the graph
+  GraphSlot many, step;
 };
 
 static void ev_create(cudaEvent_t* e) { MLC_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming)); }
@@ -140,7 +146,8 @@ void batch_release(mlc_ctx* ctx) {
   if (b->aux) cudaStreamDestroy(b->aux);
   if (b->tail) cudaStreamDestroy(b->tail);
   if (b->prof_dev) cudaFree(b->prof_dev);
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (GraphSlot* g : {&b->many, &b->step})
+    if (g->exec) cudaGraphExecDestroy(g->exec);
   if (b->cap) cudaStreamDestroy(b->cap);
   if (b->h2d) cudaStreamDestroy(b->h2d);
   if (b->d2h) cudaStreamDestroy(b->d2h);
@@ -266,7 +273,13 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     fft2_forward(ctx, *p, map->data, map->prec, map->spec);
     map->spec_valid = true;
   }
-  MLC_CUDA(cudaEventRecord(b->pix_free, ctx->stream));
+  {
+    // (not while the sequence is being captured into a graph: an event recorded in a
+    // capture may not be waited on by the uncaptured host-buffer path)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    MLC_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) MLC_CUDA(cudaEventRecord(b->pix_free, ctx->stream));
+  }
 
   // ---- tracks
   const char* x0 = (const char*)tr.x0;
@@ -441,10 +454,86 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
   if (host && !(flags & MLC_ASYNC)) sync_all(ctx, b);
 }
 
+// Replays the slot's graph when key() matches the key it was captured with; otherwise runs
+// enqueue() eagerly (this call's result, and the run that sizes every workspace and fills
+// every cache the sequence consults), then captures a second enqueue() on the internal
+// stream -- streams that the sequence forks to through events join the capture -- and
+// keeps the instantiated graph for later calls.  Nothing is allocated or synchronised
+// while capturing: every buffer exists after the eager run and the key holds their
+// addresses.
+template <typename Enq, typename Key>
+static void run_graph(mlc_ctx* ctx, BatchIO* b, GraphSlot& slot, Enq&& enqueue, Key&& key) {
+  if (slot.exec && slot.key == key()) {
+    ctx->launches += slot.launches;
+    MLC_CUDA(cudaGraphLaunch(slot.exec, ctx->stream));
+    return;
+  }
+  const unsigned long long l0 = ctx->launches;
+  enqueue();
+  const unsigned long long nl = ctx->launches - l0;
+  if (slot.exec) {
+    MLC_CUDA(cudaGraphExecDestroy(slot.exec));
+    slot.exec = nullptr;
+  }
+  const unsigned long long launches = ctx->launches;
+  // the capture stream starts after the eager run (the graph launch itself goes on the
+  // context's stream later; the capture only records)
+  cudaStream_t saved = ctx->stream;
+  ctx->stream = b->cap;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    try {
+      enqueue();
+    } catch (...) {
+      cudaStreamEndCapture(b->cap, &g);
+      if (g) cudaGraphDestroy(g);
+      ctx->stream = saved;
+      ctx->launches = launches;
+      throw;
+    }
+    e = cudaStreamEndCapture(b->cap, &g);
+  }
+  ctx->stream = saved;
+  ctx->launches = launches;
+  MLC_CUDA(e);
+  e = cudaGraphInstantiate(&slot.exec, g, 0);
+  cudaGraphDestroy(g);
+  MLC_CUDA(e);
+  slot.key = key();
+  slot.launches = nl;
+}
+
 void convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const mlc_profile* profs,
                             const mlc_tracks& tr, int mode, int mag, void* out, int flags) {
-  if (map->prec == MLC_F64) run<double>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags);
-  else run<float>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags);
+  auto go = [&] {
+    if (map->prec == MLC_F64) run<double>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags & ~MLC_GRAPH);
+    else run<float>(ctx, map, pixels, nprof, profs, tr, mode, mag, out, flags & ~MLC_GRAPH);
+  };
+  if (!(flags & MLC_GRAPH) || ctx->timing) {
+    go();
+    return;
+  }
+  MLC_REQUIRE(!(flags & MLC_IO_HOST), MLC_ERR_ARG, "MLC_GRAPH takes device buffers only");
+  BatchIO* b = batch_get(ctx);
+  // the rasters first (host work, and an upload when the list changed): the graph reads
+  // them from the same device buffer
+  std::vector<int> pN;
+  std::vector<size_t> poff;
+  const double* dprof = stage_profiles(ctx, b, b->parity, nprof, profs, map->Nx, map->Ny, pN, poff);
+  auto key = [&] {
+    std::vector<uint64_t> kv = {(uint64_t)map,      (uint64_t)map->data, (uint64_t)map->spec, (uint64_t)pixels,
+                                (uint64_t)nprof,    (uint64_t)mode,      (uint64_t)mag,       (uint64_t)out,
+                                (uint64_t)tr.x0,    (uint64_t)tr.y0,     (uint64_t)tr.phi,    (uint64_t)tr.v,
+                                (uint64_t)tr.off,   (uint64_t)tr.t,      (uint64_t)tr.ntracks, (uint64_t)tr.nepochs,
+                                (uint64_t)dprof,    (uint64_t)map_fft_prec(map), (uint64_t)ctx->autotune};
+    for (int s = 0; s < WS_NSLOTS; s++) kv.push_back((uint64_t)ctx->ws_ptr[s]);
+    for (int k = 0; k < nprof; k++) kv.push_back((uint64_t)pN[k]);
+    return kv;
+  };
+  run_graph(ctx, b, b->step, go, key);
+  if (!pixels) return;
+  map->spec_valid = true;  // the replayed forward transform has refreshed the spectrum
 }
 
 // Convolutions of one map with many profiles into out + k * stride (the map's precision):
@@ -481,42 +570,7 @@ void convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* pro
     enqueue();
     return;
   }
-  if (b->graph && b->graph_key == key()) {
-    ctx->launches += b->graph_launches;
-    MLC_CUDA(cudaGraphLaunch(b->graph, ctx->stream));
-    return;
-  }
-  const unsigned long long l0 = ctx->launches;
-  enqueue();  // this call's result; also grows every workspace slot the sequence uses
-  const unsigned long long nl = ctx->launches - l0;
-  if (b->graph) {
-    MLC_CUDA(cudaGraphExecDestroy(b->graph));
-    b->graph = nullptr;
-  }
-  const unsigned long long launches = ctx->launches;
-  cudaStream_t saved = ctx->stream;
-  ctx->stream = b->cap;
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal);
-  if (e == cudaSuccess) {
-    try {
-      enqueue();
-    } catch (...) {
-      cudaStreamEndCapture(b->cap, &g);
-      if (g) cudaGraphDestroy(g);
-      ctx->stream = saved;
-      throw;
-    }
-    e = cudaStreamEndCapture(b->cap, &g);
-  }
-  ctx->stream = saved;
-  ctx->launches = launches;
-  MLC_CUDA(e);
-  e = cudaGraphInstantiate(&b->graph, g, 0);
-  cudaGraphDestroy(g);
-  MLC_CUDA(e);
-  b->graph_key = key();
-  b->graph_launches = nl;
+  run_graph(ctx, b, b->many, enqueue, key);
 }
 
 void ctx_join(mlc_ctx* ctx) {

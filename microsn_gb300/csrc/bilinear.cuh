@@ -1,5 +1,5 @@
-// Bilinear sampling weights shared by the track sampler (sample.cu) and the
-// differentiable track fit (fit.cu).
+// Bilinear sampling weights shared by the track samplers (sample.cu, and the pair sides
+// of pairdiff.cu) and the differentiable track fit (fit.cu).
 #pragma once
 
 #include "mlc_common.cuh"
@@ -20,12 +20,18 @@ struct Bilin {
   bool inside;
 };
 
+// Whole numbers to 64-bit integers.  FP32 goes through a 32-bit integer: F2I.S64 runs on
+// the FP64 pipe, F2I.S32 does not.  FP32 offsets are fractions here, and FP32 track
+// coordinates stay far inside +-2^31 pixels; FP64 ones may not, and convert directly.
+__device__ __forceinline__ long floor_to_long(float f) { return (long)(int)f; }
+__device__ __forceinline__ long floor_to_long(double f) { return (long)f; }
+
 template <typename T>
 __device__ __forceinline__ Bilin<T> bilin_weights(long bx, T fx, long by, T fy, int Nx, int Ny) {
   Bilin<T> B;
   // absolute coordinate = b + f ; hull of centres is [0.5, N - 0.5]
   const T flx = floor(fx), fly = floor(fy);
-  const long jx = bx + (long)flx, iy = by + (long)fly;  // pixel containing the point
+  const long jx = bx + floor_to_long(flx), iy = by + floor_to_long(fly);  // pixel containing the point
   const T rx = fx - flx, ry = fy - fly;                 // in [0, 1)
   B.inside = !((jx < 0) || (jx == 0 && rx < (T)0.5) || (jx > Nx - 1) || (jx == Nx - 1 && rx > (T)0.5) ||
                (iy < 0) || (iy == 0 && ry < (T)0.5) || (iy > Ny - 1) || (iy == Ny - 1 && ry > (T)0.5));
@@ -48,6 +54,16 @@ __device__ __forceinline__ Bilin<T> bilin_weights(long bx, T fx, long by, T fy, 
   B.w2 = b * c;
   B.w3 = a * c;
   return B;
+}
+
+// The bilinear value of one map at the weights B (points outside the hull are the caller's).
+template <typename T>
+__device__ __forceinline__ T bilin_read(const T* __restrict__ m, const Bilin<T>& B, int Nx) {
+  T z = B.w0 * __ldg(m + (long)B.iu * Nx + B.jl);
+  z += B.w1 * __ldg(m + (long)B.iu * Nx + B.jr);
+  z += B.w2 * __ldg(m + (long)B.il * Nx + B.jl);
+  z += B.w3 * __ldg(m + (long)B.il * Nx + B.jr);
+  return z;
 }
 
 // sin and cos of an FP32 angle as float-float pairs, our own evaluation: Cody-Waite
@@ -112,7 +128,7 @@ __device__ __forceinline__ float track_offset(float f0, float t, ff vc, long* d)
   const ff x = ff(f0, 0.f) + ff(ph, __fmaf_rn(t, vc.lo, __fmaf_rn(t, vc.hi, -ph)));
   const float fl = floorf(x.hi);
   float r = __fadd_rn(__fsub_rn(x.hi, fl), x.lo);
-  long dd = (long)fl;
+  long dd = floor_to_long(fl);
   if (r < 0.f) {
     r = __fadd_rn(r, 1.f);
     dd -= 1;
@@ -158,8 +174,8 @@ struct TrackGeom<float> {
     sincos_ff(phi, &s, &c);
     vc = ff_norm(ff(V, 0.f) * c);
     vs = ff_norm(ff(V, 0.f) * s);
-    bx = (long)floorf(X0);
-    by = (long)floorf(Y0);
+    bx = floor_to_long(floorf(X0));
+    by = floor_to_long(floorf(Y0));
     fx0 = X0 - (float)bx;  // exact
     fy0 = Y0 - (float)by;
   }

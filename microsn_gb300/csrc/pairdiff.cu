@@ -13,8 +13,10 @@
 // weighting in FP64, a power-of-two quantisation step per curve, 24-bit integers split
 // into three signed 8-bit slices stored as bf16 (exact), and the exact squared norms.
 #include <cmath>
+#include <cstring>
 #include <vector>
 
+#include "bilinear.cuh"
 #include "mlc_internal.h"
 #include "pairdiff.h"
 
@@ -178,10 +180,12 @@ double pairdiff_prepare(mlc_ctx* ctx, const float* A, const float* B, int NA, in
   double* dw = dsw + T;
   double* dd = dw + T;
   double* rowmax = dd + T;
+  // on the context's stream (which may not synchronise with the legacy default stream),
+  // then waited for: the host vectors are freed on return
+  MLC_CUDA(cudaMemcpyAsync(dsw, sw.data(), sizeof(double) * T, cudaMemcpyHostToDevice, ctx->stream));
+  MLC_CUDA(cudaMemcpyAsync(dw, w.data(), sizeof(double) * T, cudaMemcpyHostToDevice, ctx->stream));
+  MLC_CUDA(cudaMemcpyAsync(dd, d.data(), sizeof(double) * T, cudaMemcpyHostToDevice, ctx->stream));
   MLC_CUDA(cudaStreamSynchronize(ctx->stream));
-  MLC_CUDA(cudaMemcpy(dsw, sw.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
-  MLC_CUDA(cudaMemcpy(dw, w.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
-  MLC_CUDA(cudaMemcpy(dd, d.data(), sizeof(double) * T, cudaMemcpyHostToDevice));
   // centred, weighted curves (FP64), both sides
   double* cen = (double*)ws_get(ctx, WS_KREAL, sizeof(double) * ((size_t)NA + NB) * T);
   {
@@ -211,6 +215,8 @@ double pairdiff_prepare(mlc_ctx* ctx, const float* A, const float* B, int NA, in
   memcpy(&mx, &hm, 8);
   const double delta = mx > 0 ? std::exp2(std::ceil(std::log2(mx / (double)PD_QMAX))) : 1.0;
   ops.delta = delta;
+  ops.cenA = cen;
+  ops.cenB = cen + (size_t)NA * T;
   // operands, norms, float-float norms and exponents
   const size_t rowsA = ops.NApad, rowsB = ops.NBpad;
   ops.a = (uint16_t*)ws_get(ctx, WS_PAIR_ACC, sizeof(uint16_t) * 3 * ops.Kp * (rowsA + rowsB) +
@@ -240,6 +246,194 @@ double pairdiff_prepare(mlc_ctx* ctx, const float* A, const float* B, int NA, in
   MLC_REQUIRE(herr != 2, MLC_ERR_LIMIT, "curve amplitudes beyond 2^20 * 8355711 (after weighting)");
   MLC_REQUIRE(herr == 0, MLC_ERR_ARG, "non-finite curve values");
   return delta;
+}
+
+// ---------------------------------------------------------------- sides built once per image
+
+// The sample -> magnitude -> centre/weight pass of one expanding-source curve per warp, from
+// the convolved maps (no light curve stored): curve r = the magnitudes of track r at the nep
+// shared epochs t, band-minor (element e nbands + b), sampled like k_sample_expanding
+// (sample.cu) and centred and weighted like k_pd_center -- the same arithmetic in the same
+// order (lane l takes elements l, l + 32, ...), so the centred curves are those of the
+// two-stage path bit for bit.  T = nep nbands <= 128.
+__global__ void __launch_bounds__(256) k_pd_center_expanding(const float* __restrict__ maps, long npix, int Nx,
+                                                             int Ny, int nbands, int nep, int N,
+                                                             const float* __restrict__ x0,
+                                                             const float* __restrict__ y0,
+                                                             const float* __restrict__ phi,
+                                                             const float* __restrict__ v,
+                                                             const float* __restrict__ t,
+                                                             const double* __restrict__ sw,
+                                                             const double* __restrict__ w,
+                                                             const double* __restrict__ d, double W, int offset,
+                                                             double* __restrict__ out,
+                                                             double* __restrict__ rowmax) {
+  constexpr int PER = 4;  // elements per lane: T <= 128
+  const int lane = threadIdx.x & 31;
+  const long r = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (r >= N) return;
+  const int T = nep * nbands;
+  const TrackGeom<float> g(x0[r], y0[r], phi[r], v[r]);
+  float x[PER];
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int q = lane + 32 * i;
+    x[i] = 0.f;
+    if (q < T) {
+      const int e = q / nbands, b = q - e * nbands;
+      const Bilin<float> B = g.at(t[e], Nx, Ny);
+      const float mu = B.inside ? bilin_read<float>(maps + (long)(e * nbands + b) * npix, B, Nx) : 0.f;
+      x[i] = -2.5f * mlc_log10(mu);
+    }
+  }
+  double mean = 0.0;
+  if (offset) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < PER; i++) {
+      const int q = lane + 32 * i;
+      if (q < T) s += w[q] * ((double)x[i] + (d ? d[q] : 0.0));
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    mean = s / W;
+  }
+  double mx = 0.0;
+#pragma unroll
+  for (int i = 0; i < PER; i++) {
+    const int q = lane + 32 * i;
+    if (q < T) {
+      const double vv = sw[q] * ((double)x[i] + (d ? d[q] : 0.0) - mean);
+      out[r * T + q] = vv;
+      mx = fmax(mx, fabs(vv));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) rowmax[r] = mx;
+}
+
+namespace {
+
+// One device allocation for a side: weight tables (sqrt w, w, d), centred curves, row
+// maxima, operands, norms, steps and the max/error words; sizes from N and T.
+void side_alloc(mlc_ctx* ctx, PdSide& sd, int N, int T, const double* w_host, const double* d_host, int offset, double& W) {
+  MLC_REQUIRE(N >= 1 && T >= 1 && T <= 128, MLC_ERR_LIMIT, "pair side: N >= 1 and 1 <= T <= 128");
+  sd.N = N;
+  sd.T = T;
+  sd.Kp = (int)round_up(T, 64);
+  sd.Npad = (int)round_up(N, PD_SIDE_PAD);
+  sd.offset = offset != 0;
+  sd.has_d = d_host != nullptr;
+  sd.w.assign(w_host, w_host + T);
+  W = 0.0;
+  for (int i = 0; i < T; i++) {
+    MLC_REQUIRE(sd.w[i] >= 0 && std::isfinite(sd.w[i]), MLC_ERR_ARG, "weights must be finite and >= 0");
+    W += sd.w[i];
+  }
+  MLC_REQUIRE(W > 0, MLC_ERR_ARG, "weights sum to zero");
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t b_tab = al(sizeof(double) * 3 * T), b_cen = al(sizeof(double) * (size_t)N * T),
+               b_max = al(sizeof(double) * N), b_ops = al(sizeof(uint16_t) * 3 * (size_t)sd.Kp * sd.Npad),
+               b_n2 = al(sizeof(long long) * sd.Npad), b_nff = al(sizeof(float2) * sd.Npad),
+               b_ex = al(sizeof(int) * sd.Npad), b_fl = 256;
+  sd.bytes = b_tab + b_cen + b_max + b_ops + b_n2 + b_nff + b_ex + b_fl;
+  MLC_CUDA(cudaMalloc(&sd.mem, sd.bytes));
+  char* p = (char*)sd.mem + b_tab;
+  sd.cen = (double*)p;
+  p += b_cen;
+  sd.rowmax = (double*)p;
+  p += b_max;
+  sd.ops = (uint16_t*)p;
+  p += b_ops;
+  sd.norm2 = (long long*)p;
+  p += b_n2;
+  sd.norm2_ff = (float2*)p;
+  p += b_nff;
+  sd.exps = (int*)p;
+  std::vector<double> tab(3 * (size_t)T, 0.0);
+  for (int i = 0; i < T; i++) {
+    tab[i] = std::sqrt(sd.w[i]);
+    tab[T + i] = sd.w[i];
+    if (d_host) tab[2 * T + i] = d_host[i];
+  }
+  MLC_CUDA(cudaMemcpyAsync(sd.mem, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));  // tab is freed on return
+}
+
+// The reported step from the largest row maximum, then the sliced integers (as in
+// pairdiff_prepare; every row keeps its own step).
+void side_finish(mlc_ctx* ctx, PdSide& sd) {
+  unsigned long long* gmax = (unsigned long long*)((char*)sd.mem + sd.bytes - 256);
+  int* derr = (int*)(gmax + 1);
+  MLC_CUDA(cudaMemsetAsync(gmax, 0, 16, ctx->stream));
+  {
+    MLC_KSCOPE(ctx, "pd_maxreduce");
+    k_pd_maxreduce<<<std::max(1, std::min(ceil_div(sd.N, 256), ctx->sm_count * 4)), 256, 0, ctx->stream>>>(
+        sd.rowmax, (long)sd.N, gmax);
+  }
+  {
+    MLC_KSCOPE(ctx, "pd_quantize");
+    k_pd_quantize<<<ceil_div(sd.Npad, 8), 256, 0, ctx->stream>>>(sd.cen, sd.rowmax, sd.N, sd.Npad, sd.T, sd.Kp, sd.ops,
+                                                                 sd.norm2, sd.norm2_ff, sd.exps, derr);
+  }
+  MLC_CHECK_LAUNCH();
+  unsigned long long hm[2] = {0, 0};
+  MLC_CUDA(cudaMemcpyAsync(hm, gmax, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  double mx;
+  std::memcpy(&mx, &hm[0], 8);
+  int herr;
+  std::memcpy(&herr, &hm[1], sizeof herr);
+  sd.delta = mx > 0 ? std::exp2(std::ceil(std::log2(mx / (double)PD_QMAX))) : 1.0;
+  MLC_REQUIRE(herr != 2, MLC_ERR_LIMIT, "curve amplitudes beyond 2^20 * 8355711 (after weighting)");
+  MLC_REQUIRE(herr == 0, MLC_ERR_ARG, "non-finite curve values");
+}
+
+}  // namespace
+
+void pd_side_free(PdSide& sd) {
+  if (sd.mem) cudaFree(sd.mem);
+  sd.mem = nullptr;
+}
+
+void pd_side_from_curves(mlc_ctx* ctx, const float* X, int N, int T, const double* w_host, const double* d_host,
+                         int offset, PdSide& sd) {
+  double W;
+  side_alloc(ctx, sd, N, T, w_host, d_host, offset, W);
+  try {
+    const double* tab = (const double*)sd.mem;
+    {
+      MLC_KSCOPE(ctx, "pd_center");
+      k_pd_center<<<ceil_div(N, 8), 256, 0, ctx->stream>>>(X, N, T, tab, tab + T, d_host ? tab + 2 * T : nullptr, W,
+                                                           sd.offset, sd.cen, sd.rowmax);
+    }
+    MLC_CHECK_LAUNCH();
+    side_finish(ctx, sd);
+  } catch (...) {
+    pd_side_free(sd);
+    throw;
+  }
+}
+
+void pd_side_from_expanding(mlc_ctx* ctx, const float* maps, int Nx, int Ny, int nep, int nbands, int ntracks,
+                            const float* x0, const float* y0, const float* phi, const float* v, const float* t,
+                            const double* w_host, const double* d_host, int offset, PdSide& sd) {
+  MLC_REQUIRE(nep >= 1 && nbands >= 1 && Nx >= 2 && Ny >= 2, MLC_ERR_ARG, "pair side: bad map or epoch sizes");
+  double W;
+  side_alloc(ctx, sd, ntracks, nep * nbands, w_host, d_host, offset, W);
+  try {
+    const double* tab = (const double*)sd.mem;
+    {
+      MLC_KSCOPE(ctx, "pd_center_expanding");
+      k_pd_center_expanding<<<ceil_div(ntracks, 8), 256, 0, ctx->stream>>>(
+          maps, (long)Nx * Ny, Nx, Ny, nbands, nep, ntracks, x0, y0, phi, v, t, tab, tab + sd.T,
+          d_host ? tab + 2 * sd.T : nullptr, W, sd.offset, sd.cen, sd.rowmax);
+    }
+    MLC_CHECK_LAUNCH();
+    side_finish(ctx, sd);
+  } catch (...) {
+    pd_side_free(sd);
+    throw;
+  }
 }
 
 }  // namespace mlc

@@ -3,6 +3,8 @@
 
 #include <stdint.h>
 
+#include <vector>
+
 #include "mlc_internal.h"
 
 namespace mlc {
@@ -27,6 +29,27 @@ struct PdOperands {
   float2* beta_ff = nullptr;
   int* ea = nullptr;           // step exponent per A row
   int* eb = nullptr;           // step exponent per B row
+  const double* cenA = nullptr;  // NA x T centred, weighted curves (FP64), for the exact list
+  const double* cenB = nullptr;  // NB x T
+};
+
+// The operands of one image's curves ("side"), built once and used by every pair it takes
+// part in: centred, weighted curves, their sliced integers, norms and steps, in one device
+// allocation of `bytes` at `mem` (owned by the side).  Rows are padded to PD_SIDE_PAD, a
+// multiple of both tile heights, so a side serves as A or as B.
+constexpr int PD_SIDE_PAD = 384;
+struct PdSide {
+  int N = 0, Npad = 0, T = 0, Kp = 0, offset = 0, has_d = 0;
+  double delta = 1.0;     // largest step 2^e of its curves
+  std::vector<double> w;  // the weights it was built with (host)
+  double* cen = nullptr;
+  double* rowmax = nullptr;
+  uint16_t* ops = nullptr;
+  long long* norm2 = nullptr;
+  float2* norm2_ff = nullptr;
+  int* exps = nullptr;
+  void* mem = nullptr;
+  size_t bytes = 0;
 };
 
 struct PdResult {
@@ -39,6 +62,20 @@ struct PdResult {
 void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int NA, int NB, int T,
                   const double* w_host, const double* d_host, int offset, int nbins, double lo, double hi,
                   uint64_t* hist_host, int k, double* tv, int64_t* ti, int64_t* tj, float* out, PdResult& res);
+
+// A side from FP32 curves (N x T, row-major), or straight from the convolved maps of an
+// expanding source (maps: nep x nbands planes of Ny x Nx FP32; curve r of track r is its
+// magnitudes at the nep shared epochs t, band-minor): sampled, converted to magnitudes,
+// centred and weighted in one pass, no light curve stored.  d_host (nullable): the observed
+// difference curve, for a side used as B only.  The side's memory is allocated here.
+void pd_side_from_curves(mlc_ctx* ctx, const float* X, int N, int T, const double* w_host, const double* d_host,
+                         int offset, PdSide& side);
+void pd_side_from_expanding(mlc_ctx* ctx, const float* maps, int Nx, int Ny, int nep, int nbands, int ntracks,
+                            const float* x0, const float* y0, const float* phi, const float* v, const float* t,
+                            const double* w_host, const double* d_host, int offset, PdSide& side);
+void pd_side_free(PdSide& side);
+void pairdiff_sides(mlc_ctx* ctx, const PdSide& A, const PdSide& B, int nbins, double lo, double hi,
+                    uint64_t* hist_host, int k, double* tv, int64_t* ti, int64_t* tj, float* out, PdResult& res);
 
 double pairdiff_prepare(mlc_ctx* ctx, const float* A, const float* B, int NA, int NB, int T, const double* w_host,
                         const double* d_host, int offset, PdOperands& ops);

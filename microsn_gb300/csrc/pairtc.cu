@@ -344,8 +344,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
   }
 }
 
-// Exact FP64 chi2 of listed pairs from the centred, weighted curves (P = cen[i], Q = cen[NA + j]).
-__global__ void __launch_bounds__(256) k_pd_refine(const double* __restrict__ cen, int NA, int T, const int* __restrict__ ri,
+// Exact FP64 chi2 of listed pairs from the centred, weighted curves (P = cenA[i], Q = cenB[j]).
+__global__ void __launch_bounds__(256) k_pd_refine(const double* __restrict__ cenA, const double* __restrict__ cenB,
+                                                   int T, const int* __restrict__ ri,
                                                    const int* __restrict__ rj, unsigned n, int nbins, double lo,
                                                    double width, unsigned long long* __restrict__ hist, float thr,
                                                    unsigned cap, unsigned* __restrict__ ncand, float* __restrict__ cval,
@@ -353,8 +354,8 @@ __global__ void __launch_bounds__(256) k_pd_refine(const double* __restrict__ ce
                                                    int NB) {
   for (unsigned p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
     const int i = ri[p], j = rj[p];
-    const double* a = cen + (long)i * T;
-    const double* b = cen + ((long)NA + j) * T;
+    const double* a = cenA + (long)i * T;
+    const double* b = cenB + (long)j * T;
     double s = 0.0;
     for (int t = 0; t < T; t++) {
       const double r = b[t] - a[t];
@@ -380,7 +381,8 @@ __global__ void __launch_bounds__(256) k_pd_refine(const double* __restrict__ ce
 }
 
 // chi2 of pseudo-random pairs (integer hash of the sample index) for the top-k threshold.
-__global__ void __launch_bounds__(256) k_pd_sample(const double* __restrict__ cen, int NA, int NB, int T, long S,
+__global__ void __launch_bounds__(256) k_pd_sample(const double* __restrict__ cenA, const double* __restrict__ cenB,
+                                                   int NA, int NB, int T, long S,
                                                    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < S; p += (long)gridDim.x * blockDim.x) {
     uint64_t z = (uint64_t)p * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
@@ -388,8 +390,8 @@ __global__ void __launch_bounds__(256) k_pd_sample(const double* __restrict__ ce
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
     z ^= z >> 31;
     const int i = (int)((z & 0xFFFFFFFFull) % (uint64_t)NA), j = (int)((z >> 32) % (uint64_t)NB);
-    const double* a = cen + (long)i * T;
-    const double* b = cen + ((long)NA + j) * T;
+    const double* a = cenA + (long)i * T;
+    const double* b = cenB + (long)j * T;
     double s = 0.0;
     for (int t = 0; t < T; t++) {
       const double r = b[t] - a[t];
@@ -484,20 +486,16 @@ CUtensorMap make_map(void* base, int rows, int kcols, int box_rows) {
 
 }  // namespace
 
-// Tensor-core pair chi2 with fused log10-chi2 histogram and top-k.
-void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int NA, int NB, int T,
-                  const double* w_host, const double* d_host, int offset, int nbins, double lo, double hi,
-                  uint64_t* hist_host, int k, double* tv, int64_t* ti, int64_t* tj, float* out, PdResult& res) {
-  MLC_REQUIRE(method == 1 || T <= 4096, MLC_ERR_LIMIT, "T <= 4096");
-  MLC_REQUIRE(method == 0 || (T >= 1 && T <= MAX_KP), MLC_ERR_LIMIT,
-              "tensor-core pair chi2 supports T <= 128 epochs");
-  MLC_REQUIRE(nbins >= 1 && nbins <= MAX_BINS && hi > lo, MLC_ERR_ARG, "histogram: 1..4096 bins, hi > lo");
-  MLC_REQUIRE(NA >= 1 && NB >= 1 && k >= 0, MLC_ERR_ARG, "bad sizes");
-  PdOperands ops;
-  const double delta = pairdiff_prepare(ctx, A, B, NA, NB, T, w_host, d_host, offset, ops);
-  res.delta = delta;
+// Pair chi2 from prepared operands, with the fused log10-chi2 histogram and top-k: the
+// tensor-core kernel (method 1) or the plain FP64 chunks (method 0, which reads the FP32
+// curves A and B and the tables pairdiff_prepare left in the small workspace).
+static void pairdiff_core(mlc_ctx* ctx, int method, const float* A, const float* B, const PdOperands& ops,
+                          const double* w_host, const double* d_host, int offset, int nbins, double lo, double hi,
+                          uint64_t* hist_host, int k, double* tv, int64_t* ti, int64_t* tj, float* out,
+                          PdResult& res) {
+  const int NA = ops.NA, NB = ops.NB, T = ops.T;
+  res.delta = ops.delta;
   const int nkb = ops.Kp / 64;
-  const double* cen = (const double*)ctx->ws_ptr[WS_KREAL];
   CUtensorMap tmA = make_map(ops.a, ops.NApad, 3 * ops.Kp, TM);
   CUtensorMap tmB = make_map(ops.b, ops.NBpad, 3 * ops.Kp, TN);
   const long long P = (long long)NA * NB;
@@ -511,7 +509,7 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
     uint32_t* sv = (uint32_t*)(sk + S);
     {
       MLC_KSCOPE(ctx, "pd_sample");
-      k_pd_sample<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(cen, NA, NB, T, S, sk, sv);
+      k_pd_sample<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(ops.cenA, ops.cenB, NA, NB, T, S, sk, sv);
     }
     MLC_CHECK_LAUNCH();
     radix_sort_u64_u32(ctx, S, sk, sv);
@@ -635,7 +633,8 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
     if (hc[1] > 0) {
       MLC_KSCOPE(ctx, "pd_refine");
       k_pd_refine<<<std::max(1u, std::min((hc[1] + 255) / 256, (unsigned)ctx->sm_count * 8)), 256, 0, ctx->stream>>>(
-          cen, NA, T, ri, rj, hc[1], nbins, lo, (hi - lo) / nbins, hist, prm.thr, cap, counters, cval, ci, cj, out, NB);
+          ops.cenA, ops.cenB, T, ri, rj, hc[1], nbins, lo, (hi - lo) / nbins, hist, prm.thr, cap, counters, cval,
+          ci, cj, out, NB);
     }
     MLC_CHECK_LAUNCH();
     MLC_CUDA(cudaMemcpyAsync(hc, counters, 16, cudaMemcpyDeviceToHost, ctx->stream));
@@ -714,6 +713,51 @@ void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int 
       tj[q] = -1;
     }
   }
+}
+
+void pairdiff_run(mlc_ctx* ctx, int method, const float* A, const float* B, int NA, int NB, int T,
+                  const double* w_host, const double* d_host, int offset, int nbins, double lo, double hi,
+                  uint64_t* hist_host, int k, double* tv, int64_t* ti, int64_t* tj, float* out, PdResult& res) {
+  MLC_REQUIRE(method == 1 || T <= 4096, MLC_ERR_LIMIT, "T <= 4096");
+  MLC_REQUIRE(method == 0 || (T >= 1 && T <= MAX_KP), MLC_ERR_LIMIT,
+              "tensor-core pair chi2 supports T <= 128 epochs");
+  MLC_REQUIRE(nbins >= 1 && nbins <= MAX_BINS && hi > lo, MLC_ERR_ARG, "histogram: 1..4096 bins, hi > lo");
+  MLC_REQUIRE(NA >= 1 && NB >= 1 && k >= 0, MLC_ERR_ARG, "bad sizes");
+  PdOperands ops;
+  pairdiff_prepare(ctx, A, B, NA, NB, T, w_host, d_host, offset, ops);
+  pairdiff_core(ctx, method, A, B, ops, w_host, d_host, offset, nbins, lo, hi, hist_host, k, tv, ti, tj, out, res);
+}
+
+// Two prepared sides: the operands point into the sides' own memory (rows padded to
+// PD_SIDE_PAD, beyond both tile heights, and zero there), so nothing is recomputed.
+void pairdiff_sides(mlc_ctx* ctx, const PdSide& A, const PdSide& B, int nbins, double lo, double hi,
+                    uint64_t* hist_host, int k, double* tv, int64_t* ti, int64_t* tj, float* out, PdResult& res) {
+  MLC_REQUIRE(A.T == B.T && A.offset == B.offset && A.w == B.w, MLC_ERR_ARG,
+              "pair sides built with different epochs, weights or offset forms");
+  MLC_REQUIRE(!A.has_d, MLC_ERR_ARG, "side A must be built without the observed difference curve d");
+  MLC_REQUIRE(A.T >= 1 && A.T <= MAX_KP, MLC_ERR_LIMIT, "tensor-core pair chi2 supports T <= 128 epochs");
+  MLC_REQUIRE(nbins >= 1 && nbins <= MAX_BINS && hi > lo, MLC_ERR_ARG, "histogram: 1..4096 bins, hi > lo");
+  MLC_REQUIRE(A.N >= 1 && B.N >= 1 && k >= 0, MLC_ERR_ARG, "bad sizes");
+  PdOperands ops;
+  ops.NA = A.N;
+  ops.NB = B.N;
+  ops.T = A.T;
+  ops.Kp = A.Kp;
+  ops.NApad = (int)round_up(A.N, PD_TILE_M);
+  ops.NBpad = (int)round_up(B.N, PD_TILE_N);
+  ops.delta = std::max(A.delta, B.delta);  // the step pairdiff_prepare reports for both sides together
+  ops.a = A.ops;
+  ops.b = B.ops;
+  ops.alpha = A.norm2;
+  ops.beta = B.norm2;
+  ops.alpha_ff = A.norm2_ff;
+  ops.beta_ff = B.norm2_ff;
+  ops.ea = A.exps;
+  ops.eb = B.exps;
+  ops.cenA = A.cen;
+  ops.cenB = B.cen;
+  pairdiff_core(ctx, 1, nullptr, nullptr, ops, A.w.data(), nullptr, A.offset, nbins, lo, hi, hist_host, k, tv, ti,
+                tj, out, res);
 }
 
 }  // namespace mlc

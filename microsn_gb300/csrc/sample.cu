@@ -33,14 +33,6 @@ void sample_nearest(mlc_ctx* ctx, const double* map, int Nx, int Ny, int k, int 
   MLC_CHECK_LAUNCH();
 }
 
-template <typename T>
-__device__ __forceinline__ T bilin_read(const T* __restrict__ m, const Bilin<T>& B, int Nx) {
-  T z = B.w0 * __ldg(m + (long)B.iu * Nx + B.jl);
-  z += B.w1 * __ldg(m + (long)B.iu * Nx + B.jr);
-  z += B.w2 * __ldg(m + (long)B.il * Nx + B.jl);
-  z += B.w3 * __ldg(m + (long)B.il * Nx + B.jr);
-  return z;
-}
 
 
 template <typename T>

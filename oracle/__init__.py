@@ -481,6 +481,14 @@ def refcuda_available() -> bool:
     return os.path.isdir(os.path.join(REFCUDA_DIR, "microlc", "src"))
 
 
+def refcuda_build_async():
+    """Start compiling the reference's CUDA path (where its sources are staged) in the
+    background and return the process, else None; refcuda() waits for the same make."""
+    if not refcuda_available():
+        return None
+    return subprocess.Popen(["make", "-s", "-f", REFCUDA_MK, "-j8"], stdout=subprocess.DEVNULL)
+
+
 def refcuda():
     """The reference's own CUDA path (expanding_source, setup_integral_GPU, calculate_chi2_GPU,
     bin_chi2_GPU) built unchanged for sm_103a by oracle/refcuda.mk (compiled on first use),

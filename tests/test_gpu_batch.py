@@ -237,3 +237,47 @@ def test_fused_last_pass_interleave_equals_separate_calls(bctx, prec, nprof):
     got = mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=True)
     ref = _separate(bctx, m, profs, trd, True)
     assert torch.equal(got, ref)
+
+
+@pytest.mark.parametrize("prec,fft,nprof", [("f32", "native", 12), ("f32", "f32x2", 12), ("f64", "native", 5)])
+def test_step_as_cuda_graph_equals_eager(bctx, prec, fft, nprof):
+    """graph=True: the first call runs eagerly and captures the whole step (forward spectrum,
+    both convolution chains, the split last pass, sampling); later calls replay it.  Each
+    replay -- after new pixels, new track values and new profile values of the same raster
+    sizes were written into the same buffers -- equals the eager call on the same inputs,
+    and one replay counts the kernels of the captured sequence."""
+    import microsn_gb300 as mlc
+    N = 2000
+    dt = np.float32 if prec == "f32" else np.float64
+    m = mlc.Map(bctx, synth.lognormal_map(N, seed=51).astype(dt), prec)
+    if fft != "native":
+        m.set_fft(fft)
+    profs = _profiles(nprof)
+    pix = torch.as_tensor(synth.lognormal_map(N, seed=52).astype(dt), device=DEV)
+    trd = _device(_host_tracks(800, N, 53, dt))
+    out = torch.empty((nprof, trd["t"].numel()), dtype=pix.dtype, device=DEV)
+    mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=True, pixels=pix, out=out, graph=True)  # eager + capture
+    ref = mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=True, pixels=pix)
+    assert torch.equal(out, ref)
+    l0 = bctx.launch_count()
+    mlc.convolve_sample_tracks(bctx, m, profs, trd, mag=True, pixels=pix, out=out, graph=True)  # replay
+    per_call = bctx.launch_count() - l0
+    assert per_call > nprof
+    assert torch.equal(out, ref)
+    # new contents in the same buffers: pixels, tracks, profile values (same raster sizes)
+    pix.copy_(torch.as_tensor(synth.lognormal_map(N, seed=54).astype(dt), device=DEV))
+    new_tr = _host_tracks(800, N, 55, dt)
+    for k in ("x0", "y0", "phi", "v"):
+        trd[k].copy_(torch.as_tensor(new_tr[k], device=DEV))
+    profs2 = list(profs)
+    profs2[0] = mlc.profile("limb_darkened", 1.5, 1.0, ref_compat=False, u=0.2)  # same raster size as profs[0]
+    assert mlc.profile_raster(profs2[0]).shape == mlc.profile_raster(profs[0]).shape
+    l0 = bctx.launch_count()
+    mlc.convolve_sample_tracks(bctx, m, profs2, trd, mag=True, pixels=pix, out=out, graph=True)
+    assert bctx.launch_count() - l0 == per_call  # replayed, not recaptured
+    ref2 = mlc.convolve_sample_tracks(bctx, m, profs2, trd, mag=True, pixels=pix)
+    assert torch.equal(out, ref2)
+    # the graph form takes device buffers only
+    with pytest.raises(mlc.MlcError):
+        mlc.convolve_sample_tracks(bctx, m, profs, {k: a.cpu().numpy() for k, a in trd.items()}, graph=True)
+    m.close()
