@@ -63,6 +63,13 @@ def parse():
     ap.add_argument("--n", "--side", dest="n", type=int, default=None,
                     help="map side (profiling cases only; not a bench number)")
     ap.add_argument("--tracks", type=int, default=None, help="track count (profiling cases only)")
+    ap.add_argument("--kernel-case", default=None,
+                    choices=["step", "pair_bin_fused", "mpd", "flux_ratio", "track_fit", "sort", "pair_sides"],
+                    help="run one workload alone at the given sizes, for an ncu capture (prints its times; not a "
+                         "bench line)")
+    ap.add_argument("--nprof", type=int, default=None, help="profiles of the step (profiling cases only)")
+    ap.add_argument("--fft", choices=["native", "f32x2"], default=None,
+                    help="transform arithmetic of the step's FP32 map (profiling cases only)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="FFT form for every profile (for ncu captures, under which the autotuner's first-call "
                          "timings are distorted)")
@@ -476,36 +483,40 @@ def c5_workload(args, ctx, dev, rank):
         tracks.append([torch.as_tensor(a, dtype=torch.float32, device=dev) for a in (x0, y0, phi, v)])
     T = C5_EPOCHS * nb
     w = 1.0 / rng.uniform(0.02, 0.1, T) ** 2
-    lcs = [torch.empty((ntr, T), dtype=torch.float32, device=dev) for _ in maps]
     pairs = list(itertools.combinations(range(len(maps)), 2))
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
 
-    def curves():
+    def step():
+        """Per image: its convolutions (one CUDA graph), then its pair side straight from the
+        convolved maps (sample -> magnitude -> centre -> sliced integers, no light curve);
+        then the tensor-core chi2 of every track pair of every image pair."""
+        sides, t_conv, t_side = [], 0.0, 0.0
         for i, m in enumerate(maps):
             m.refresh()
+            e[0].record()
             mlc.convolve_many(ctx, m, profs, out=conv, graph=True)
-            mlc.sample_expanding(ctx, conv, nb, *tracks[i], t, out=lcs[i])
-
-    def pair_stage():
-        res = []
-        for a, b in pairs:
-            res.append(mlc.pair_chi2_magdiff(ctx, lcs[a], lcs[b], w, None, True, method="tensor", nbins=PAIR_BINS,
-                                             lo=-1.0, hi=9.0, k=PAIR_K))
-        return res
-
-    curves(); pair_stage()  # warm-up: captures the convolution graphs, sizes the workspaces
-    torch.cuda.synchronize()
-    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    steps = max(1, min(args.steps, 2))
-    t_curves = t_pairs = 0.0
-    for _ in range(steps):
+            e[1].record()
+            sides.append(mlc.PairSide.expanding(ctx, conv, C5_EPOCHS, nb, *tracks[i], t, w, None, True))
+            e[2].record()
+            torch.cuda.synchronize()
+            t_conv += e[0].elapsed_time(e[1]); t_side += e[1].elapsed_time(e[2])
         e[0].record()
-        curves()
+        res = [mlc.pair_chi2_sides(ctx, sides[a], sides[b], nbins=PAIR_BINS, lo=-1.0, hi=9.0, k=PAIR_K)
+               for a, b in pairs]
         e[1].record()
-        res = pair_stage()
-        e[2].record()
         torch.cuda.synchronize()
-        t_curves += e[0].elapsed_time(e[1]); t_pairs += e[1].elapsed_time(e[2])
-    t_curves /= steps; t_pairs /= steps
+        for sd in sides:
+            sd.close()
+        return res, t_conv, t_side, e[0].elapsed_time(e[1])
+
+    step()  # warm-up: captures the convolution graphs, sizes the workspaces
+    torch.cuda.synchronize()
+    nsteps = max(1, min(args.steps, 2))
+    t_conv = t_sides = t_pairs = 0.0
+    for _ in range(nsteps):
+        res, a, b, c = step()
+        t_conv += a; t_sides += b; t_pairs += c
+    t_conv /= nsteps; t_sides /= nsteps; t_pairs /= nsteps
     # the same convolutions without the graph, for the launch-overhead comparison
     e[0].record()
     for m in maps:
@@ -517,26 +528,56 @@ def c5_workload(args, ctx, dev, rank):
         mlc.convolve_many(ctx, m, profs, out=conv, graph=True)
     e[1].record(); torch.cuda.synchronize()
     conv_graph = e[0].elapsed_time(e[1])
+    # the two-stage form it replaces (light curves of every image stored, then each image
+    # pair prepared from them), timed once with the convolutions of the last image reused
+    lc = torch.empty((ntr, T), dtype=torch.float32, device=dev)
+    lcs = [lc, torch.empty_like(lc)]
+    e[0].record()
+    mlc.sample_expanding(ctx, conv, nb, *tracks[len(maps) - 1], t, out=lcs[0])
+    e[1].record()
+    mlc.sample_expanding(ctx, conv, nb, *tracks[0], t, out=lcs[1])
+    mlc.pair_chi2_magdiff(ctx, lcs[0], lcs[1], w, None, True, method="tensor", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
+                          k=PAIR_K)
+    e[2].record(); torch.cuda.synchronize()
+    two_stage_curves_ms = e[0].elapsed_time(e[1])
+    two_stage_pair_ms = e[1].elapsed_time(e[2]) - two_stage_curves_ms
+    del lcs, lc
     npairs = len(pairs) * float(ntr) * ntr
-    total = t_curves + t_pairs
-    # the pair stage against FP64 on a fixed subset (images 0 and 1, 1000 x 1000 curves):
-    # the tensor-core chi2 matrix against the FP64 plain kernel on the same curves
+    total = t_conv + t_sides + t_pairs
+    # parity on a fixed subset (1000 tracks of the last image x 1000 of image 0, on the last
+    # image's convolved maps): the fused sides equal the two-stage tensor form bit for bit,
+    # and the tensor-core chi2 stays within 1e-5 of the FP64 plain kernel on the same curves
     sa = torch.randperm(ntr, generator=torch.Generator().manual_seed(4))[:1000].to(dev)
     sb = torch.randperm(ntr, generator=torch.Generator().manual_seed(5))[:1000].to(dev)
-    As, Bs = lcs[0][sa].contiguous(), lcs[1][sb].contiguous()
-    mt = mlc.pair_chi2_magdiff(ctx, As, Bs, w, None, True, method="tensor", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
-                               want_matrix=True)["matrix"].double()
-    mp_ = mlc.pair_chi2_magdiff(ctx, As, Bs, w, None, True, method="plain", nbins=PAIR_BINS, lo=-1.0, hi=9.0,
-                                want_matrix=True)["matrix"].double()
-    pair_rel = ((mt - mp_).abs() / mp_.abs().clamp_min(1e-30)).max().item()
-    del mt, mp_, As, Bs
+    ta = [a[sa].contiguous() for a in tracks[len(maps) - 1]]
+    tb = [a[sb].contiguous() for a in tracks[0]]
+    As = mlc.sample_expanding(ctx, conv, nb, *ta, t)
+    Bs = mlc.sample_expanding(ctx, conv, nb, *tb, t)
+    kw = dict(nbins=PAIR_BINS, lo=-1.0, hi=9.0, k=PAIR_K, want_matrix=True)
+    sA = mlc.PairSide.expanding(ctx, conv, C5_EPOCHS, nb, *ta, t, w, None, True)
+    sB = mlc.PairSide.expanding(ctx, conv, C5_EPOCHS, nb, *tb, t, w, None, True)
+    fused = mlc.pair_chi2_sides(ctx, sA, sB, **kw)
+    sA.close(); sB.close()
+    two = mlc.pair_chi2_magdiff(ctx, As, Bs, w, None, True, method="tensor", **kw)
+    plain = mlc.pair_chi2_magdiff(ctx, As, Bs, w, None, True, method="plain", **kw)["matrix"].double()
+    mt = fused["matrix"].double()
+    pair_rel = ((mt - plain).abs() / plain.abs().clamp_min(1e-30)).max().item()
+    fused_equal = bool(torch.equal(fused["matrix"], two["matrix"]) and np.array_equal(fused["hist"], two["hist"])
+                       and np.array_equal(fused["topk_val"], two["topk_val"]))
+    del mt, plain, As, Bs, fused, two
     out = {"workload": f"supernova: {len(maps)} x {N}^2 FP32 maps, {len(profs)} limb-darkened expanding-photosphere "
                        f"profiles per map ({C5_EPOCHS} epochs x {nb} bands), {ntr} tracks per image, offset "
                        f"magnitude-difference chi2 of all track pairs of {len(pairs)} image pairs (T = {T})",
-           "ms_per_step": total, "curves_ms": t_curves, "pairs_ms": t_pairs,
+           "form": "per image: convolutions as one CUDA graph, then a pair side sampled straight from the convolved "
+                   "maps (no light curves in HBM); per image pair: the tensor-core chi2 of the two sides",
+           "ms_per_step": total, "conv_ms": t_conv, "sides_ms": t_sides, "pairs_ms": t_pairs,
+           "two_stage": {"what": "the form this replaces, for one image pair: light curves written to HBM, then "
+                                 "both sides prepared from them inside the pair call",
+                         "curves_ms_per_image": two_stage_curves_ms, "pair_ms_per_image_pair": two_stage_pair_ms,
+                         "sides_ms_per_image": t_sides / len(maps), "pairs_ms_per_image_pair": t_pairs / len(pairs)},
            "light_curves_per_s": len(maps) * ntr * nb / (total / 1000.0),
            "pair_chi2_per_s": npairs / (t_pairs / 1000.0),
-           "convolutions_per_s": len(maps) * len(profs) / (t_curves / 1000.0),
+           "convolutions_per_s": len(maps) * len(profs) / (t_conv / 1000.0),
            "conv_ms_graph": conv_graph, "conv_ms_eager": conv_eager,
            "refined_pairs": int(sum(r["stats"]["refined"] for r in res)),
            "histogram_total": float(sum(float(r["hist"].sum()) for r in res)),
@@ -545,8 +586,10 @@ def c5_workload(args, ctx, dev, rank):
            "pairs_total": npairs,
            "max_rel_err_vs_fp64": pair_rel,
            "parity_subset": {"pairs": 1000 * 1000, "max_rel_err_vs_fp64": pair_rel, "tolerance": 1e-5,
-                             "what": "tensor-core pair chi2 vs the FP64 plain kernel on the same FP32 light curves "
-                                     "(images 0 and 1, 1000 x 1000 fixed curves)"}}
+                             "fused_equals_two_stage": fused_equal,
+                             "what": "fused sides vs the two-stage tensor form (bit for bit) and the tensor-core "
+                                     "pair chi2 vs the FP64 plain kernel on the same FP32 light curves (1000 x 1000 "
+                                     "fixed tracks of two images on one image's convolved maps)"}}
     for m in maps:
         m.close()
     del conv
@@ -1062,10 +1105,104 @@ def run_reference(args):
 
 # ----------------------------------------------------------------------------- main arm
 
+def kernel_case(args):
+    """One workload alone, on small sizes, for ncu captures of its kernels (-k, -c): the
+    step (--side, --tracks, --nprof, --fft), the ratio pair path, the MPD histogram, the
+    flux-ratio likelihood, the track fit, the radix sort of 2^24 keys, or the pair sides of
+    two images of an expanding source.  Prints one JSON line of times (not a bench line)."""
+    import numpy as np
+    import torch
+
+    import microsn_gb300 as mlc
+    from microsn_gb300 import build as B
+    from microsn_gb300 import synth
+    B.build()
+    dev = "cuda:0"
+    ctx = mlc.Context(0)
+    if args.no_autotune:
+        ctx.set_autotune(False)
+    args.no_cpu = True
+    case = args.kernel_case
+    res = {"kernel_case": case}
+    n = args.n or 2000
+    if case in ("step", "pair_bin_fused", "mpd"):
+        mp_t, _ = synth.rayshoot_gpu(ctx, n, WIDTH, KAPPA, GAMMA, seed=MAP_SEED, rays_per_pixel=RAYS_PER_PIXEL,
+                                     dtype=torch.float32)
+        m = mlc.Map(ctx, mp_t, "f32")
+        m.set_fft(args.fft or HEADLINE_FFT)
+    if case == "step":
+        ntr = args.tracks or 100_000
+        _, tr, E = make_tracks_torch(ntr, n, TRACK_SEED, dev, torch.float32)
+        profs = profiles_for(n)[: args.nprof or 16]
+        out = torch.empty((len(profs), E), dtype=torch.float32, device=dev)
+        dpix = m.tensor()
+        for _ in range(max(args.warmup, 1)):
+            mlc.convolve_sample_tracks(ctx, m, profs, tr, mag=True, pixels=dpix, out=out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            mlc.convolve_sample_tracks(ctx, m, profs, tr, mag=True, pixels=dpix, out=out)
+        e1.record(); torch.cuda.synchronize()
+        res.update(side=n, tracks=ntr, epochs=E, nprof=len(profs), fft=args.fft or HEADLINE_FFT,
+                   ms_per_step=e0.elapsed_time(e1) / args.steps)
+    elif case == "pair_bin_fused":
+        args.small = args.small or n < 4000
+        res.update(ratio_pair_workload(args, ctx, m, dev, 0))
+    elif case == "mpd":
+        res.update(mpd_workload(args, ctx, m, 0))
+    elif case == "flux_ratio":
+        res.update(flux_ratio_workload(args, ctx, dev, 0))
+    elif case == "track_fit":
+        res.update(c4_workload(args, ctx, dev, 0))
+    elif case == "sort":
+        nk = 1 << 24
+        g = torch.Generator(device="cpu").manual_seed(7)
+        keys0 = torch.rand(nk, generator=g, dtype=torch.float64).to(dev)
+        vals0 = torch.arange(nk, dtype=torch.int32, device=dev)
+        keys, vals = keys0.clone(), vals0.clone()
+        mlc.sort_f64_u32(ctx, keys, vals)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms = 0.0
+        for _ in range(args.steps):
+            keys.copy_(keys0); vals.copy_(vals0)
+            e0.record()
+            mlc.sort_f64_u32(ctx, keys, vals)
+            e1.record(); torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+        res.update(keys=nk, ms_per_sort=ms / args.steps, sorted=bool(torch.all(keys[1:] >= keys[:-1]).item()))
+    elif case == "pair_sides":
+        N, nep, nb = n, 40, 3
+        mp_t, _ = synth.rayshoot_gpu(ctx, N, 20.0, 0.45, 0.4, seed=6, rays_per_pixel=4.0, dtype=torch.float32)
+        m = mlc.Map(ctx, mp_t, "f32")
+        R = np.linspace(1.0, 100.0 * N / C5_N, nep)
+        profs = [mlc.profile("limb_darkened", r / np.sqrt(2.0), 1.0, ref_compat=False, u=u) for r in R for u in C5_U]
+        conv = mlc.convolve_many(ctx, m, profs)
+        ntr = args.tracks or 20_000
+        rng = np.random.default_rng(60)
+        t = torch.as_tensor(np.arange(nep) * 2.0, dtype=torch.float32, device=dev)
+        mg = 0.3 * N
+        trk = [[torch.as_tensor(a, dtype=torch.float32, device=dev) for a in
+                (rng.uniform(mg, N - mg, ntr), rng.uniform(mg, N - mg, ntr), rng.uniform(0, 2 * np.pi, ntr),
+                 rng.uniform(0.2, 1.0, ntr))] for _ in range(2)]
+        w = 1.0 / rng.uniform(0.02, 0.1, nep * nb) ** 2
+        for _ in range(max(args.warmup, 1)):
+            sA = mlc.PairSide.expanding(ctx, conv, nep, nb, *trk[0], t, w, None, True)
+            sB = mlc.PairSide.expanding(ctx, conv, nep, nb, *trk[1], t, w, None, True)
+            r = mlc.pair_chi2_sides(ctx, sA, sB, nbins=PAIR_BINS, lo=-1.0, hi=9.0, k=PAIR_K)
+            sA.close(); sB.close()
+        torch.cuda.synchronize()
+        res.update(side=N, tracks=ntr, T=nep * nb, refined=r["stats"]["refined"])
+    print(json.dumps(res, default=float), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernel_case:
+        return kernel_case(args)
     import numpy as np
     import torch
 
@@ -1162,6 +1299,20 @@ def main():
     kernels = {k: {"ms_per_step": v, "launches_per_step": kt[k][1] / ksteps,
                    "GB_per_s": (algorithmic_bytes(k, n, E, len(profs), es=spec_es) / (kt[k][0] / kt[k][1] / 1000.0) / 1e9)
                    if algorithmic_bytes(k, n, E, len(profs), es=spec_es) else None} for k, v in per_step.items()}
+
+    # ---- the same step as one CUDA graph (captured on its first graph call, then replayed)
+    def graph_step():
+        mlc.convolve_sample_tracks(ctx, m, profs, tr, mag=True, pixels=dpix, out=out, graph=True)
+
+    graph_step(); graph_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        graph_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    cuda_graph = {"ms_per_step": e0.elapsed_time(e1) / args.steps, "eager_ms_per_step": ms_step,
+                  "what": "the timed step replayed as one CUDA graph (graph=True): same kernels, one launch"}
 
     # ---- e2e through the library with host buffers
     h_map = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
@@ -1363,7 +1514,7 @@ def main():
                         "track positions" if HEADLINE_FFT == "f32x2" else "FP32 transforms"),
                "max_rel_err_vs_fp64": accuracy["max_rel_chi2"] if accuracy else None,
                "accuracy_vs_fp64": accuracy,
-               "plain_fp64": plain, "kernels": kernels,
+               "plain_fp64": plain, "kernels": kernels, "cuda_graph": cuda_graph,
                "sampling_stage": ({"value": world * lc_per_step / (kernels["sample_tracks_il"]["ms_per_step"] / 1000.0),
                                    "unit": UNIT, "ms_per_step": kernels["sample_tracks_il"]["ms_per_step"]}
                                   if "sample_tracks_il" in kernels else None),
