@@ -64,7 +64,8 @@ def parse():
                     help="map side (profiling cases only; not a bench number)")
     ap.add_argument("--tracks", type=int, default=None, help="track count (profiling cases only)")
     ap.add_argument("--kernel-case", default=None,
-                    choices=["step", "pair_bin_fused", "mpd", "flux_ratio", "track_fit", "sort", "pair_sides"],
+                    choices=["step", "pair_bin_fused", "mpd", "flux_ratio", "track_fit", "sort", "pair_sides", "c1",
+                             "c5"],
                     help="run one workload alone at the given sizes, for an ncu capture (prints its times; not a "
                          "bench line)")
     ap.add_argument("--nprof", type=int, default=None, help="profiles of the step (profiling cases only)")
@@ -277,17 +278,19 @@ def c1_workload(args, ctx, dev, rank):
             m.set_fft("native")
 
     out = {}
-    chi_ref = None
     chis = {}
+    chi_u = torch.empty_like(chi2)
     for name, fn in (("fused", lambda: step("fused")), ("fused_f32x2", ff_step), ("plain", plain_step)):
         for _ in range(max(args.warmup, 1)):
             h = fn()
-        if name == "fused":
-            chi_ref = chi2.clone()
-            chis[name] = chi_ref[0].cpu().numpy()
-        elif name == "fused_f32x2":
-            out["f32x2_vs_native_max_rel_chi2"] = float(((chi2 - chi_ref).abs() / chi_ref.abs()).max())
-            chis[name] = chi2[0].cpu().numpy()
+        if name != "plain":
+            # per-track chi2 in track order (the step sorts its copy in place) from the
+            # convolution this form just wrote
+            mlc.track_chi2_offset(ctx, conv, 1, *tr, t, obs, w, out=chi_u)
+            chis[name] = chi_u[0].cpu().numpy().copy()
+        if name == "fused_f32x2":
+            out["f32x2_vs_native_max_rel_chi2"] = float(np.max(np.abs(chis[name] - chis["fused"]) /
+                                                               np.abs(chis["fused"])))
         torch.cuda.synchronize()
         steps = max(1, min(args.steps, 10))
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
@@ -1109,7 +1112,8 @@ def kernel_case(args):
     """One workload alone, on small sizes, for ncu captures of its kernels (-k, -c): the
     step (--side, --tracks, --nprof, --fft), the ratio pair path, the MPD histogram, the
     flux-ratio likelihood, the track fit, the radix sort of 2^24 keys, or the pair sides of
-    two images of an expanding source.  Prints one JSON line of times (not a bench line)."""
+    two images of an expanding source; or one of the bench's side workloads alone (c1, c5).
+    Prints one JSON line of times (not a bench line)."""
     import numpy as np
     import torch
 
@@ -1155,6 +1159,11 @@ def kernel_case(args):
         res.update(flux_ratio_workload(args, ctx, dev, 0))
     elif case == "track_fit":
         res.update(c4_workload(args, ctx, dev, 0))
+    elif case == "c1":
+        args.no_cpu = False
+        res.update(c1_workload(args, ctx, dev, 0))
+    elif case == "c5":
+        res.update(c5_workload(args, ctx, dev, 0))
     elif case == "sort":
         nk = 1 << 24
         g = torch.Generator(device="cpu").manual_seed(7)

@@ -14,12 +14,21 @@
 
 namespace mlc {
 
-uint64_t f64_to_key(double d);
 void radix_sort_u64_u32(mlc_ctx* ctx, long n, uint64_t* keys, uint32_t* vals);
 
+// The key of the reference's z sort (thrust::stable_sort_by_key on doubles, a radix sort):
+// the order of the bit patterns with the sign folded in, -0.0 taken as +0.0 (the radix sort
+// keeps the two in pair-index order), and NaN placed by its sign bit -- the GPU's 0/0
+// (0xfff8...) and a negative NaN operand before -inf, a positive NaN operand after +inf.
 __device__ __forceinline__ uint64_t key_of(double d) {
   uint64_t u = __double_as_longlong(d);
+  if (u == 0x8000000000000000ull) u = 0;
   return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+
+// The double a key stands for (-0.0 comes back as +0.0, equal under comparison).
+__device__ __forceinline__ double value_of(uint64_t k) {
+  return __longlong_as_double((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k);
 }
 
 // z keys and pair indices for the stable rank sort.
@@ -29,7 +38,7 @@ __global__ void k_pair_z(const double* __restrict__ LCA, const double* __restric
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
     const int a = (int)(p / Nloc), b = (int)(p % Nloc);
     const double z = __ldg(LCA + (long)a * Nprof) / __ldg(LCB + (long)b * Nprof);
-    keys[p] = z == z ? key_of(z) : ~0ull;  // NaN (0/0, whatever its sign bit) after every edge
+    keys[p] = key_of(z);
     idx[p] = (uint32_t)p;
   }
 }
@@ -40,16 +49,20 @@ __global__ void k_invert_perm(const uint32_t* __restrict__ perm, long P, uint32_
     rank[perm[r]] = (uint32_t)r;
 }
 
-// upper_bound of each edge key in the sorted keys
-__global__ void k_upper_bound(const uint64_t* __restrict__ sorted, long P, const uint64_t* __restrict__ ekeys,
+// upper_bound of each edge in the sorted z: the reference's binary search
+// (thrust::upper_bound, gpu_functions.cu:388) step for step -- the same midpoints and the
+// same FP64 comparison edge < z, so that NaN z (never greater than an edge) land where they
+// land there: those before -inf count in the first bin, those after +inf in the bins the
+// search's path gives them.
+__global__ void k_upper_bound(const uint64_t* __restrict__ sorted, long P, const double* __restrict__ edges,
                               int nb, uint32_t* __restrict__ upper) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nb) return;
-  const uint64_t e = ekeys[i];
+  const double e = edges[i];
   long lo = 0, hi = P;
   while (lo < hi) {
     const long mid = (lo + hi) >> 1;
-    if (e < sorted[mid]) hi = mid;
+    if (e < value_of(sorted[mid])) hi = mid;
     else lo = mid + 1;
   }
   upper[i] = (uint32_t)lo;
@@ -189,8 +202,14 @@ __global__ void __launch_bounds__(256) k_pair_bin_fused(const double* __restrict
         exact = (lo < nb && ef_s[lo] - z32 <= tol) || (lo > 0 && z32 - ef_s[lo - 1] <= tol);
       }
       if (exact) {
-        const double z = __ldg(LCA + (long)a * Nprof) / __ldg(LCB + (long)b * Nprof);
-        if (z != z) continue;  // 0/0: the rank order puts NaN above every edge
+        double z = __ldg(LCA + (long)a * Nprof) / __ldg(LCB + (long)b * Nprof);
+        // NaN: the rank order puts a negative one (the GPU's 0/0) before every z, in the
+        // first bin, and a positive one (from a NaN light-curve value) after +inf, counted
+        // here in no bin
+        if (z != z) {
+          if (!signbit(z)) continue;
+          z = -INFINITY;
+        }
         lo = 0;
         hi = nb;
         while (lo < hi) {
@@ -247,14 +266,12 @@ void pair_setup(mlc_ctx* ctx, int Nloc, int Nprof, const double* LCA, const doub
     MLC_CHECK_LAUNCH();
   }
   if (Nbins > 0) {
-    std::vector<uint64_t> ek(Nbins);
-    for (int i = 0; i < Nbins; i++) ek[i] = f64_to_key(edges_host[i]);
-    uint64_t* dek = (uint64_t*)ws_get(ctx, WS_SMALL, sizeof(uint64_t) * Nbins + sizeof(uint32_t) * Nbins);
-    uint32_t* dup = reinterpret_cast<uint32_t*>(dek + Nbins);
-    MLC_CUDA(cudaMemcpyAsync(dek, ek.data(), sizeof(uint64_t) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
+    double* dedge = (double*)ws_get(ctx, WS_SMALL, sizeof(double) * Nbins + sizeof(uint32_t) * Nbins);
+    uint32_t* dup = reinterpret_cast<uint32_t*>(dedge + Nbins);
+    MLC_CUDA(cudaMemcpyAsync(dedge, edges_host, sizeof(double) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
     {
       MLC_KSCOPE(ctx, "pair_upper_bound");
-      k_upper_bound<<<ceil_div(Nbins, 256), 256, 0, ctx->stream>>>(keys, P, dek, Nbins, dup);
+      k_upper_bound<<<ceil_div(Nbins, 256), 256, 0, ctx->stream>>>(keys, P, dedge, Nbins, dup);
     }
     MLC_CHECK_LAUNCH();
     std::vector<uint32_t> up(Nbins);

@@ -289,10 +289,35 @@ int orc_setup_chi2(double MA, double MB, double V0, double Dfac, int Nd, const d
 
 /* ---- pair z, rank table, z bins (gpu_functions.cu:351-401, kernel_z :643-658) ---- */
 
+/* The reference sorts z with thrust::stable_sort_by_key on doubles, a radix sort over the
+ * bit patterns: negative values (sign bit set) by their inverted bits, the rest above them;
+ * -0.0 ranks as +0.0; NaN ranks by its sign bit (a negative NaN before -inf, a positive
+ * one after +inf).  Ties keep the pair order. */
+static uint64_t radix_key(double d) {
+  uint64_t u;
+  memcpy(&u, &d, 8);
+  if (u == 0x8000000000000000ull) u = 0;
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+
+/* z = a / b as kernel_z computes it on the GPU: a NaN operand passes through (sign
+ * included); 0/0 and inf/inf give the GPU's default NaN, whose sign bit is set (the host's
+ * default NaN differs between machines). */
+static double gpu_div(double a, double b) {
+  if (a != a) return a;
+  if (b != b) return b;
+  double z = a / b;
+  if (z != z) {
+    const uint64_t u = 0xfff8000000000000ull;
+    memcpy(&z, &u, 8);
+  }
+  return z;
+}
+
 static const double* g_sort_keys;
 static int cmp_key_then_index(const void* pa, const void* pb) {
   uint32_t a = *(const uint32_t*)pa, b = *(const uint32_t*)pb;
-  double ka = g_sort_keys[a], kb = g_sort_keys[b];
+  uint64_t ka = radix_key(g_sort_keys[a]), kb = radix_key(g_sort_keys[b]);
   if (ka < kb) return -1;
   if (kb < ka) return 1;
   return (a < b) ? -1 : (a > b); /* stable: original pair index breaks ties */
@@ -307,7 +332,7 @@ void orc_pair_rank(int Nloc, int Nprof, const double* LCA, const double* LCB, in
   double* z = (double*)malloc(sizeof(double) * P);
   uint32_t* perm = (uint32_t*)malloc(sizeof(uint32_t) * P);
   for (int a = 0; a < Nloc; a++)
-    for (int b = 0; b < Nloc; b++) z[(long)a * Nloc + b] = LCA[(long)a * Nprof] / LCB[(long)b * Nprof];
+    for (int b = 0; b < Nloc; b++) z[(long)a * Nloc + b] = gpu_div(LCA[(long)a * Nprof], LCB[(long)b * Nprof]);
   for (long p = 0; p < P; p++) perm[p] = (uint32_t)p;
   g_sort_keys = z;
   qsort(perm, P, sizeof(uint32_t), cmp_key_then_index);

@@ -72,3 +72,46 @@ def test_pair_path_matches_reference_cuda(ctx, golden, Nloc):
     fb, fe, fn = mlc.pair_bin_fused(ctx, v, T(LCA), T(DLCA), T(LCB), T(DLCB), edges)
     assert np.array_equal(fn, ref["nper"])
     np.testing.assert_allclose(fb[full], ref["bchi2"][full], rtol=1e-10)
+
+
+@pytest.mark.parametrize("nan_inputs", [False, True])
+def test_pair_path_zero_and_nan_quotients_match_reference_cuda(ctx, golden, nan_inputs):
+    """z = 0/x (both signs of zero), x/0 and 0/0: the reference's radix sort ranks -0.0 with
+    +0.0 in pair order and the GPU's 0/0 NaN (sign bit set) before every other z, so those
+    pairs fall in the first bin; with NaN light-curve values of either sign as well, a
+    negative NaN joins them and a positive one goes after +inf.  Ranks, bins and bin means
+    equal the reference's own CUDA path, and the oracle's ranks and bins equal both."""
+    import microsn_gb300 as mlc
+    rng = np.random.default_rng(23)
+    Nloc, Nprof = 700, 5
+    LCA = np.exp(rng.normal(0, 0.6, (Nloc, Nprof)))
+    LCB = np.exp(rng.normal(0, 0.6, (Nloc, Nprof)))
+    LCA[0:60:2, 0] = -0.0
+    LCA[1:60:2, 0] = 0.0
+    LCB[100:130, 0] = 0.0
+    if nan_inputs:
+        LCA[200:203, 0] = np.nan
+        LCA[300:303, 0] = np.copysign(np.nan, -1.0)
+    DLCA, DLCB = np.diff(LCA, axis=1), np.diff(LCB, axis=1)
+    edges = mlc.bin_edges(300, 1e-4, 300, True)
+    v = mlc.setup_chi2_calculation((0.4, 0.5), (1.0,), float(golden["setup_Dfac"]), golden["setup_d"],
+                                   golden["setup0_t"], golden["setup_s"], golden["setup_sizes"])
+    ref = oracle.refcuda_pair_path(LCA, DLCA, LCB, DLCB,
+                                   dict(Njp=v.Njp, indA=v.indA, indB=v.indB, facA=v.facA, facB=v.facB, d=v.d, s=v.s),
+                                   edges)
+    T = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=DEV)
+    rank_t, lower, nper = mlc.setup_integral(ctx, T(LCA), T(LCB), edges)
+    rank = rank_t.cpu().numpy().view(np.uint32)
+    assert np.array_equal(rank, ref["rank"])
+    assert np.array_equal(lower, ref["lower"]) and np.array_equal(nper, ref["nper"])
+    r_o, l_o, n_o = oracle.pair_rank(LCA, LCB, edges)
+    assert np.array_equal(r_o, ref["rank"]) and np.array_equal(l_o, ref["lower"]) and np.array_equal(n_o, ref["nper"])
+    nan_first = 60 * 30 + (3 * Nloc if nan_inputs else 0)  # 0/0 pairs, and every pair of a negative-NaN row
+    assert nper[0] >= nan_first
+    chi2 = mlc.calculate_chi2(ctx, v, T(LCA), T(DLCA), T(LCB), T(DLCB), rank_t)
+    bc, be = mlc.bin_chi2(ctx, lower, nper, chi2)
+    np.testing.assert_allclose(bc, ref["bchi2"], rtol=1e-12)  # NaN where the reference has NaN
+    np.testing.assert_allclose(be, ref["bexp"], rtol=1e-12, atol=1e-300)
+    if not nan_inputs:  # the rank-free kernel: the same counts (positive NaN z have no bin there)
+        _, _, fn = mlc.pair_bin_fused(ctx, v, T(LCA), T(DLCA), T(LCB), T(DLCB), edges)
+        assert np.array_equal(fn, ref["nper"])
