@@ -14,14 +14,15 @@
 // rounding could matter) and, with a matrix requested, every pair whose quantisation error
 // could exceed 1e-6 relative are recomputed in FP64 by k_pd_refine.
 //
-// Kernel layout (one persistent CTA per SM, 16 warps):
+// Kernel layout (one persistent CTA per SM, 4 + 12..24 warps):
 //   warp 0      TMA producer: the work item's 128 A rows (3 slices x Kp, resident in shared
 //               memory) and, double-buffered, each 48-row B tile
 //   warp 1      MMA issuer (one thread): 9 slice pairs x Kp/16 tcgen05.mma per tile into one
 //               of two TMEM buffers (5 accumulators x 48 columns each; buffers at columns
 //               0 and 256 of the 512 allocated)
 //   warp 2      TMEM allocation / release
-//   warps 4-15  epilogue (three warps per TMEM lane quadrant, 16 columns each): TMEM ->
+//   warps 4..    epilogue (12, 16 or 24 warps, the same number per TMEM lane quadrant; the
+//               autotuner picks the count): TMEM ->
 //               registers, chi2 assembly, log10-chi2 histogram in shared memory, top-k
 //               candidates below a threshold, refinement list, optional matrix
 // Every barrier wait is bounded; a timeout sets the error flag and all roles unwind.
@@ -45,8 +46,20 @@ namespace {
 
 constexpr int TM = PD_TILE_M, TN = PD_TILE_N;
 constexpr int NSTAGE = 2;
-constexpr int EPI_WARPS = 12;  // three per SM sub-partition, 16 columns each
-constexpr int NTHREADS = (4 + EPI_WARPS) * 32;
+// Epilogue shapes: EPIW warps (a multiple of 4: the same number per TMEM lane quadrant, one
+// per SM sub-partition each), each taking WCOLS of the 48 tile columns, CCH per TMEM load.
+// 12 warps: 16 columns (loads of 8); 16: 12 (loads of 4); 24: 8 (one load of 8).
+template <int EPIW>
+struct Epi {
+  static constexpr int warps = EPIW;
+  static constexpr int per_q = EPIW / 4;
+  static constexpr int wcols = TN / per_q;
+  static constexpr int cch = wcols % 8 == 0 ? 8 : 4;
+  static constexpr int threads = (4 + EPIW) * 32;
+  static_assert(EPIW % 4 == 0 && wcols * per_q == TN && wcols % cch == 0 && wcols <= 16, "epilogue column split");
+};
+constexpr int MAX_EPIW = 24;
+constexpr int EPI_CHOICES[] = {12, 16, 24};
 constexpr int TMEM_COLS = 512;
 constexpr int MAX_KP = 128;
 constexpr int MAX_BINS = 4096;
@@ -82,7 +95,7 @@ struct PdParams {
 
 size_t smem_bytes(int nkb, int nbins) {
   return 1024 + (size_t)3 * nkb * A_BOX + (size_t)NSTAGE * 3 * nkb * B_BOX + 16 * 8 + 16 +
-         sizeof(uint32_t) * ((nbins + 2 + 3) & ~3) + (size_t)EPI_WARPS * 16 * sizeof(float4);
+         sizeof(uint32_t) * ((nbins + 2 + 3) & ~3) + (size_t)MAX_EPIW * 16 * sizeof(float4);
 }
 
 // 2^k for k in [-126, 127]; 0 below (the terms it scales are then negligible)
@@ -107,11 +120,17 @@ __device__ __forceinline__ float chi2_assemble(float2 A, float2 B, float u0, flo
   return t2 + (((e1 + e2) + e3) + ((A.y + B.y) - ((u2 + u3) + u4)));
 }
 
-__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" ::"r"(EPI_WARPS * 32) : "memory"); }
+template <int EPIW>
+__device__ __forceinline__ void epi_sync() {
+  asm volatile("bar.sync 1, %0;" ::"r"(EPIW * 32) : "memory");
+}
 
-template <int NKB, bool OUT>  // 64-element K boxes per slice (Kp / 64); chi2 matrix written
-__global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_constant__ CUtensorMap tmA,
-                                                             const __grid_constant__ CUtensorMap tmB, PdParams P) {
+// NKB: 64-element K boxes per slice (Kp / 64); OUT: chi2 matrix written; EPIW: epilogue warps
+template <int NKB, bool OUT, int EPIW>
+__global__ void __launch_bounds__(Epi<EPIW>::threads, 1) k_pairdiff_tc(const __grid_constant__ CUtensorMap tmA,
+                                                                        const __grid_constant__ CUtensorMap tmB,
+                                                                        PdParams P) {
+  constexpr int EPI_WARPS = EPIW, WCOLS = Epi<EPIW>::wcols, CCH = Epi<EPIW>::cch, NTHREADS = Epi<EPIW>::threads;
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int nkb = NKB;
@@ -128,7 +147,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
   volatile int* abort_s = (volatile int*)(tmem_slot + 1);
   uint32_t* hist_s = tmem_slot + 4;
   // nbins counters, then the two out-of-range counters (below lo, at or above hi)
-  float4* colv = (float4*)(hist_s + ((P.nbins + 2 + 3) & ~3));  // [EPI_WARPS][16] column constants
+  float4* colv = (float4*)(hist_s + ((P.nbins + 2 + 3) & ~3));  // [EPIW][16] column constants
   const uint32_t hist_sa = tc::smem_u32(hist_s);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -219,7 +238,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
     }
   } else if (warp >= 4) {
     // ------------------------------------------------ epilogue
-    const int q = warp & 3, h = (warp - 4) >> 2;  // lane quadrant, column third
+    const int q = warp & 3, h = (warp - 4) >> 2;  // lane quadrant, column group
     const uint32_t lane_addr = (uint32_t)(32 * q) << 16;
     // Every epilogue warp walks the same items and reaches the two named-barrier syncs per
     // item the same number of times; after an abort it only skips the work.
@@ -233,14 +252,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
       const int ei = irow ? P.ea[i] : PD_EMIN;
       const float pa = pow2f(ei);  // 2^ei
       float4* cv = colv + (warp - 4) * 16;
-      // this warp's 16 columns h*16 + c of a tile: (beta_ff, 2^(ej+33)) fetched one tile ahead
+      // this warp's WCOLS columns h*WCOLS + c of a tile: (beta_ff, 2^(ej+33)) fetched one tile ahead
       // (the loads run while the previous tile is processed), staged in shared memory and read
       // back as one broadcast load per element
       float2 nb = make_float2(0.f, 0.f);
       int ne = PD_EMIN;
       auto fetch = [&](int jt) {
-        const int jl = jt * TN + h * 16 + lane;
-        const bool lok = lane < 16 && jt < j1 && jl < P.NB;
+        const int jl = jt * TN + h * WCOLS + lane;
+        const bool lok = lane < WCOLS && jt < j1 && jl < P.NB;
         nb = lok ? __ldg(P.beta_ff + jl) : make_float2(0.f, 0.f);
         ne = lok ? __ldg(P.eb + jl) : PD_EMIN;
       };
@@ -249,7 +268,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
         const uint32_t tb = ct & 1, tu = ct >> 1;
         if (*abort_s) break;
         // (the previous tile's reads of cv ended at the __syncwarp closing it)
-        if (lane < 16) cv[lane] = make_float4(nb.x, nb.y, pow2f(ne + 33), 0.f);  // 2 x 2^(ei+ej) x 2^32 with pa
+        if (lane < WCOLS) cv[lane] = make_float4(nb.x, nb.y, pow2f(ne + 33), 0.f);  // 2 x 2^(ei+ej) x 2^32 with pa
         fetch(jt + 1);
         __syncwarp();
         if (!tc::mbar_wait(t_full + tb, tu & 1)) {
@@ -259,21 +278,21 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
         tc::fence_after_sync();
         // full tiles (every row and column real) skip the per-element range tests
         const bool fast = irow && (jt + 1) * TN <= P.NB;
-        for (int ch = 0; ch < 2; ch++) {
-          const int col0 = h * 16 + ch * 8;
-          uint32_t r0[8], r1[8], r2[8], r3[8], r4[8];
+        for (int ch = 0; ch < WCOLS / CCH; ch++) {
+          const int col0 = h * WCOLS + ch * CCH;
+          uint32_t r0[CCH], r1[CCH], r2[CCH], r3[CCH], r4[CCH];
           const uint32_t ta = tmem + tb * TBUF + lane_addr + col0;
-          tc::tmem_ld8(ta, r0);
-          tc::tmem_ld8(ta + TN, r1);
-          tc::tmem_ld8(ta + 2 * TN, r2);
-          tc::tmem_ld8(ta + 3 * TN, r3);
-          tc::tmem_ld8(ta + 4 * TN, r4);
+          tc::tmem_ld<CCH>(ta, r0);
+          tc::tmem_ld<CCH>(ta + TN, r1);
+          tc::tmem_ld<CCH>(ta + 2 * TN, r2);
+          tc::tmem_ld<CCH>(ta + 3 * TN, r3);
+          tc::tmem_ld<CCH>(ta + 4 * TN, r4);
           tc::tmem_wait_ld();
 #pragma unroll
-          for (int c = 0; c < 8; c++) {
+          for (int c = 0; c < CCH; c++) {
             const int j = jt * TN + col0 + c;
             if (!fast && (!irow || j >= P.NB)) continue;
-            const float4 b = cv[ch * 8 + c];
+            const float4 b = cv[ch * CCH + c];
             // 2 x 2^(ei+ej) = sum_d 2^(ei+ej+33-8d) X_d; s0 = 2^(ei+ej+33) is an exact product
             const float s0 = pa * b.z;
             const float X0 = __uint_as_float(r0[c]), X1 = __uint_as_float(r1[c]);
@@ -325,7 +344,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
         if (lane == 0) tc::mbar_arrive(t_empty + tb);
       }
       // flush this item's histogram (per item, so the 32-bit shared counters cannot overflow)
-      epi_sync();
+      epi_sync<EPIW>();
       for (int b = (int)threadIdx.x - 128; b < P.nbins + 2; b += EPI_WARPS * 32) {
         const uint32_t v = hist_s[b];
         if (v) {
@@ -333,7 +352,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_pairdiff_tc(const __grid_consta
           hist_s[b] = 0;
         }
       }
-      epi_sync();
+      epi_sync<EPIW>();
     }
   }
   tc::fence_before_sync();
@@ -486,6 +505,87 @@ CUtensorMap make_map(void* base, int rows, int kcols, int box_rows) {
 
 }  // namespace
 
+using PdKernel = decltype(&k_pairdiff_tc<1, false, 16>);
+
+template <int NKB, bool OUT>
+static PdKernel pd_kernel_t(int epiw) {
+  switch (epiw) {
+    case 12: return k_pairdiff_tc<NKB, OUT, 12>;
+    case 24: return k_pairdiff_tc<NKB, OUT, 24>;
+    default: return k_pairdiff_tc<NKB, OUT, 16>;
+  }
+}
+
+static PdKernel pd_kernel(int nkb, bool out, int epiw) {
+  return nkb == 1 ? (out ? pd_kernel_t<1, true>(epiw) : pd_kernel_t<1, false>(epiw))
+                  : (out ? pd_kernel_t<2, true>(epiw) : pd_kernel_t<2, false>(epiw));
+}
+
+// The epilogue warp count for this shape class (K boxes, matrix or not, histogram size,
+// pair count to the nearest power of four): with the autotuner on, the first call of a
+// class times one launch of each count on the real operands (the pass loop that follows
+// clears and recomputes every output) and keeps the fastest; otherwise 16.
+static int pd_epilogue_choice(mlc_ctx* ctx, int nkb, bool out, int nbins, long long P, int grid, size_t smem,
+                              const CUtensorMap& tmA, const CUtensorMap& tmB, const PdParams& prm,
+                              unsigned* counters, unsigned long long* hist) {
+  if (!ctx->autotune) return 16;
+  int lg = 0;
+  while ((1LL << (2 * (lg + 1))) <= P) lg++;
+  char key[96];
+  std::snprintf(key, sizeof key, "pairdiff_tc K%d%s bins%d pairs~4^%d", 64 * nkb, out ? " matrix" : "",
+                nbins <= 1024 ? 1024 : 4096, lg);
+  auto it = ctx->tune.find(key);
+  if (it != ctx->tune.end()) return it->second;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  MLC_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return 16;
+  const bool saved = ctx->timing;
+  ctx->timing = false;  // tuning launches stay out of the per-kernel timings
+  cudaEvent_t a = nullptr, b = nullptr;
+  std::vector<std::pair<int, float>> ms;
+  try {
+    MLC_CUDA(cudaEventCreate(&a));
+    MLC_CUDA(cudaEventCreate(&b));
+    PdParams q = prm;
+    q.thr = -1.f;  // no candidates while timing
+    for (int e : EPI_CHOICES) {
+      const auto kern = pd_kernel(nkb, out, e);
+      set_max_smem((const void*)kern, smem);
+      MLC_CUDA(cudaMemsetAsync(counters, 0, 16, ctx->stream));
+      MLC_CUDA(cudaMemsetAsync(hist, 0, 8 * (size_t)(nbins + 2), ctx->stream));
+      MLC_CUDA(cudaEventRecord(a, ctx->stream));
+      kern<<<grid, (4 + e) * 32, smem, ctx->stream>>>(tmA, tmB, q);
+      MLC_CHECK_LAUNCH();
+      MLC_CUDA(cudaEventRecord(b, ctx->stream));
+      MLC_CUDA(cudaEventSynchronize(b));
+      unsigned hc[4];
+      MLC_CUDA(cudaMemcpy(hc, counters, 16, cudaMemcpyDeviceToHost));
+      MLC_REQUIRE(hc[2] == 0, MLC_ERR_TIMEOUT, "tensor-core pair kernel: a pipeline wait timed out");
+      float t = 0.f;
+      MLC_CUDA(cudaEventElapsedTime(&t, a, b));
+      ms.emplace_back(e, t);
+    }
+  } catch (...) {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    ctx->timing = saved;
+    throw;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  ctx->timing = saved;
+  const auto best = *std::min_element(ms.begin(), ms.end(), [](const auto& x, const auto& y) { return x.second < y.second; });
+  ctx->tune[key] = best.first;
+  std::string rec;
+  for (const auto& m : ms) {
+    char buf[48];
+    std::snprintf(buf, sizeof buf, "%sepi%d=%.4f", rec.empty() ? "" : " ", m.first, m.second);
+    rec += buf;
+  }
+  ctx->tune_log[key] = rec;
+  return best.first;
+}
+
 // Pair chi2 from prepared operands, with the fused log10-chi2 histogram and top-k: the
 // tensor-core kernel (method 1) or the plain FP64 chunks (method 0, which reads the FP32
 // curves A and B and the tables pairdiff_prepare left in the small workspace).
@@ -575,10 +675,13 @@ static void pairdiff_core(mlc_ctx* ctx, int method, const float* A, const float*
   prm.err = (int*)(counters + 2);
   const size_t smem = smem_bytes(nkb, nbins);
   MLC_REQUIRE(nkb == 1 || nkb == 2, MLC_ERR_LIMIT, "tensor-core pair chi2 supports T <= 128 epochs");
-  auto kern = nkb == 1 ? (out ? k_pairdiff_tc<1, true> : k_pairdiff_tc<1, false>)
-                       : (out ? k_pairdiff_tc<2, true> : k_pairdiff_tc<2, false>);
-  set_max_smem((const void*)kern, smem);
   const int grid = std::min(grid_max, prm.nitems);
+  const int epiw = method == 1 ? pd_epilogue_choice(ctx, nkb, out != nullptr, nbins, P, grid, smem, tmA, tmB, prm,
+                                                    counters, hist)
+                               : 16;
+  const auto kern = pd_kernel(nkb, out != nullptr, epiw);
+  const int nthreads = (4 + epiw) * 32;
+  set_max_smem((const void*)kern, smem);
   // plain form: FP64 chi2 of row chunks, then histogram / candidates of each chunk
   double* wd = nullptr;
   const long rows_per_chunk = std::max<long>(1, std::min<long>(NA, (1L << 27) / NB));
@@ -597,7 +700,7 @@ static void pairdiff_core(mlc_ctx* ctx, int method, const float* A, const float*
     MLC_CUDA(cudaMemsetAsync(hist, 0, 8 * (size_t)(nbins + 2), ctx->stream));
     if (method == 1) {
       MLC_KSCOPE(ctx, "pairdiff_tc");
-      kern<<<grid, NTHREADS, smem, ctx->stream>>>(tmA, tmB, prm);
+      kern<<<grid, nthreads, smem, ctx->stream>>>(tmA, tmB, prm);
     } else {
       for (long r0 = 0; r0 < NA; r0 += rows_per_chunk) {
         const long nr = std::min<long>(rows_per_chunk, NA - r0);
