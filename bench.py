@@ -64,8 +64,8 @@ def parse():
                     help="map side (profiling cases only; not a bench number)")
     ap.add_argument("--tracks", type=int, default=None, help="track count (profiling cases only)")
     ap.add_argument("--kernel-case", default=None,
-                    choices=["step", "pair_bin_fused", "mpd", "flux_ratio", "track_fit", "sort", "pair_sides", "c1",
-                             "c5"],
+                    choices=["step", "pair_bin_fused", "mpd", "flux_ratio", "track_fit", "sort", "pair_sides", "pair",
+                             "c1", "c5"],
                     help="run one workload alone at the given sizes, for an ncu capture (prints its times; not a "
                          "bench line)")
     ap.add_argument("--nprof", type=int, default=None, help="profiles of the step (profiling cases only)")
@@ -1129,7 +1129,7 @@ def kernel_case(args):
     case = args.kernel_case
     res = {"kernel_case": case}
     n = args.n or 2000
-    if case in ("step", "pair_bin_fused", "mpd"):
+    if case in ("step", "pair_bin_fused", "mpd", "pair"):
         mp_t, _ = synth.rayshoot_gpu(ctx, n, WIDTH, KAPPA, GAMMA, seed=MAP_SEED, rays_per_pixel=RAYS_PER_PIXEL,
                                      dtype=torch.float32)
         m = mlc.Map(ctx, mp_t, "f32")
@@ -1158,6 +1158,8 @@ def kernel_case(args):
         res.update(flux_ratio_workload(args, ctx, dev, 0))
     elif case == "track_fit":
         res.update(c4_workload(args, ctx, dev, 0))
+    elif case == "pair":  # the pair-chi2/s workload (10^5 x 10^5 curves; --tracks N: N x N)
+        res.update(pair_workload(args, ctx, m, profiles_for(n), n, dev, 1, 0, torch.cuda.current_stream()))
     elif case == "c1":
         args.no_cpu = False
         res.update(c1_workload(args, ctx, dev, 0))
@@ -1202,6 +1204,7 @@ def kernel_case(args):
             sA.close(); sB.close()
         torch.cuda.synchronize()
         res.update(side=N, tracks=ntr, T=nep * nb, refined=r["stats"]["refined"])
+    res["autotune"] = {k: {"choice": c, "ms": t} for k, (c, t) in ctx.autotune_report().items()}
     print(json.dumps(res, default=float), flush=True)
 
 

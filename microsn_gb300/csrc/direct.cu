@@ -219,6 +219,7 @@ int conv_direct_choice(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const 
   const auto best = *std::min_element(ms.begin(), ms.end(),
                                       [](const auto& x, const auto& y) { return x.second < y.second; });
   ctx->tune[key] = best.first;
+  ctx->tune_name[key] = best.first < 0 ? "fft" : kVariants[best.first].name;
   std::string rec;
   for (const auto& m : ms) {
     char b[64];
@@ -241,7 +242,8 @@ void conv_auto(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const void* Fm
 std::string autotune_report(mlc_ctx* ctx) {
   std::string s;
   for (const auto& kv : ctx->tune) {
-    s += kv.first + ": " + (kv.second < 0 ? std::string("fft") : std::string(kVariants[kv.second].name));
+    auto nm = ctx->tune_name.find(kv.first);
+    s += kv.first + ": " + (nm != ctx->tune_name.end() ? nm->second : std::to_string(kv.second));
     auto l = ctx->tune_log.find(kv.first);
     if (l != ctx->tune_log.end()) s += " (" + l->second + ")";
     s += "\n";

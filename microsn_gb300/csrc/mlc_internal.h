@@ -95,6 +95,7 @@ struct mlc_ctx {
   bool autotune = true;
   std::map<std::string, int> tune;
   std::map<std::string, std::string> tune_log;
+  std::map<std::string, std::string> tune_name;  // the choice as the report prints it
 };
 
 struct mlc_map {

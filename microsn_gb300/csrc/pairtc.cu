@@ -576,6 +576,7 @@ static int pd_epilogue_choice(mlc_ctx* ctx, int nkb, bool out, int nbins, long l
   ctx->timing = saved;
   const auto best = *std::min_element(ms.begin(), ms.end(), [](const auto& x, const auto& y) { return x.second < y.second; });
   ctx->tune[key] = best.first;
+  ctx->tune_name[key] = "epi" + std::to_string(best.first);
   std::string rec;
   for (const auto& m : ms) {
     char buf[48];
