@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--nprof", type=int, default=None, help="profiles of the step (profiling cases only)")
     ap.add_argument("--fft", choices=["native", "f32x2"], default=None,
                     help="transform arithmetic of the step's FP32 map (profiling cases only)")
+    ap.add_argument("--tune", action="append", default=[], metavar="KEY=CHOICE",
+                    help="pin an autotuner choice (mlc_ctx_tune_set), e.g. 'conv P1 f32x2->f32 10000x10000=1'")
     ap.add_argument("--no-autotune", action="store_true",
                     help="FFT form for every profile (for ncu captures, under which the autotuner's first-call "
                          "timings are distorted)")
@@ -1125,6 +1127,9 @@ def kernel_case(args):
     ctx = mlc.Context(0)
     if args.no_autotune:
         ctx.set_autotune(False)
+    for kv in args.tune:
+        key, _, val = kv.rpartition("=")
+        ctx.tune_set(key, int(val))
     args.no_cpu = True
     case = args.kernel_case
     res = {"kernel_case": case}

@@ -100,13 +100,25 @@ int mlc_ctx_set_timing(mlc_ctx* ctx, int on);
 /* Launch autotuner (on by default; no reference counterpart).  For each new (map size,
  * profile size) of an FP32 fused convolution the first call times the FFT form against
  * the direct tiled form's tile shapes (mlc_convolve_direct) on the context's stream and
- * keeps the fastest; later calls reuse the choice.  Tuning synchronises the stream once
+ * keeps the fastest; likewise the fused convolution's P1 variant per map size and
+ * arithmetic, and the pair kernel's epilogue width per shape class.  Later calls reuse the
+ * choice.  Tuning synchronises the stream once
  * per key and is skipped while the stream is captured into a CUDA graph.  Off: the FFT
  * form everywhere (results then do not depend on timings).  The report lists every tuned
  * key, its choice and the candidates' times: NUL-terminated text into buf (cap bytes);
  * returns the text length, or a negative status. */
 int mlc_ctx_set_autotune(mlc_ctx* ctx, int on);
 int mlc_ctx_autotune_report(mlc_ctx* ctx, char* buf, int cap);
+
+/* Pins the autotuner's choice for one key (as the report prints it; used whether or not
+ * the autotuner is on), e.g. to compare variants or to fix a run's kernels:
+ *   "conv f32 <Nx>x<Ny> N<pN>[ spectrum]": -1 FFT form, 0..3 direct tile shape;
+ *   "conv P1 <arithmetic> <Nx>x<Ny>": 0 map spectrum prefetched into L2, 1 staged in
+ *     shared memory (float-float and FP64 transforms);
+ *   "pairdiff_tc K<64|128>[ matrix] bins<1024|4096> pairs~4^<k>": epilogue warps 12, 16
+ *     or 24.
+ * Other values fall back to the default. */
+int mlc_ctx_tune_set(mlc_ctx* ctx, const char* key, int choice);
 int mlc_ctx_kernel_times(mlc_ctx* ctx, char* names_host, int name_cap, double* ms_host, long* launches_host,
                          int cap, int reset);
 

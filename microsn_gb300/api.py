@@ -83,6 +83,10 @@ class Context:
         """Launch autotuner on (default) or off (FFT form everywhere)."""
         self.check(self.L.mlc_ctx_set_autotune(self.h, int(on)))
 
+    def tune_set(self, key: str, choice: int):
+        """Pin the autotuner's choice for one key (see mlc_ctx_tune_set)."""
+        self.check(self.L.mlc_ctx_tune_set(self.h, key.encode(), int(choice)))
+
     def autotune_report(self) -> dict:
         """{key: (choice, {candidate: ms})} of every tuned key."""
         buf = C.create_string_buffer(1 << 16)

@@ -143,6 +143,15 @@ int mlc_ctx_set_autotune(mlc_ctx* ctx, int on) {
   return guarded(ctx, [&] { ctx->autotune = on != 0; });
 }
 
+int mlc_ctx_tune_set(mlc_ctx* ctx, const char* key, int choice) {
+  if (!ctx || !key || !*key) return fail(ctx, MLC_ERR_ARG, "null argument");
+  return guarded(ctx, [&] {
+    ctx->tune[key] = choice;
+    ctx->tune_name[key] = "pinned " + std::to_string(choice);
+    ctx->tune_log.erase(key);
+  });
+}
+
 int mlc_ctx_autotune_report(mlc_ctx* ctx, char* buf, int cap) {
   if (!ctx || !buf || cap < 1) return -MLC_ERR_ARG;
   int n = 0;

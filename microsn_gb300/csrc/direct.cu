@@ -196,7 +196,7 @@ int conv_direct_choice(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const 
   char key[96];
   std::snprintf(key, sizeof key, "conv f32 %dx%d N%d%s", p.Nx, p.Ny, pN, spectrum ? " spectrum" : "");
   auto it = ctx->tune.find(key);
-  if (it != ctx->tune.end()) return it->second;
+  if (it != ctx->tune.end()) return it->second >= -1 && it->second < kNumVariants ? it->second : -1;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   MLC_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
   if (cs != cudaStreamCaptureStatusNone) return -1;
@@ -229,6 +229,33 @@ int conv_direct_choice(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const 
   }
   ctx->tune_log[key] = rec;
   return best.first;
+}
+
+bool p1_staged_choice(mlc_ctx* ctx, const FftPlan2D& p, const std::function<void(bool)>& run) {
+  char key[96];
+  const char* pn = p.prec == MLC_F64 ? "f64" : p.prec == MLC_F32 ? "f32" : p.prec == PREC_FF ? "f32x2" : "f32x2->f32";
+  std::snprintf(key, sizeof key, "conv P1 %s %dx%d", pn, p.Nx, p.Ny);
+  auto it = ctx->tune.find(key);
+  if (it != ctx->tune.end()) return it->second != 0;
+  if (!ctx->autotune) return false;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  MLC_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return false;
+  struct TimingOff {
+    mlc_ctx* c;
+    bool saved;
+    ~TimingOff() { c->timing = saved; }
+  } off{ctx, ctx->timing};
+  ctx->timing = false;
+  const float t0 = time_on_stream(ctx, [&] { run(false); });
+  const float t1 = time_on_stream(ctx, [&] { run(true); });
+  const int choice = t1 < t0 ? 1 : 0;
+  ctx->tune[key] = choice;
+  ctx->tune_name[key] = choice ? "smem-staged" : "l2-prefetch";
+  char rec[96];
+  std::snprintf(rec, sizeof rec, "l2-prefetch=%.4f smem-staged=%.4f", t0, t1);
+  ctx->tune_log[key] = rec;
+  return choice != 0;
 }
 
 void conv_auto(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const void* Fmap, const double* prof, int pN,

@@ -323,9 +323,21 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
 // CTAs (32 warps) per SM, the same number of barriers as the three-level form.
 template <typename T, int JP>
 __device__ __forceinline__ void c2r5_level(C2<T>* s, const C2<T>* w) {
-  constexpr int SP = JP / 5, WS = 625 / JP;
+  constexpr int SP = JP / 5, WS = 625 / JP, NB = 5000 / JP;
   for (int it = threadIdx.x; it < 1000; it += blockDim.x) {
-    const int blk = it / SP, m = it - blk * SP;
+    // Item (blk, m) reads and writes s[blk JP + m + r SP], r < 5.  With runs of SP >= 32 the
+    // warp's 32 consecutive m are 32 consecutive elements; shorter runs (JP = 125, 25) would
+    // put a warp over blocks JP apart in a few banks (a 5-way conflict at JP = 25), so there
+    // consecutive threads take consecutive blocks instead: stride JP (odd) in 16-byte
+    // elements spreads them over every bank, and the warp shares its twiddles.
+    int blk, m;
+    if constexpr (SP >= 32) {
+      blk = it / SP;
+      m = it - blk * SP;
+    } else {
+      m = it / NB;
+      blk = it - m * NB;
+    }
     C2<T>* b = s + blk * JP + m;
     C2<T> u[5];
 #pragma unroll
@@ -582,7 +594,11 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
 // most 160 threads are held to 40 registers (ten CTAs per SM instead of seven for 10 x 10,
 // 8 bytes of spills): this pass waits on latency, and the extra CTAs hide more of it
 // (4.31 -> 4.13 ms per 16 profiles at 10000^2).
-template <typename T, int CW, int L1, int L2>
+// STAGE: the map-spectrum tile is copied into shared memory (cp.async, 16 bytes per copy,
+// issued at the start and waited for before forward stage 2) instead of being prefetched
+// into L2 and read from there in stage 2: no global-load latency in stage 2, for
+// N2 CW sizeof(C2<T>) more shared memory per CTA (fewer resident CTAs).
+template <typename T, int CW, int L1, int L2, bool STAGE = false>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) ? 6 : 0) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
                                                      long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
                                                      int N1, const C2<T>* __restrict__ twy, T scale) {
@@ -593,16 +609,28 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
   C2<T>* w1 = y + N2 * CW;                        // W_N1^(n1 kk), n1 < N1
   C2<T>* w2 = w1 + N1;                            // W_Ny^(n kk), n < N2
   C2<T>* wl = w2 + N2;                            // W_N2^m, m < N2
+  C2<T>* fs = wl + N2;                            // STAGE: [N2][CW] map-spectrum tile
   const int kk = blockIdx.y;
   const long col0 = (long)blockIdx.x * CW;
   const int c = threadIdx.x % CW, g = threadIdx.x / CW;
-  // the map-spectrum tile (N2 rows of CW values, the only DRAM input) is needed in forward
-  // stage 2, after two L2 round trips and four barriers: start pulling it into L2 now
-  // (without registers or shared memory, which the other chain's P2 CTAs need)
-  constexpr int LINES = (int)(CW * sizeof(C2<T>) / 128);  // 128-byte lines per strip row
-  for (int n = threadIdx.x; n < N2 * LINES; n += blockDim.x)
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + ((long)kk * N2 + n / LINES) * pitch + col0 +
-                                                    (n % LINES) * (128 / (int)sizeof(C2<T>))));
+  if constexpr (STAGE) {
+    static_assert(sizeof(C2<T>) == 16, "staged form: 16-byte elements (FP64, float-float)");
+    constexpr int Q = CW;  // one 16-byte copy per element; fs starts at a multiple of 16 bytes
+    for (int n = threadIdx.x; n < N2 * Q; n += blockDim.x) {
+      const char* src = reinterpret_cast<const char*>(Fmap + ((long)kk * N2 + n / Q) * pitch + col0) + (n % Q) * 16;
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(reinterpret_cast<char*>(fs + (n / Q) * CW) + (n % Q) * 16);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  } else {
+    // the map-spectrum tile (N2 rows of CW values, the only DRAM input) is needed in forward
+    // stage 2, after two L2 round trips and four barriers: start pulling it into L2 now
+    // (without registers or shared memory, which the other chain's P2 CTAs need)
+    constexpr int LINES = (int)(CW * sizeof(C2<T>) / 128);  // 128-byte lines per strip row
+    for (int n = threadIdx.x; n < N2 * LINES; n += blockDim.x)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + ((long)kk * N2 + n / LINES) * pitch + col0 +
+                                                      (n % LINES) * (128 / (int)sizeof(C2<T>))));
+  }
   for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * kk) % N1) * N2);
   for (int n = threadIdx.x; n < N2; n += blockDim.x) {
     w2[n] = ldc(twy + (long)n * kk);
@@ -682,6 +710,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
       for (int k1 = 0; k1 < L1; k1++) y[(g * L1 + k1) * CW + c] = k1 == 0 ? v[0] : cmul(v[k1], wl[g * k1]);
     }
   }
+  if constexpr (STAGE) asm volatile("cp.async.wait_all;" ::: "memory");  // this thread's copies
   __syncthreads();
   // forward stage 2, product, inverse stage A: thread (k1 = g, c)
   if (g < L1) {
@@ -691,7 +720,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
     Dft<T, L2, false>::run(u);
 #pragma unroll
     for (int k2 = 0; k2 < L2; k2++) {
-      const C2<T> f = Fmap[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c];
+      const C2<T> f = STAGE ? fs[(g + L1 * k2) * CW + c] : Fmap[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c];
       u[k2] = cscale(cmul(f, u[k2]), scale);
     }
     Dft<T, L2, true>::run(u);  // over k2 -> n2
@@ -906,6 +935,11 @@ void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const d
     using K2 = void (*)(const C2<T>*, C2<T>*, long, const C2<T>*, int, int, int, const C2<T>*, T);
     K2 k2 = nullptr;
     int nthr = 0;
+    // float-float and FP64 at N2 = 100: the map-spectrum tile prefetched into L2, or staged in
+    // shared memory (chosen per map size by the autotuner, or pinned with mlc_ctx_tune_set)
+    K2 k2s = nullptr;
+    if constexpr (sizeof(C2<T>) == 16)
+      if (p.N2 == 100) k2s = k_conv_fused2<T, CW, 10, 10, true>;
     switch (p.N2) {
       case 100: k2 = k_conv_fused2<T, CW, 10, 10>; nthr = 10 * CW; break;
       case 128: k2 = k_conv_fused2<T, CW, 8, 16>; nthr = 16 * CW; break;
@@ -917,12 +951,21 @@ void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const d
     }
     if (k2) {
       const size_t smem2 = ((size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
-      set_max_smem((const void*)k2, smem2);
+      const size_t smem2s = smem2 + (size_t)p.N2 * CW * sizeof(C2<T>);
+      auto launch = [&](bool staged) {
+        const K2 k = staged ? k2s : k2;
+        const size_t sm = staged ? smem2s : smem2;
+        set_max_smem((const void*)k, sm);
+        k<<<dim3(nstrips, p.N1), nthr, sm, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp, (const C2<T>*)kx,
+                                                          h, p.Ny, p.N1, (const C2<T>*)p.twy, scale);
+      };
+      const bool staged = k2s && p1_staged_choice(ctx, p, [&](bool st) {
+                            launch(st);
+                            MLC_CHECK_LAUNCH();
+                          });
       {
         MLC_KSCOPE(ctx, "conv_fused_spectrum");
-        k2<<<dim3(nstrips, p.N1), nthr, smem2, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp,
-                                                              (const C2<T>*)kx, h, p.Ny, p.N1,
-                                                              (const C2<T>*)p.twy, scale);
+        launch(staged);
       }
       MLC_CHECK_LAUNCH();
       launch_colpass<T, true>(ctx, p, tmp, 'A', 0);

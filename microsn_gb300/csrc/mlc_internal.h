@@ -1,6 +1,7 @@
 // Internal host-side state of the library: context, workspace pool, maps, FFT plans.
 #pragma once
 
+#include <functional>
 #include <map>
 #include <memory>
 #include <string>
@@ -190,6 +191,10 @@ int conv_direct_choice(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const 
 void conv_auto(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const void* Fmap, const double* prof, int pN,
                void* out);
 std::string autotune_report(mlc_ctx* ctx);
+// The fused convolution's P1 variant for this map size and arithmetic: true for the one that
+// stages the map-spectrum tile in shared memory.  The autotuner times run(false) and
+// run(true) once per key; a pinned or earlier choice is reused.
+bool p1_staged_choice(mlc_ctx* ctx, const FftPlan2D& p, const std::function<void(bool)>& run);
 // conv_fused up to P2: the inverse half-spectrum (Ny x Wp complex) into spec_out.
 void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
                          void* spec_out, int kx_slot = WS_KX);

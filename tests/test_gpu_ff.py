@@ -107,7 +107,7 @@ def test_ff_fp32_map_convolution_matches_oracle(ctx, Ny, Nx):
         assert _rel(got.cpu().numpy().astype(np.float64), ref, 1e-3 * ref.mean()) < FF32_REL, (shape, rhalf)
 
 
-@pytest.mark.parametrize("N,nprof", [(2000, 12), (360, 5)])
+@pytest.mark.parametrize("N,nprof", [(2000, 12), (360, 5), (10000, 2)])
 def test_ff_fp32_map_batched_step_matches_fp64(ctx, N, nprof):
     """The batched step of an FP32 map in float-float mode against the FP64 step on the same
     pixels: FP32 magnitudes within a few FP32 ulp of the FP64 ones."""
@@ -130,3 +130,26 @@ def test_ff_fp32_map_batched_step_matches_fp64(ctx, N, nprof):
     # FP32 magnitudes: the flux within FP32_REL (1.0857 FP32_REL in magnitude), then the FP32
     # logarithm and its rounding (|m| < 8: an ulp is at most 9.5e-7)
     assert float((got.double()[fin] - ref[fin]).abs().max()) < 1.0857 * FF32_REL + 2e-6
+
+
+@pytest.mark.parametrize("prec,key", [("f32", "conv P1 f32x2->f32 10000x10000"), ("f64", "conv P1 f32x2 10000x10000")])
+def test_p1_staged_and_prefetched_forms_agree(lib_built, prec, key):
+    """The fused convolution's P1 in float-float arithmetic at 10000^2 (N2 = 100), with the map
+    spectrum prefetched into L2 or staged in shared memory (the autotuner's two candidates,
+    pinned here): the same arithmetic, so the same pixels bit for bit."""
+    import microsn_gb300 as mlc
+    N = 10000
+    dt = np.float32 if prec == "f32" else np.float64
+    mp = synth.lognormal_map(N, seed=17).astype(dt)
+    p = mlc.profile("exponential", 12.0, 1.0, ref_compat=False)
+    out = []
+    for choice in (0, 1):
+        c = mlc.Context(0)
+        c.tune_set(key, choice)
+        m = mlc.Map(c, mp, prec)
+        m.set_fft("f32x2")
+        out.append(mlc.convolve(c, m, p, "fused").cpu())
+        assert c.autotune_report()[key][0] == f"pinned {choice}"
+        m.close()
+        c.close()
+    assert torch.equal(out[0], out[1])
