@@ -113,8 +113,10 @@ int mlc_ctx_autotune_report(mlc_ctx* ctx, char* buf, int cap);
 /* Pins the autotuner's choice for one key (as the report prints it; used whether or not
  * the autotuner is on), e.g. to compare variants or to fix a run's kernels:
  *   "conv f32 <Nx>x<Ny> N<pN>[ spectrum]": -1 FFT form, 0..3 direct tile shape;
- *   "conv P1 <arithmetic> <Nx>x<Ny>": 0 map spectrum prefetched into L2, 1 staged in
- *     shared memory (float-float and FP64 transforms);
+ *   "conv P1 <arithmetic> <Nx>x<Ny>[ two-chain]": 0 map spectrum prefetched into L2, 1
+ *     staged in shared memory (float-float and FP64 transforms); " two-chain" is the
+ *     batched step's key, where the second convolution chain runs alongside (not timed:
+ *     0 unless pinned);
  *   "pairdiff_tc K<64|128>[ matrix] bins<1024|4096> pairs~4^<k>": epilogue warps 12, 16
  *     or 24.
  * Other values fall back to the default. */

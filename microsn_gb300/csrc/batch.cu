@@ -358,6 +358,11 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
       MLC_CUDA(cudaEventRecord(b->spec_ready, ctx->stream));
       MLC_CUDA(cudaStreamWaitEvent(b->aux, b->spec_ready, 0));
     }
+    struct ChainsFlag {  // the convolutions below know they share the GPU with a second chain
+      mlc_ctx* c;
+      ~ChainsFlag() { c->two_chains = false; }
+    } chains_flag{ctx};
+    ctx->two_chains = two;
     for (int q = 0; q < nm; q++) {
       mp[q] = maps + (size_t)q * slot;
       const double* pr = dprof + poff[g0 + q];

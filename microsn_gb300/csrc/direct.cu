@@ -234,10 +234,15 @@ int conv_direct_choice(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const 
 bool p1_staged_choice(mlc_ctx* ctx, const FftPlan2D& p, const std::function<void(bool)>& run) {
   char key[96];
   const char* pn = p.prec == MLC_F64 ? "f64" : p.prec == MLC_F32 ? "f32" : p.prec == PREC_FF ? "f32x2" : "f32x2->f32";
-  std::snprintf(key, sizeof key, "conv P1 %s %dx%d", pn, p.Nx, p.Ny);
+  // Beside the second convolution chain of the batched step the staged form's extra shared
+  // memory crowds out the other chain's CTAs: measured alone it is the faster form (1.06
+  // against 1.11 ms per profile at 10000^2, float-float), in the step the slower one (54.4
+  // against 53.5 ms per step).  That context has its own key, not timed, prefetching unless
+  // pinned.
+  std::snprintf(key, sizeof key, "conv P1 %s %dx%d%s", pn, p.Nx, p.Ny, ctx->two_chains ? " two-chain" : "");
   auto it = ctx->tune.find(key);
   if (it != ctx->tune.end()) return it->second != 0;
-  if (!ctx->autotune) return false;
+  if (!ctx->autotune || ctx->two_chains) return false;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   MLC_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
   if (cs != cudaStreamCaptureStatusNone) return false;

@@ -94,6 +94,7 @@ struct mlc_ctx {
   mlc::BatchIO* batch = nullptr;
   // launch autotuner: key -> choice (-1: FFT form; >= 0: direct tile shape), candidate timings
   bool autotune = true;
+  bool two_chains = false;  // set while the batched step runs two convolution chains side by side
   std::map<std::string, int> tune;
   std::map<std::string, std::string> tune_log;
   std::map<std::string, std::string> tune_name;  // the choice as the report prints it

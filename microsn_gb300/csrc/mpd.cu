@@ -36,26 +36,44 @@ static float f32_up(double x) {
   return f;
 }
 
+// Positive floating-point values order like their bit patterns read as signed integers,
+// and every value outside (0, +inf) falls outside [vmin, vmax) as an integer too (negative
+// values and -0.0 read negative, +inf and NaN above vmax's bits): the range test and the
+// edge search below are integer compares, with results identical to FP64 compares -- GB300's
+// FP64 pipe is narrow, and this kernel made one to three FP64 compares per pixel.
+__device__ __forceinline__ long long order_bits(double v) { return __double_as_longlong(v); }
+__device__ __forceinline__ int order_bits(float v) { return __float_as_int(v); }
+
+// log2 of a positive value, within 0.09, from its exponent and leading mantissa bits: a
+// guess of the bin (off by a few bins) that the exact edge search then corrects.
+__device__ __forceinline__ float log2_guess(long long b) {
+  return (float)((int)(b >> 32) - (1023 << 20)) * 0x1p-20f;
+}
+__device__ __forceinline__ float log2_guess(int b) { return (float)(b - (127 << 23)) * 0x1p-23f; }
+
 template <typename T>
 __global__ void __launch_bounds__(512) k_binned_mpd(const T* __restrict__ data, long npix, int nb,
                                                     const T* __restrict__ edges, T vmin, T vmax, float logmin,
                                                     float inv_dl, unsigned long long* __restrict__ counts) {
+  using B = decltype(order_bits(T()));
   extern __shared__ unsigned char smem_raw[];
-  T* e = reinterpret_cast<T*>(smem_raw);
+  B* e = reinterpret_cast<B*>(smem_raw);
   uint32_t* c = reinterpret_cast<uint32_t*>(e + nb);
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
-    e[i] = edges[i];
+    e[i] = order_bits(edges[i]);
     c[i] = 0;
   }
   __syncthreads();
+  const B lo = order_bits(vmin), hi = order_bits(vmax);  // vmin > 0
+  const float ga = 0.30102999566398120f * inv_dl, gb = -logmin * inv_dl;  // bins per log2, offset
   const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
   for (long base = blockIdx.x * (long)blockDim.x; base < npix; base += (long)gridDim.x * blockDim.x) {
     const long p = base + threadIdx.x;
     int bin = -1;
     if (p < npix) {
-      const T v = data[p];
-      if (v >= vmin && v < vmax) {
-        const float g = (log10f((float)v) - logmin) * inv_dl;
+      const B v = order_bits(data[p]);
+      if (v >= lo && v < hi) {
+        const float g = fmaf(log2_guess(v), ga, gb);
         int i = g < 0.f ? 0 : (g > (float)nb ? nb : (int)g);
         while (i > 0 && v <= e[i - 1]) i--;
         while (i < nb && v > e[i]) i++;

@@ -7,6 +7,7 @@
 // them through L1/L2; the z ranking uses the hand-written radix sort; bin means are a
 // parallel segmented reduction; and a fused variant computes each pair's z bin directly
 // and accumulates chi2 and exp(-chi2/2) per bin without any Nloc^2 array.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -117,15 +118,23 @@ __global__ void __launch_bounds__(256) k_pair_chi2_ratio(const double* __restric
   chi2[rank ? rank[p] : p] = c;
 }
 
-// Per bin: mean chi2 and mean exp(-chi2/2) over its slice; one CTA per bin.
-__global__ void __launch_bounds__(256) k_bin_means(const double* __restrict__ chi2, const uint32_t* __restrict__ lower,
-                                                   const uint32_t* __restrict__ nper, double* __restrict__ bchi2,
-                                                   double* __restrict__ bexp) {
-  const int bin = blockIdx.x;
-  const uint32_t n = nper[bin], lo = lower[bin];
+// Bin means of the rank-ordered chi2 (bin_chi2_GPU): every bin's slice is cut into pieces
+// of at most BIN_PIECE values, one CTA per piece sums chi2 and exp(-chi2/2) over it, and a
+// second kernel adds each bin's pieces in order -- a fixed summation order (the result does
+// not depend on timing), and a bin of millions of pairs is spread over many CTAs (one CTA
+// per bin left most SMs idle behind the largest bins).
+constexpr uint32_t BIN_PIECE = 1u << 15;
+struct BinPiece {
+  uint32_t first, count;
+};
+
+__global__ void __launch_bounds__(256) k_bin_piece_sums(const double* __restrict__ chi2,
+                                                        const BinPiece* __restrict__ pieces,
+                                                        double* __restrict__ psum, double* __restrict__ pexp) {
+  const BinPiece pc = pieces[blockIdx.x];
   double sc = 0.0, se = 0.0;
-  for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
-    const double c = chi2[(long)lo + k];
+  for (uint32_t k = threadIdx.x; k < pc.count; k += blockDim.x) {
+    const double c = chi2[(long)pc.first + k];
     sc += c;
     se += exp(-0.5 * c);
   }
@@ -145,14 +154,31 @@ __global__ void __launch_bounds__(256) k_bin_means(const double* __restrict__ ch
       a += r1[w];
       b += r2[w];
     }
-    if (n > 0) {
-      bexp[bin] = b / n;
-      bchi2[bin] = a / n;
-    } else {
-      bexp[bin] = exp(-2000.0 / 2.0);
-      bchi2[bin] = 2000.0;
-    }
+    psum[blockIdx.x] = a;
+    pexp[blockIdx.x] = b;
   }
+}
+
+// Per bin: the sum of its pieces [pfirst[bin], pfirst[bin + 1]) over its count; an empty bin
+// gets the reference's values (chi2 2000, exp(-1000)).
+__global__ void k_bin_combine(const uint32_t* __restrict__ pfirst, const uint32_t* __restrict__ nper,
+                              const double* __restrict__ psum, const double* __restrict__ pexp, int nb,
+                              double* __restrict__ bchi2, double* __restrict__ bexp) {
+  const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bin >= nb) return;
+  const uint32_t n = nper[bin];
+  if (n == 0) {
+    bexp[bin] = exp(-2000.0 / 2.0);
+    bchi2[bin] = 2000.0;
+    return;
+  }
+  double a = 0.0, b = 0.0;
+  for (uint32_t q = pfirst[bin]; q < pfirst[bin + 1]; q++) {
+    a += psum[q];
+    b += pexp[q];
+  }
+  bexp[bin] = b / n;
+  bchi2[bin] = a / n;
 }
 
 // Fused rank-free pair binning.  Bin of z = LCA_a / LCB_b: smallest i with z <= edge_i,
@@ -352,21 +378,41 @@ void pair_chi2_ratio(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, co
 void bin_chi2(mlc_ctx* ctx, int Nbins, const uint32_t* lower_host, const uint32_t* nper_host,
               const double* chi2_sorted, double* bchi2_host, double* bexp_host) {
   if (Nbins <= 0) return;
-  char* sm = (char*)ws_get(ctx, WS_SMALL, (sizeof(double) * 2 + sizeof(uint32_t) * 2) * Nbins + 64);
+  std::vector<BinPiece> pieces;
+  std::vector<uint32_t> pfirst(Nbins + 1), nper(nper_host, nper_host + Nbins);
+  for (int b = 0; b < Nbins; b++) {
+    pfirst[b] = (uint32_t)pieces.size();
+    for (uint32_t k = 0; k < nper_host[b]; k += BIN_PIECE)
+      pieces.push_back(BinPiece{lower_host[b] + k, std::min(BIN_PIECE, nper_host[b] - k)});
+  }
+  pfirst[Nbins] = (uint32_t)pieces.size();
+  const size_t np = std::max<size_t>(pieces.size(), 1);
+  char* sm = (char*)ws_get(ctx, WS_SMALL, sizeof(double) * (2 * Nbins + 2 * np) + sizeof(BinPiece) * np +
+                                              sizeof(uint32_t) * (2 * Nbins + 1) + 256);
   double* bc = (double*)sm;
   double* be = bc + Nbins;
-  uint32_t* lo = reinterpret_cast<uint32_t*>(be + Nbins);
-  uint32_t* np = lo + Nbins;
-  MLC_CUDA(cudaMemcpyAsync(lo, lower_host, sizeof(uint32_t) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
-  MLC_CUDA(cudaMemcpyAsync(np, nper_host, sizeof(uint32_t) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
-  {
+  double* ps = be + Nbins;
+  double* pe = ps + np;
+  BinPiece* dp = reinterpret_cast<BinPiece*>(pe + np);
+  uint32_t* dfirst = reinterpret_cast<uint32_t*>(dp + np);
+  uint32_t* dn = dfirst + Nbins + 1;
+  if (!pieces.empty())
+    MLC_CUDA(cudaMemcpyAsync(dp, pieces.data(), sizeof(BinPiece) * pieces.size(), cudaMemcpyHostToDevice, ctx->stream));
+  MLC_CUDA(cudaMemcpyAsync(dfirst, pfirst.data(), sizeof(uint32_t) * (Nbins + 1), cudaMemcpyHostToDevice, ctx->stream));
+  MLC_CUDA(cudaMemcpyAsync(dn, nper.data(), sizeof(uint32_t) * Nbins, cudaMemcpyHostToDevice, ctx->stream));
+  if (!pieces.empty()) {
     MLC_KSCOPE(ctx, "pair_bin_means");
-    k_bin_means<<<Nbins, 256, 0, ctx->stream>>>(chi2_sorted, lo, np, bc, be);
+    k_bin_piece_sums<<<(unsigned)pieces.size(), 256, 0, ctx->stream>>>(chi2_sorted, dp, ps, pe);
+  }
+  MLC_CHECK_LAUNCH();
+  {
+    MLC_KSCOPE(ctx, "pair_bin_combine");
+    k_bin_combine<<<ceil_div(Nbins, 128), 128, 0, ctx->stream>>>(dfirst, dn, ps, pe, Nbins, bc, be);
   }
   MLC_CHECK_LAUNCH();
   MLC_CUDA(cudaMemcpyAsync(bchi2_host, bc, sizeof(double) * Nbins, cudaMemcpyDeviceToHost, ctx->stream));
   MLC_CUDA(cudaMemcpyAsync(bexp_host, be, sizeof(double) * Nbins, cudaMemcpyDeviceToHost, ctx->stream));
-  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));  // (also keeps the host vectors alive for the copies)
 }
 
 void pair_bin_fused(mlc_ctx* ctx, int Njp, const int* indA, const int* indB, const double* facA,
