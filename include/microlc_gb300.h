@@ -121,6 +121,19 @@ int mlc_ctx_autotune_report(mlc_ctx* ctx, char* buf, int cap);
  *     or 24.
  * Other values fall back to the default. */
 int mlc_ctx_tune_set(mlc_ctx* ctx, const char* key, int choice);
+
+/* Cached profile spectra (no reference counterpart; the reference transforms the full-size
+ * kernel of every profile for every map, gpu_functions.cu:183-201).  mlc_convolve_sample_tracks
+ * and mlc_convolve_many keep the spectra of their last profile list -- each profile's
+ * spectrum as the fused convolution holds it before the product with the map spectrum --
+ * and reuse them while the list, the map size and the transform arithmetic repeat: a
+ * convolution then skips the profile's transform (P0 and the forward half of P1; the same
+ * operations on the same values otherwise, so the same results bit for bit).  They take
+ * nprof x (Ny x (Nx/2+1) complex) of the map's transform arithmetic: 800 MB per profile at
+ * 10000^2 in float-float.  max_bytes: -1 (default) a quarter of the device memory, 0 never
+ * cache, else the limit; lists that do not fit are convolved without the cache.  Map sizes
+ * whose column split has N2 = 100 or 128 (e.g. 2000^2 ... 10000^2, 8192^2). */
+int mlc_ctx_set_profile_cache(mlc_ctx* ctx, long long max_bytes);
 int mlc_ctx_kernel_times(mlc_ctx* ctx, char* names_host, int name_cap, double* ms_host, long* launches_host,
                          int cap, int reset);
 

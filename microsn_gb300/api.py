@@ -83,6 +83,10 @@ class Context:
         """Launch autotuner on (default) or off (FFT form everywhere)."""
         self.check(self.L.mlc_ctx_set_autotune(self.h, int(on)))
 
+    def set_profile_cache(self, max_bytes: int = -1):
+        """Device bytes the cached profile spectra may take (-1: a quarter of the device, 0: off)."""
+        self.check(self.L.mlc_ctx_set_profile_cache(self.h, int(max_bytes)))
+
     def tune_set(self, key: str, choice: int):
         """Pin the autotuner's choice for one key (see mlc_ctx_tune_set)."""
         self.check(self.L.mlc_ctx_tune_set(self.h, key.encode(), int(choice)))

@@ -143,6 +143,12 @@ int mlc_ctx_set_autotune(mlc_ctx* ctx, int on) {
   return guarded(ctx, [&] { ctx->autotune = on != 0; });
 }
 
+int mlc_ctx_set_profile_cache(mlc_ctx* ctx, long long max_bytes) {
+  if (!ctx) return MLC_ERR_ARG;
+  if (max_bytes < -1) return fail(ctx, MLC_ERR_ARG, "max_bytes: -1, 0 or a byte count");
+  return guarded(ctx, [&] { ctx->profile_cache_bytes = max_bytes; });
+}
+
 int mlc_ctx_tune_set(mlc_ctx* ctx, const char* key, int choice) {
   if (!ctx || !key || !*key) return fail(ctx, MLC_ERR_ARG, "null argument");
   return guarded(ctx, [&] {

@@ -69,6 +69,11 @@ struct BatchIO {
   std::vector<int> prof_N;
   std::vector<size_t> prof_off;
   int parity = 0;
+  // the profiles' spectra (as the fused convolution's P1 holds them before the product with
+  // the map spectrum) of the last profile list, map size and transform arithmetic
+  void* kcache = nullptr;
+  size_t kcache_cap = 0, kcache_stride = 0;
+  std::vector<unsigned char> kcache_key;
   // the kernel sequences of the last mlc_convolve_many and mlc_convolve_sample_tracks calls
   // with MLC_GRAPH, each replayed while every pointer and size it baked in stays the same
   cudaStream_t cap = nullptr;
@@ -146,6 +151,7 @@ void batch_release(mlc_ctx* ctx) {
   if (b->aux) cudaStreamDestroy(b->aux);
   if (b->tail) cudaStreamDestroy(b->tail);
   if (b->prof_dev) cudaFree(b->prof_dev);
+  if (b->kcache) cudaFree(b->kcache);
   for (GraphSlot* g : {&b->many, &b->step})
     if (g->exec) cudaGraphExecDestroy(g->exec);
   if (b->cap) cudaStreamDestroy(b->cap);
@@ -235,6 +241,32 @@ static const double* stage_profiles(mlc_ctx* ctx, BatchIO* b, int par, int nprof
   b->prof_N = pN;
   b->prof_off = poff;
   return dprof;
+}
+
+// The profile spectra of the list just staged (stage_profiles), computed once and kept while
+// the list, the map size and the transform arithmetic repeat: a convolution then reads its
+// profile's spectrum instead of transforming the profile (P0 and half of P1).  nullptr
+// where the plan has no cached form or the spectra would exceed the context's budget.
+static const char* profile_cache(mlc_ctx* ctx, BatchIO* b, const FftPlan2D& p, int nprof, const double* dprof,
+                                 const std::vector<int>& pN, const std::vector<size_t>& poff) {
+  if (ctx->profile_cache_bytes == 0 || !profile_spectrum_supported(p)) return nullptr;
+  std::vector<unsigned char> key = b->prof_key;
+  key.push_back((unsigned char)p.prec);
+  if (b->kcache && key == b->kcache_key) return (const char*)b->kcache;
+  size_t budget = (size_t)ctx->profile_cache_bytes;
+  if (ctx->profile_cache_bytes < 0) {
+    size_t fr = 0, tot = 0;
+    MLC_CUDA(cudaMemGetInfo(&fr, &tot));
+    budget = tot / 4;
+  }
+  const size_t stride = (size_t)round_up((long)p.spec_bytes(), 256);
+  if ((size_t)nprof * stride > budget) return nullptr;
+  b->kcache_key.clear();  // invalid until the new spectra are queued
+  char* kc = (char*)grow_dev(ctx, b, b->kcache, b->kcache_cap, (size_t)nprof * stride);
+  for (int k = 0; k < nprof; k++) profile_spectrum(ctx, p, dprof + poff[k], pN[k], kc + (size_t)k * stride);
+  b->kcache_stride = stride;
+  b->kcache_key = std::move(key);
+  return kc;
 }
 
 template <typename T>
@@ -335,6 +367,7 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
   // cluster kernel runs the last pass of all the group's profiles straight into the
   // interleaved layout (no planar maps, no separate interleave pass).
   const bool fuse_il = ntr > 0 && mode == MLC_CONV_FUSED && rows_c2r_interleave_supported(*p);
+  const char* kc = fuse_il ? profile_cache(ctx, b, *p, nprof, dprof, pN, poff) : nullptr;
   const size_t slot = fuse_il ? p->spec_bytes() : (size_t)npix * es;
   char* maps = (char*)ws_get(ctx, WS_BATCH_MAPS, (size_t)nm_max * slot);
   void* imap = ntr > 0 ? ws_get(ctx, WS_BATCH_IMAP, (size_t)pow2_at_least(nm_max) * npix * es) : nullptr;
@@ -376,14 +409,16 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
         cudaStream_t main = ctx->stream;
         ctx->stream = b->aux;
         try {
-          conv_fused_spectrum(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q], WS_KX2);
+          if (kc) conv_cached_spectrum(ctx, *p, map->spec, kc + (size_t)(g0 + q) * b->kcache_stride, (void*)mp[q]);
+          else conv_fused_spectrum(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q], WS_KX2);
         } catch (...) {
           ctx->stream = main;
           throw;
         }
         ctx->stream = main;
       } else if (fuse_il) {
-        conv_fused_spectrum(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
+        if (kc) conv_cached_spectrum(ctx, *p, map->spec, kc + (size_t)(g0 + q) * b->kcache_stride, (void*)mp[q]);
+        else conv_fused_spectrum(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
       } else if (mode == MLC_CONV_FUSED) {
         conv_fused(ctx, *p, map->spec, pr, pN[g0 + q], (void*)mp[q]);
       } else {
@@ -526,12 +561,17 @@ void convolve_sample_tracks(mlc_ctx* ctx, mlc_map* map, const void* pixels, int 
   std::vector<int> pN;
   std::vector<size_t> poff;
   const double* dprof = stage_profiles(ctx, b, b->parity, nprof, profs, map->Nx, map->Ny, pN, poff);
+  // and the profile spectra, recomputed here (outside the graph) when the list changed
+  FftPlan2D* p = plan_get(ctx, map->Nx, map->Ny, map_fft_prec(map));
+  const bool fuse_il = tr.ntracks > 0 && mode == MLC_CONV_FUSED && rows_c2r_interleave_supported(*p);
+  const char* kc = fuse_il ? profile_cache(ctx, b, *p, nprof, dprof, pN, poff) : nullptr;
   auto key = [&] {
     std::vector<uint64_t> kv = {(uint64_t)map,      (uint64_t)map->data, (uint64_t)map->spec, (uint64_t)pixels,
                                 (uint64_t)nprof,    (uint64_t)mode,      (uint64_t)mag,       (uint64_t)out,
                                 (uint64_t)tr.x0,    (uint64_t)tr.y0,     (uint64_t)tr.phi,    (uint64_t)tr.v,
                                 (uint64_t)tr.off,   (uint64_t)tr.t,      (uint64_t)tr.ntracks, (uint64_t)tr.nepochs,
-                                (uint64_t)dprof,    (uint64_t)map_fft_prec(map), (uint64_t)ctx->autotune};
+                                (uint64_t)dprof,    (uint64_t)map_fft_prec(map), (uint64_t)ctx->autotune,
+                                (uint64_t)kc};
     for (int s = 0; s < WS_NSLOTS; s++) kv.push_back((uint64_t)ctx->ws_ptr[s]);
     for (int k = 0; k < nprof; k++) kv.push_back((uint64_t)pN[k]);
     return kv;
@@ -557,16 +597,22 @@ void convolve_many(mlc_ctx* ctx, mlc_map* map, int nprof, const mlc_profile* pro
   std::vector<size_t> poff;
   const double* dprof = stage_profiles(ctx, b, par, nprof, profs, map->Nx, map->Ny, pN, poff);
   const size_t es = map->prec == MLC_F64 ? 8 : 4;
+  const char* kc = mode == MLC_CONV_FUSED ? profile_cache(ctx, b, *p, nprof, dprof, pN, poff) : nullptr;
   auto enqueue = [&] {
     for (int k = 0; k < nprof; k++) {
       void* o = (char*)out + (size_t)k * stride * es;
-      if (mode == MLC_CONV_FUSED) conv_auto(ctx, *p, map->data, map->spec, dprof + poff[k], pN[k], o);
-      else conv_plain(ctx, *p, map->spec, dprof + poff[k], pN[k], o);
+      if (mode != MLC_CONV_FUSED) {
+        conv_plain(ctx, *p, map->spec, dprof + poff[k], pN[k], o);
+      } else if (kc && conv_direct_choice(ctx, *p, map->data, map->spec, dprof + poff[k], pN[k], o, false) < 0) {
+        conv_cached(ctx, *p, map->spec, kc + (size_t)k * b->kcache_stride, o);
+      } else {
+        conv_auto(ctx, *p, map->data, map->spec, dprof + poff[k], pN[k], o);
+      }
     }
   };
   auto key = [&] {
     std::vector<uint64_t> kv = {(uint64_t)map, (uint64_t)map->spec, (uint64_t)nprof, (uint64_t)mode, (uint64_t)out,
-                                (uint64_t)stride, (uint64_t)dprof};
+                                (uint64_t)stride, (uint64_t)dprof, (uint64_t)kc};
     for (int s = 0; s < WS_NSLOTS; s++) kv.push_back((uint64_t)ctx->ws_ptr[s]);
     for (int k = 0; k < nprof; k++) kv.push_back((uint64_t)pN[k]);
     return kv;

@@ -219,6 +219,34 @@ void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, con
   else conv_fused_impl<float>(ctx, p, Fmap, prof, pN, nullptr, spec_out, kx_slot);
 }
 
+bool profile_spectrum_supported(const FftPlan2D& p) {
+  if (prec_is_ff(p.prec)) return profile_spectrum_supported_impl<ff>(p);
+  if (p.prec == MLC_F64) return profile_spectrum_supported_impl<double>(p);
+  return profile_spectrum_supported_impl<float>(p);
+}
+
+void profile_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const double* prof, int pN, void* ks) {
+  if (prec_is_ff(p.prec)) profile_spectrum_impl<ff>(ctx, p, prof, pN, ks);
+  else if (p.prec == MLC_F64) profile_spectrum_impl<double>(ctx, p, prof, pN, ks);
+  else profile_spectrum_impl<float>(ctx, p, prof, pN, ks);
+}
+
+void conv_cached_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* spec_out) {
+  if (prec_is_ff(p.prec)) conv_cached_impl<ff>(ctx, p, Fmap, ks, spec_out);
+  else if (p.prec == MLC_F64) conv_cached_impl<double>(ctx, p, Fmap, ks, spec_out);
+  else conv_cached_impl<float>(ctx, p, Fmap, ks, spec_out);
+}
+
+void conv_cached(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* out) {
+  if (p.prec == PREC_FFS) {
+    void* tmp = ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
+    conv_cached_impl<ff>(ctx, p, Fmap, ks, tmp);
+    rows_c2r_impl<ff, float>(ctx, p, tmp, out);
+  } else if (p.prec == PREC_FF) conv_cached_real_impl<ff>(ctx, p, Fmap, ks, out);
+  else if (p.prec == MLC_F64) conv_cached_real_impl<double>(ctx, p, Fmap, ks, out);
+  else conv_cached_real_impl<float>(ctx, p, Fmap, ks, out);
+}
+
 bool rows_c2r_interleave_supported(const FftPlan2D& p) {
   return (p.M == 5000 || p.M == 4096 || p.M == 2000 || p.M == 1000) && p.Ny <= 65535;  // rows on grid.y
 }

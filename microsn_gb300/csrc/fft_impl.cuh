@@ -598,10 +598,17 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
 // issued at the start and waited for before forward stage 2) instead of being prefetched
 // into L2 and read from there in stage 2: no global-load latency in stage 2, for
 // N2 CW sizeof(C2<T>) more shared memory per CTA (fewer resident CTAs).
-template <typename T, int CW, int L1, int L2, bool STAGE = false>
+// MODE splits the pass around the profile's spectrum, for profiles that are convolved with
+// many maps: 1 stops after forward stage 2 and stores the profile's spectrum in the map
+// spectrum's layout into ks (as the registers hold it, so that mode 2 continues exactly as
+// mode 0 would); 2 starts from it (ks times the map spectrum, then the inverse stages) --
+// no profile sub-pass and no forward transform.  0 is the whole pass.
+template <typename T, int CW, int L1, int L2, bool STAGE = false, int MODE = 0>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) ? 6 : 0) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
                                                      long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
-                                                     int N1, const C2<T>* __restrict__ twy, T scale) {
+                                                     int N1, const C2<T>* __restrict__ twy, T scale,
+                                                     C2<T>* __restrict__ ks) {
+  static_assert(MODE >= 0 && MODE <= 2 && (!STAGE || MODE == 0), "P1 modes");
   constexpr int N2 = L1 * L2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* a = reinterpret_cast<C2<T>*>(smem_raw);  // [N2][CW] profile column sub-pass
@@ -622,21 +629,26 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
       asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
-  } else {
+  } else if constexpr (MODE != 1) {
     // the map-spectrum tile (N2 rows of CW values, the only DRAM input) is needed in forward
     // stage 2, after two L2 round trips and four barriers: start pulling it into L2 now
-    // (without registers or shared memory, which the other chain's P2 CTAs need)
+    // (without registers or shared memory, which the other chain's P2 CTAs need); mode 2
+    // reads the profile's spectrum tile there as well
     constexpr int LINES = (int)(CW * sizeof(C2<T>) / 128);  // 128-byte lines per strip row
-    for (int n = threadIdx.x; n < N2 * LINES; n += blockDim.x)
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + ((long)kk * N2 + n / LINES) * pitch + col0 +
-                                                      (n % LINES) * (128 / (int)sizeof(C2<T>))));
+    for (int n = threadIdx.x; n < N2 * LINES; n += blockDim.x) {
+      const long e = ((long)kk * N2 + n / LINES) * pitch + col0 + (n % LINES) * (128 / (int)sizeof(C2<T>));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(Fmap + e));
+      if constexpr (MODE == 2) asm volatile("prefetch.global.L2 [%0];" ::"l"(ks + e));
+    }
   }
-  for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * kk) % N1) * N2);
+  if constexpr (MODE != 2)
+    for (int n1 = threadIdx.x; n1 < N1; n1 += blockDim.x) w1[n1] = ldc(twy + ((n1 * kk) % N1) * N2);
   for (int n = threadIdx.x; n < N2; n += blockDim.x) {
     w2[n] = ldc(twy + (long)n * kk);
     wl[n] = ldc(twy + (long)n * N1);
   }
   __syncthreads();
+  if constexpr (MODE != 2) {
   // profile: column sub-pass A restricted to its non-zero rows, then twiddle W_Ny^(n2 kk).
   // Thread (g, c) owns the rows n2 = g + G i (G = blockDim / CW); the terms run outer and the
   // elements inner, so the loads of all its elements for one term are in flight together.
@@ -712,22 +724,32 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
   }
   if constexpr (STAGE) asm volatile("cp.async.wait_all;" ::: "memory");  // this thread's copies
   __syncthreads();
+  }  // MODE != 2
   // forward stage 2, product, inverse stage A: thread (k1 = g, c)
   if (g < L1) {
     C2<T> u[L2];
+    if constexpr (MODE != 2) {
 #pragma unroll
-    for (int n2 = 0; n2 < L2; n2++) u[n2] = y[(n2 * L1 + g) * CW + c];
-    Dft<T, L2, false>::run(u);
-#pragma unroll
-    for (int k2 = 0; k2 < L2; k2++) {
-      const C2<T> f = STAGE ? fs[(g + L1 * k2) * CW + c] : Fmap[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c];
-      u[k2] = cscale(cmul(f, u[k2]), scale);
+      for (int n2 = 0; n2 < L2; n2++) u[n2] = y[(n2 * L1 + g) * CW + c];
+      Dft<T, L2, false>::run(u);
     }
-    Dft<T, L2, true>::run(u);  // over k2 -> n2
-    // the thread rewrites exactly the entries of y it read above: no other thread's data
+    if constexpr (MODE == 1) {  // the profile's spectrum, frequencies k1 + L1 k2 of row block kk
 #pragma unroll
-    for (int n2 = 0; n2 < L2; n2++) y[(n2 * L1 + g) * CW + c] = n2 == 0 ? u[0] : cmulc(u[n2], wl[g * n2]);
+      for (int k2 = 0; k2 < L2; k2++) ks[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c] = u[k2];
+    } else {
+#pragma unroll
+      for (int k2 = 0; k2 < L2; k2++) {
+        const long e = ((long)kk * N2 + g + L1 * k2) * pitch + col0 + c;
+        const C2<T> f = STAGE ? fs[(g + L1 * k2) * CW + c] : Fmap[e];
+        u[k2] = cscale(cmul(f, MODE == 2 ? ks[e] : u[k2]), scale);
+      }
+      Dft<T, L2, true>::run(u);  // over k2 -> n2
+      // the thread rewrites exactly the entries of y it read above: no other thread's data
+#pragma unroll
+      for (int n2 = 0; n2 < L2; n2++) y[(n2 * L1 + g) * CW + c] = n2 == 0 ? u[0] : cmulc(u[n2], wl[g * n2]);
+    }
   }
+  if constexpr (MODE == 1) return;  // (every thread: no barrier follows)
   __syncthreads();
   // inverse stage B: thread (n2 = g, c) over k1 -> rows n2 + L2 n1
   if (g < L2) {
@@ -932,7 +954,7 @@ void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const d
   const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
   {
     // two-level register kernel where N2 splits into two supported factors
-    using K2 = void (*)(const C2<T>*, C2<T>*, long, const C2<T>*, int, int, int, const C2<T>*, T);
+    using K2 = void (*)(const C2<T>*, C2<T>*, long, const C2<T>*, int, int, int, const C2<T>*, T, C2<T>*);
     K2 k2 = nullptr;
     int nthr = 0;
     // float-float and FP64 at N2 = 100: the map-spectrum tile prefetched into L2, or staged in
@@ -957,7 +979,7 @@ void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const d
         const size_t sm = staged ? smem2s : smem2;
         set_max_smem((const void*)k, sm);
         k<<<dim3(nstrips, p.N1), nthr, sm, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)tmp, p.Wp, (const C2<T>*)kx,
-                                                          h, p.Ny, p.N1, (const C2<T>*)p.twy, scale);
+                                                          h, p.Ny, p.N1, (const C2<T>*)p.twy, scale, nullptr);
       };
       const bool staged = k2s && p1_staged_choice(ctx, p, [&](bool st) {
                             launch(st);
@@ -985,6 +1007,81 @@ void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const d
   MLC_CHECK_LAUNCH();
   launch_colpass<T, true>(ctx, p, tmp, 'A', 0);
   if (!spec_out) launch_rows_c2r<T>(ctx, p, tmp, out);
+}
+
+// P1's register kernel in mode MODE for the plan's N2 (nullptr where there is none): the
+// sizes whose profile spectra are cached (N2 = 100: 2000^2 ... 10000^2; 128: 8192^2 and
+// the other multiples of 128).
+template <typename T, int MODE>
+static auto p1_mode_kernel(int N2, int& nthr) {
+  constexpr int CW = strip_width<T>();
+  using K = void (*)(const C2<T>*, C2<T>*, long, const C2<T>*, int, int, int, const C2<T>*, T, C2<T>*);
+  K k = nullptr;
+  switch (N2) {
+    case 100: k = k_conv_fused2<T, CW, 10, 10, false, MODE>; nthr = 10 * CW; break;
+    case 128: k = k_conv_fused2<T, CW, 8, 16, false, MODE>; nthr = 16 * CW; break;
+    default: break;
+  }
+  return k;
+}
+
+template <typename T>
+bool profile_spectrum_supported_impl(const FftPlan2D& p) {
+  int nthr = 0;
+  return p1_mode_kernel<T, 1>(p.N2, nthr) != nullptr;
+}
+
+// The profile's spectrum as P1 holds it before the product (P0, then P1 up to forward
+// stage 2), in the map spectrum's layout (Ny x Wp) into ks.
+template <typename T>
+void profile_spectrum_impl(mlc_ctx* ctx, const FftPlan2D& p, const double* prof, int pN, void* ks) {
+  constexpr int CW = strip_width<T>();
+  const int h = pN / 2;
+  MLC_REQUIRE(pN % 2 == 0 && 2 * h <= p.Ny && 2 * h <= p.Nx, MLC_ERR_LIMIT, "profile raster larger than the map");
+  int nthr = 0;
+  const auto k = p1_mode_kernel<T, 1>(p.N2, nthr);
+  MLC_REQUIRE(k != nullptr, MLC_ERR_LIMIT, "no cached profile spectra for this map size");
+  void* kx = ws_get(ctx, WS_KX, (size_t)(2 * h > 0 ? 2 * h : 1) * p.Wp * sizeof(C2<T>));
+  launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
+  const size_t smem = ((size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
+  set_max_smem((const void*)k, smem);
+  {
+    MLC_KSCOPE(ctx, "conv_profile_spectrum");
+    k<<<dim3(ceil_div(p.Wc, CW), p.N1), nthr, smem, ctx->stream>>>(nullptr, nullptr, p.Wp, (const C2<T>*)kx, h,
+                                                                     p.Ny, p.N1, (const C2<T>*)p.twy, T(0),
+                                                                     (C2<T>*)ks);
+  }
+  MLC_CHECK_LAUNCH();
+}
+
+// conv_fused_impl up to P2 (the inverse half-spectrum into spec_out) from a profile
+// spectrum made by profile_spectrum_impl: P1 is the product and the inverse stages only.
+// The same operations on the same values as the whole pass, so the same results bit for bit.
+template <typename T>
+void conv_cached_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* spec_out) {
+  constexpr int CW = strip_width<T>();
+  int nthr = 0;
+  const auto k = p1_mode_kernel<T, 2>(p.N2, nthr);
+  MLC_REQUIRE(k != nullptr, MLC_ERR_LIMIT, "no cached profile spectra for this map size");
+  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));
+  const size_t smem = ((size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
+  set_max_smem((const void*)k, smem);
+  {
+    MLC_KSCOPE(ctx, "conv_fused_spectrum");
+    k<<<dim3(ceil_div(p.Wc, CW), p.N1), nthr, smem, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)spec_out, p.Wp,
+                                                                     nullptr, 0, p.Ny, p.N1, (const C2<T>*)p.twy,
+                                                                     scale, (C2<T>*)ks);
+  }
+  MLC_CHECK_LAUNCH();
+  launch_colpass<T, true>(ctx, p, spec_out, 'A', 0);
+}
+
+// The whole cached convolution into real pixels of T (P3 after conv_cached_impl).
+template <typename T>
+void conv_cached_real_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* out) {
+  void* tmp = ws_get(ctx, WS_SPEC_TMP, p.spec_bytes());
+  conv_cached_impl<T>(ctx, p, Fmap, ks, tmp);
+  launch_rows_c2r<T>(ctx, p, tmp, out);
 }
 
 template <typename T>

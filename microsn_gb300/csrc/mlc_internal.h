@@ -95,6 +95,9 @@ struct mlc_ctx {
   // launch autotuner: key -> choice (-1: FFT form; >= 0: direct tile shape), candidate timings
   bool autotune = true;
   bool two_chains = false;  // set while the batched step runs two convolution chains side by side
+  // device bytes the cached profile spectra of the step and of mlc_convolve_many may take:
+  // -1 a quarter of the device memory, 0 none (every call recomputes them)
+  long long profile_cache_bytes = -1;
   std::map<std::string, int> tune;
   std::map<std::string, std::string> tune_log;
   std::map<std::string, std::string> tune_name;  // the choice as the report prints it
@@ -196,6 +199,14 @@ std::string autotune_report(mlc_ctx* ctx);
 // stages the map-spectrum tile in shared memory.  The autotuner times run(false) and
 // run(true) once per key; a pinned or earlier choice is reused.
 bool p1_staged_choice(mlc_ctx* ctx, const FftPlan2D& p, const std::function<void(bool)>& run);
+// Cached profile spectra: the profile's spectrum as the fused convolution's P1 holds it
+// before the product with the map spectrum (Ny x Wp complex of the plan's arithmetic, the
+// map spectrum's layout), and conv_fused_spectrum starting from it.  Supported where P1 has
+// its register form for N2 = 100 or 128.
+bool profile_spectrum_supported(const FftPlan2D& p);
+void profile_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const double* prof, int pN, void* ks);
+void conv_cached_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* spec_out);
+void conv_cached(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* out);
 // conv_fused up to P2: the inverse half-spectrum (Ny x Wp complex) into spec_out.
 void conv_fused_spectrum(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN,
                          void* spec_out, int kx_slot = WS_KX);
@@ -216,6 +227,14 @@ void forward_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* in, int in_dtype
 template <typename T>
 void conv_fused_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out,
                      void* spec_out = nullptr, int kx_slot = WS_KX);
+template <typename T>
+bool profile_spectrum_supported_impl(const FftPlan2D& p);
+template <typename T>
+void profile_spectrum_impl(mlc_ctx* ctx, const FftPlan2D& p, const double* prof, int pN, void* ks);
+template <typename T>
+void conv_cached_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* spec_out);
+template <typename T>
+void conv_cached_real_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const void* ks, void* out);
 template <typename T>
 void conv_plain_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const double* prof, int pN, void* out);
 template <typename T, typename TO = typename RealOut<T>::type>

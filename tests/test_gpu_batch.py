@@ -281,3 +281,37 @@ def test_step_as_cuda_graph_equals_eager(bctx, prec, fft, nprof):
     with pytest.raises(mlc.MlcError):
         mlc.convolve_sample_tracks(bctx, m, profs, {k: a.cpu().numpy() for k, a in trd.items()}, graph=True)
     m.close()
+
+
+@pytest.mark.parametrize("prec,fft", [("f32", "native"), ("f32", "f32x2"), ("f64", "native")])
+def test_profile_spectrum_cache_equals_recomputed(lib_built, prec, fft):
+    """At 2000^2 (column split with N2 = 100) the step and convolve_many keep the profiles'
+    spectra between calls and start P1 from them: the same light curves and maps, bit for bit,
+    as a context that transforms every profile on every call -- also after the profile values
+    change (same raster sizes), which must recompute the cached spectra."""
+    import microsn_gb300 as mlc
+    N = 2000
+    dt = np.float32 if prec == "f32" else np.float64
+    mp = synth.lognormal_map(N, seed=61).astype(dt)
+    trh = _host_tracks(600, N, 62, dt)
+    profs = _profiles(10)
+    profs2 = list(profs)
+    profs2[1] = mlc.profile("exponential", 3.1, 1.0, ref_compat=False)  # same raster size as profs[1]
+    assert mlc.profile_raster(profs2[1]).shape == mlc.profile_raster(profs[1]).shape
+    outs = {}
+    for cache in (-1, 0):
+        c = mlc.Context(0)
+        c.set_autotune(False)
+        c.set_profile_cache(cache)
+        m = mlc.Map(c, mp, prec)
+        if fft != "native":
+            m.set_fft(fft)
+        trd = {k: torch.as_tensor(a, device=DEV) for k, a in trh.items()}
+        r = [mlc.convolve_sample_tracks(c, m, p, trd, mag=True).cpu() for p in (profs, profs, profs2, profs)]
+        r.append(mlc.convolve_many(c, m, profs2[:4]).cpu())
+        outs[cache] = r
+        m.close()
+        c.close()
+    for a, b in zip(outs[-1], outs[0]):
+        assert torch.equal(a, b)
+    assert not torch.equal(outs[0][1], outs[0][2])  # the changed profile changed the curves
