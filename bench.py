@@ -73,6 +73,8 @@ def parse():
                     help="transform arithmetic of the step's FP32 map (profiling cases only)")
     ap.add_argument("--tune", action="append", default=[], metavar="KEY=CHOICE",
                     help="pin an autotuner choice (mlc_ctx_tune_set), e.g. 'conv P1 f32x2->f32 10000x10000=1'")
+    ap.add_argument("--no-profile-cache", action="store_true",
+                    help="recompute every profile spectrum in every call (profiling cases only)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="FFT form for every profile (for ncu captures, under which the autotuner's first-call "
                          "timings are distorted)")
@@ -1130,6 +1132,8 @@ def kernel_case(args):
     for kv in args.tune:
         key, _, val = kv.rpartition("=")
         ctx.tune_set(key, int(val))
+    if args.no_profile_cache:
+        ctx.set_profile_cache(0)
     args.no_cpu = True
     case = args.kernel_case
     res = {"kernel_case": case}
@@ -1315,6 +1319,23 @@ def main():
     kernels = {k: {"ms_per_step": v, "launches_per_step": kt[k][1] / ksteps,
                    "GB_per_s": (algorithmic_bytes(k, n, E, len(profs), es=spec_es) / (kt[k][0] / kt[k][1] / 1000.0) / 1e9)
                    if algorithmic_bytes(k, n, E, len(profs), es=spec_es) else None} for k, v in per_step.items()}
+
+    # ---- the same step with the profile spectra recomputed in every call (cache off)
+    ctx.set_profile_cache(0)
+    step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ctx.set_profile_cache(-1)
+    step()  # the cache refilled before the timings below
+    torch.cuda.synchronize()
+    profile_cache = {"ms_per_step": ms_step, "ms_per_step_recomputed": e0.elapsed_time(e1) / args.steps,
+                     "what": "the timed step keeps the 16 profiles' spectra between calls (the profile list and map "
+                             "size repeat; the map's own spectrum is recomputed every step); recomputed: the same "
+                             "step transforming every profile in every call"}
 
     # ---- the same step as one CUDA graph (captured on its first graph call, then replayed)
     def graph_step():
@@ -1530,7 +1551,7 @@ def main():
                         "track positions" if HEADLINE_FFT == "f32x2" else "FP32 transforms"),
                "max_rel_err_vs_fp64": accuracy["max_rel_chi2"] if accuracy else None,
                "accuracy_vs_fp64": accuracy,
-               "plain_fp64": plain, "kernels": kernels, "cuda_graph": cuda_graph,
+               "plain_fp64": plain, "kernels": kernels, "cuda_graph": cuda_graph, "profile_cache": profile_cache,
                "sampling_stage": ({"value": world * lc_per_step / (kernels["sample_tracks_il"]["ms_per_step"] / 1000.0),
                                    "unit": UNIT, "ms_per_step": kernels["sample_tracks_il"]["ms_per_step"]}
                                   if "sample_tracks_il" in kernels else None),
