@@ -902,6 +902,7 @@ def algorithmic_bytes(name, n, E, nprof, e=4, es=None):
         "fft_col_A": 2 * spec,                 # in-place column sub-pass: read + write
         "fft_col_B": 2 * spec,
         "conv_fused_spectrum": 2 * spec,       # read map spectrum, write product sub-pass output
+        "conv_cached_spectrum": 3 * spec,      # read map and cached profile spectra, write the product pass
         "sample_tracks": E * e + nprof * real + E * nprof * e,  # t in, one read of each map, LCs out
         "sample_tracks_il": E * e + nprof * real + E * nprof * e,
         "interleave": 2 * nprof * real,          # read nprof planar maps, write the interleaved map

@@ -1067,7 +1067,7 @@ void conv_cached_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* Fmap, const 
   const size_t smem = ((size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
   set_max_smem((const void*)k, smem);
   {
-    MLC_KSCOPE(ctx, "conv_fused_spectrum");
+    MLC_KSCOPE(ctx, "conv_cached_spectrum");
     k<<<dim3(ceil_div(p.Wc, CW), p.N1), nthr, smem, ctx->stream>>>((const C2<T>*)Fmap, (C2<T>*)spec_out, p.Wp,
                                                                      nullptr, 0, p.Ny, p.N1, (const C2<T>*)p.twy,
                                                                      scale, (C2<T>*)ks);

@@ -296,7 +296,7 @@ def test_profile_spectrum_cache_equals_recomputed(lib_built, prec, fft):
     trh = _host_tracks(600, N, 62, dt)
     profs = _profiles(10)
     profs2 = list(profs)
-    profs2[1] = mlc.profile("exponential", 3.1, 1.0, ref_compat=False)  # same raster size as profs[1]
+    profs2[1] = mlc.profile("exponential", 1.4, 1.0, ref_compat=False)  # same raster size as profs[1]
     assert mlc.profile_raster(profs2[1]).shape == mlc.profile_raster(profs[1]).shape
     outs = {}
     for cache in (-1, 0):
