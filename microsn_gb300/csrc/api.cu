@@ -564,7 +564,7 @@ int mlc_sample_tracks_interleaved(mlc_ctx* ctx, const void* imap, int stride, in
       MLC_CUDA(cudaStreamSynchronize(ctx->stream));
     }
     sample_tracks_il(ctx, imap, stride, nmaps, Nx, Ny, precision, ntracks, x0, y0, phi, v, off, t, mag, out, (long)E,
-                     0);
+                     0, E);
   });
 }
 

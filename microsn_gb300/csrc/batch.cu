@@ -456,7 +456,7 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
     }
     if (!host) {
       sample_tracks_il(ctx, imap, stride, nm, Nx, Ny, map->prec, ntr, x0, y0, phi, v, off, t, mag,
-                       (char*)out + (size_t)g0 * E * es, (long)E, 0);
+                       (char*)out + (size_t)g0 * E * es, (long)E, 0, E);
       continue;
     }
     if (!tracks_ready) {
@@ -470,7 +470,7 @@ static void run(mlc_ctx* ctx, mlc_map* map, const void* pixels, int nprof, const
       const int s = b->ring_pos++ % b->nring;
       MLC_CUDA(cudaStreamWaitEvent(ctx->stream, b->ring_free[s], 0));
       sample_tracks_il(ctx, imap, stride, nm, Nx, Ny, map->prec, t1 - t0, x0 + t0 * es, y0 + t0 * es,
-                       phi + t0 * es, v + t0 * es, doff + t0, t, mag, b->ring[s], (long)Ec, e0);
+                       phi + t0 * es, v + t0 * es, doff + t0, t, mag, b->ring[s], (long)Ec, e0, Ec);
       MLC_CUDA(cudaEventRecord(b->ring_full[s], ctx->stream));
       MLC_CUDA(cudaStreamWaitEvent(b->d2h, b->ring_full[s], 0));
       char* dst = (char*)out + ((size_t)g0 * E + e0) * es;

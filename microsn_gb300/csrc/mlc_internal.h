@@ -54,6 +54,7 @@ enum WsSlot {
   WS_PAIR_CAND,  // pair-stage candidates, refinement list, counters, histogram
   WS_BATCH_MAPS,  // convolved maps of one profile group (mlc_convolve_sample_tracks)
   WS_BATCH_IMAP,  // their profile-interleaved copy
+  WS_SAMPLE_ORDER,  // the sampler's epoch chunks in map-cell order
   WS_NSLOTS
 };
 
@@ -274,9 +275,10 @@ void interleave_into(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long
                      void* out);
 // Interleaved-map track sampler: out[q * E + (e - ebase)] for the epochs e of the given
 // tracks (off holds global epoch indices; ebase lets a chunk of tracks fill its own buffer).
+// nep: at least off[ntracks] - off[0] (the epochs of these tracks).
 void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
                       const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
-                      const void* t, int mag, void* out, long E, int64_t ebase);
+                      const void* t, int mag, void* out, long E, int64_t ebase, int64_t nep);
 // Fused sample -> magnitude -> offset-minimised chi2 against one curve on shared epochs.
 void track_chi2_offset(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
                        const void* x0, const void* y0, const void* phi, const void* v, int Tn, const void* t,

@@ -8,6 +8,7 @@
 #include <algorithm>
 
 #include "mlc_internal.h"
+#include "scan.cuh"
 
 namespace mlc {
 
@@ -276,12 +277,147 @@ void interleave_into(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long
   interleave_impl(ctx, maps_host, nmaps, nmaps, S, off, npix, prec, out);
 }
 
+// ---- cell order: chunks of 32 consecutive epochs sampled in the order of the map cell
+// they start in.  Taking whole tracks in index order, the warps in flight at one moment
+// gather from all over the map, and a map much larger than L2 is read about twice over;
+// chunks of a few days' motion sorted by 128 x 128-pixel cell keep the gathers of the
+// warps in flight within a few cells, so each pixel comes from DRAM about once.  Every
+// epoch is computed as in k_sample_tracks_il (the same geometry and arithmetic per lane),
+// so the light curves are the same bit for bit; only the order of the work changes.
+constexpr int CHUNK_EPOCHS = 32;
+constexpr int CHUNK_CELL = 128;
+
+// first[c]: the track holding the chunk's first epoch (off[0] + 32 c).
+__global__ void k_il_chunk_tracks(const int64_t* __restrict__ off, int ntracks, int* __restrict__ first) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ntracks; r += gridDim.x * blockDim.x) {
+    const int64_t b = off[0], a0 = off[r] - b, a1 = off[r + 1] - b;
+    for (int64_t c = (a0 + CHUNK_EPOCHS - 1) / CHUNK_EPOCHS; c * CHUNK_EPOCHS < a1; c++) first[c] = r;
+  }
+}
+
+// The cell of each chunk's first epoch (clamped to the map), and the per-cell counts.
+template <typename T>
+__global__ void k_il_chunk_cells(const T* __restrict__ x0, const T* __restrict__ y0, const T* __restrict__ phi,
+                                 const T* __restrict__ v, const int64_t* __restrict__ off,
+                                 const T* __restrict__ t, const int* __restrict__ first, int ntracks, long nchunks,
+                                 int Nx, int Ny, int ncx, int ncy, uint32_t* __restrict__ cell,
+                                 uint32_t* __restrict__ count) {
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < nchunks; c += (long)gridDim.x * blockDim.x) {
+    const int64_t e = off[0] + c * CHUNK_EPOCHS;
+    if (e >= off[ntracks]) {  // past the tracks' epochs (nep above their count): an empty chunk
+      cell[c] = 0;
+      atomicAdd(count, 1u);
+      continue;
+    }
+    const int r = first[c];
+    const Bilin<T> B = TrackGeom<T>(x0[r], y0[r], phi[r], v[r]).at(t[e], Nx, Ny);
+    const int cx = min(max(B.jl, 0) / CHUNK_CELL, ncx - 1), cy = min(max(B.il, 0) / CHUNK_CELL, ncy - 1);
+    const uint32_t k = (uint32_t)(cy * ncx + cx);
+    cell[c] = k;
+    atomicAdd(count + k, 1u);
+  }
+}
+
+// Exclusive prefix sum of the cell counts (one CTA), then the write cursors of the cells.
+__global__ void __launch_bounds__(1024) k_il_cell_scan(uint32_t* __restrict__ count, int ncells) {
+  __shared__ uint32_t wsum[32];
+  uint32_t running = 0;
+  for (int c0 = 0; c0 < ncells; c0 += blockDim.x) {
+    const int c = c0 + threadIdx.x;
+    const uint32_t v = c < ncells ? count[c] : 0u;
+    uint32_t agg;
+    const uint32_t ex = block_exclusive_sum(v, &agg, wsum);
+    if (c < ncells) count[c] = running + ex;
+    running += agg;
+    __syncthreads();  // wsum is rewritten by the next round
+  }
+}
+
+__global__ void k_il_cell_scatter(const uint32_t* __restrict__ cell, long nchunks, uint32_t* __restrict__ cursor,
+                                  uint32_t* __restrict__ order) {
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < nchunks; c += (long)gridDim.x * blockDim.x)
+    order[atomicAdd(cursor + cell[c], 1u)] = (uint32_t)c;
+}
+
+// One warp per chunk, in cell order: lane l samples epoch off[0] + 32 c + l of whichever
+// track holds it (a chunk spans at most a few tracks: the first, then forward by offsets).
+template <typename T, int NM>
+__global__ void __launch_bounds__(256) k_sample_chunks_il(const T* __restrict__ imap, int Nx, int Ny, int ntracks,
+                                                          const T* __restrict__ x0, const T* __restrict__ y0,
+                                                          const T* __restrict__ phi, const T* __restrict__ v,
+                                                          const int64_t* __restrict__ off, const T* __restrict__ t,
+                                                          const int* __restrict__ first,
+                                                          const uint32_t* __restrict__ order, long nchunks, int mag,
+                                                          T* __restrict__ out, long E, int nm_out, int64_t ebase) {
+  const int lane = threadIdx.x & 31;
+  const long j = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= nchunks) return;
+  const long c = order[j];
+  const int64_t e = off[0] + c * CHUNK_EPOCHS + lane;
+  if (e >= off[ntracks]) return;
+  int r = first[c];
+  while (off[r + 1] <= e) r++;
+  const TrackGeom<T> g(x0[r], y0[r], phi[r], v[r]);
+  sample_epoch<T, NM>(imap, Nx, g.at(t[e], Nx, Ny), mag, out, E, nm_out, e - ebase);
+}
+
+// The sampler's order for these sizes: cell order where the interleaved map is larger than
+// L2 and there are enough epochs to cover it, track order otherwise; a pinned
+// "sample_tracks_il cell-order" tune key (0 or 1) decides instead.
+static bool il_cell_order(mlc_ctx* ctx, long npix, int stride, size_t es, int64_t nep) {
+  auto it = ctx->tune.find("sample_tracks_il cell-order");
+  if (it != ctx->tune.end()) return it->second != 0;
+  return (double)npix * stride * es > 256e6 && nep >= 4 * npix / (CHUNK_CELL * CHUNK_CELL) * CHUNK_EPOCHS;
+}
+
 template <typename T>
 static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int ntracks,
                            const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
-                           const void* t, int mag, void* out, long E, int64_t ebase) {
+                           const void* t, int mag, void* out, long E, int64_t ebase, int64_t nep) {
+  if (nep > 0 && il_cell_order(ctx, (long)Nx * Ny, stride, sizeof(T), nep)) {
+    const long nchunks = (long)((nep + CHUNK_EPOCHS - 1) / CHUNK_EPOCHS);
+    const int ncx = ceil_div(Nx, CHUNK_CELL), ncy = ceil_div(Ny, CHUNK_CELL), ncells = ncx * ncy;
+    MLC_REQUIRE(nchunks < (1L << 32), MLC_ERR_LIMIT, "more than 2^37 epochs in one sampling call");
+    char* ws = (char*)ws_get(ctx, WS_SAMPLE_ORDER, (size_t)nchunks * 12 + (size_t)ncells * 4 + 256);
+    int* first = (int*)ws;
+    uint32_t* cell = (uint32_t*)(first + nchunks);
+    uint32_t* order = cell + nchunks;
+    uint32_t* count = order + nchunks;
+    MLC_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t) * ncells, ctx->stream));
+    const int g = std::max(1, std::min(ctx->sm_count * 8, (int)((nchunks + 255) / 256)));
+    {
+      MLC_KSCOPE(ctx, "sample_cell_order");
+      k_il_chunk_tracks<<<std::max(1, std::min(ctx->sm_count * 8, ceil_div(ntracks, 256))), 256, 0, ctx->stream>>>(
+          off, ntracks, first);
+      k_il_chunk_cells<T><<<g, 256, 0, ctx->stream>>>((const T*)x0, (const T*)y0, (const T*)phi, (const T*)v, off,
+                                                       (const T*)t, first, ntracks, nchunks, Nx, Ny, ncx, ncy, cell,
+                                                       count);
+      k_il_cell_scan<<<1, 1024, 0, ctx->stream>>>(count, ncells);
+      k_il_cell_scatter<<<g, 256, 0, ctx->stream>>>(cell, nchunks, count, order);
+    }
+    MLC_CHECK_LAUNCH();
+    const long grid = (nchunks + 7) / 8;
+    MLC_REQUIRE(grid <= 0x7fffffffL, MLC_ERR_LIMIT, "too many epochs in one sampling call");
+#define MLC_CH_LAUNCH(NMV)                                                                                          \
+  k_sample_chunks_il<T, NMV><<<(unsigned)grid, 256, 0, ctx->stream>>>(                                              \
+      (const T*)imap, Nx, Ny, ntracks, (const T*)x0, (const T*)y0, (const T*)phi, (const T*)v, off, (const T*)t,   \
+      first, order, nchunks, mag, (T*)out, E, nmaps, ebase)
+    MLC_KSCOPE(ctx, "sample_tracks_il");
+    switch (stride) {
+      case 1: MLC_CH_LAUNCH(1); break;
+      case 2: MLC_CH_LAUNCH(2); break;
+      case 4: MLC_CH_LAUNCH(4); break;
+      case 8: MLC_CH_LAUNCH(8); break;
+      default: MLC_CH_LAUNCH(16); break;
+    }
+#undef MLC_CH_LAUNCH
+    return;
+  }
   const int grid = ceil_div(ntracks, 8);
-#define MLC_IL_LAUNCH(NMV)                                                                                    k_sample_tracks_il<T, NMV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, Nx, Ny, ntracks, (const T*)x0,                                                              (const T*)y0, (const T*)phi, (const T*)v, off,                                                              (const T*)t, mag, (T*)out, E, nmaps, ebase)
+#define MLC_IL_LAUNCH(NMV)                                                                                    \
+  k_sample_tracks_il<T, NMV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, Nx, Ny, ntracks, (const T*)x0,  \
+                                                              (const T*)y0, (const T*)phi, (const T*)v, off, \
+                                                              (const T*)t, mag, (T*)out, E, nmaps, ebase)
   MLC_KSCOPE(ctx, "sample_tracks_il");
   switch (stride) {
     case 1: MLC_IL_LAUNCH(1); break;
@@ -295,12 +431,14 @@ static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps
 
 void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
                       const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
-                      const void* t, int mag, void* out, long E, int64_t ebase) {
+                      const void* t, int mag, void* out, long E, int64_t ebase, int64_t nep) {
   if (ntracks <= 0) return;
   if (prec == MLC_F64)
-    sample_il_impl<double>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E, ebase);
+    sample_il_impl<double>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E, ebase,
+                           nep);
   else
-    sample_il_impl<float>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E, ebase);
+    sample_il_impl<float>(ctx, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E, ebase,
+                          nep);
   MLC_CHECK_LAUNCH();
 }
 

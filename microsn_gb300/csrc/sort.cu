@@ -14,6 +14,7 @@
 #include <unordered_map>
 
 #include "mlc_internal.h"
+#include "scan.cuh"
 
 namespace mlc {
 
@@ -56,34 +57,6 @@ __global__ void __launch_bounds__(SORT_THREADS) k_digit_hist(const uint64_t* __r
 // Exclusive scan, in digit-major order, of hist[pass] (256 x ntiles) -> offsets (same
 // layout).  One CTA per digit scans that digit's tiles, starting from the digit's
 // global base (the count of all keys with a smaller digit, from the host).
-// Exclusive prefix sum of v over the CTA's threads in thread order, and the CTA's total in
-// *agg: an inclusive scan within each warp (shuffles), the warps' totals scanned by warp 0
-// in shared memory, each thread's warp offset added.  blockDim.x a multiple of 32, <= 1024;
-// every thread of the CTA calls it (two barriers inside).
-__device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t v, uint32_t* agg, uint32_t* wsum) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  uint32_t x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) wsum[warp] = x;
-  __syncthreads();
-  if (warp == 0) {
-    uint32_t w = lane < nwarps ? wsum[lane] : 0u;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    wsum[lane] = w;  // inclusive totals of warps 0..lane
-  }
-  __syncthreads();
-  *agg = wsum[nwarps - 1];
-  return (warp ? wsum[warp - 1] : 0u) + x - v;
-}
-
 __global__ void __launch_bounds__(1024) k_scan_digit(const uint32_t* __restrict__ hist, int ntiles,
                                                      const uint32_t* __restrict__ digit_base,
                                                      uint32_t* __restrict__ offs) {

@@ -315,3 +315,33 @@ def test_profile_spectrum_cache_equals_recomputed(lib_built, prec, fft):
     for a, b in zip(outs[-1], outs[0]):
         assert torch.equal(a, b)
     assert not torch.equal(outs[0][1], outs[0][2])  # the changed profile changed the curves
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_sampler_cell_order_equals_track_order(lib_built, prec):
+    """The interleaved sampler in map-cell order (epoch chunks of 32 sorted by the 128-pixel
+    cell they start in; chosen for maps much larger than L2) against the track order, both
+    pinned: the same light curves bit for bit, through the device-buffer step and through
+    the host-buffer step, whose chunks of tracks start at nonzero epoch offsets."""
+    import microsn_gb300 as mlc
+    N = 2000
+    dt = np.float32 if prec == "f32" else np.float64
+    mp = synth.lognormal_map(N, seed=71).astype(dt)
+    trh = _host_tracks(3000, N, 72, dt, epochs=(5, 90))
+    profs = _profiles(5)
+    outs = {}
+    for order in (0, 1):
+        c = mlc.Context(0)
+        c.set_autotune(False)
+        c.tune_set("sample_tracks_il cell-order", order)
+        m = mlc.Map(c, mp, prec)
+        dev = mlc.convolve_sample_tracks(c, m, profs, {k: torch.as_tensor(a, device=DEV) for k, a in trh.items()},
+                                         mag=True).cpu()
+        c.set_chunk_bytes(64 * 1024)  # many chunks of tracks
+        host = mlc.convolve_sample_tracks(c, m, profs, _pinned(trh), mag=True).clone()
+        outs[order] = (dev, host)
+        m.close()
+        c.close()
+    assert torch.equal(outs[0][0], outs[1][0])
+    assert torch.equal(outs[0][1], outs[1][1])
+    assert torch.equal(outs[1][0], outs[1][1])
