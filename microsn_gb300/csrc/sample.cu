@@ -287,6 +287,15 @@ void interleave_into(mlc_ctx* ctx, const void* const* maps_host, int nmaps, long
 constexpr int CHUNK_EPOCHS = 32;
 constexpr int CHUNK_CELL = 128;
 
+// Each track's geometry (TrackGeom: pixel base, offsets, V cos phi, V sin phi), formed once
+// per call: a chunk's lanes load it instead of evaluating sin and cos per epoch.
+template <typename T>
+__global__ void k_il_track_geom(const T* __restrict__ x0, const T* __restrict__ y0, const T* __restrict__ phi,
+                                const T* __restrict__ v, int ntracks, TrackGeom<T>* __restrict__ geom) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ntracks; r += gridDim.x * blockDim.x)
+    geom[r] = TrackGeom<T>(x0[r], y0[r], phi[r], v[r]);
+}
+
 // first[c]: the track holding the chunk's first epoch (off[0] + 32 c).
 __global__ void k_il_chunk_tracks(const int64_t* __restrict__ off, int ntracks, int* __restrict__ first) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < ntracks; r += gridDim.x * blockDim.x) {
@@ -297,8 +306,7 @@ __global__ void k_il_chunk_tracks(const int64_t* __restrict__ off, int ntracks, 
 
 // The cell of each chunk's first epoch (clamped to the map), and the per-cell counts.
 template <typename T>
-__global__ void k_il_chunk_cells(const T* __restrict__ x0, const T* __restrict__ y0, const T* __restrict__ phi,
-                                 const T* __restrict__ v, const int64_t* __restrict__ off,
+__global__ void k_il_chunk_cells(const TrackGeom<T>* __restrict__ geom, const int64_t* __restrict__ off,
                                  const T* __restrict__ t, const int* __restrict__ first, int ntracks, long nchunks,
                                  int Nx, int Ny, int ncx, int ncy, uint32_t* __restrict__ cell,
                                  uint32_t* __restrict__ count) {
@@ -309,8 +317,7 @@ __global__ void k_il_chunk_cells(const T* __restrict__ x0, const T* __restrict__
       atomicAdd(count, 1u);
       continue;
     }
-    const int r = first[c];
-    const Bilin<T> B = TrackGeom<T>(x0[r], y0[r], phi[r], v[r]).at(t[e], Nx, Ny);
+    const Bilin<T> B = geom[first[c]].at(t[e], Nx, Ny);
     const int cx = min(max(B.jl, 0) / CHUNK_CELL, ncx - 1), cy = min(max(B.il, 0) / CHUNK_CELL, ncy - 1);
     const uint32_t k = (uint32_t)(cy * ncx + cx);
     cell[c] = k;
@@ -343,8 +350,7 @@ __global__ void k_il_cell_scatter(const uint32_t* __restrict__ cell, long nchunk
 // track holds it (a chunk spans at most a few tracks: the first, then forward by offsets).
 template <typename T, int NM>
 __global__ void __launch_bounds__(256) k_sample_chunks_il(const T* __restrict__ imap, int Nx, int Ny, int ntracks,
-                                                          const T* __restrict__ x0, const T* __restrict__ y0,
-                                                          const T* __restrict__ phi, const T* __restrict__ v,
+                                                          const TrackGeom<T>* __restrict__ geom,
                                                           const int64_t* __restrict__ off, const T* __restrict__ t,
                                                           const int* __restrict__ first,
                                                           const uint32_t* __restrict__ order, long nchunks, int mag,
@@ -357,7 +363,7 @@ __global__ void __launch_bounds__(256) k_sample_chunks_il(const T* __restrict__ 
   if (e >= off[ntracks]) return;
   int r = first[c];
   while (off[r + 1] <= e) r++;
-  const TrackGeom<T> g(x0[r], y0[r], phi[r], v[r]);
+  const TrackGeom<T> g = geom[r];
   sample_epoch<T, NM>(imap, Nx, g.at(t[e], Nx, Ny), mag, out, E, nm_out, e - ebase);
 }
 
@@ -378,8 +384,10 @@ static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps
     const long nchunks = (long)((nep + CHUNK_EPOCHS - 1) / CHUNK_EPOCHS);
     const int ncx = ceil_div(Nx, CHUNK_CELL), ncy = ceil_div(Ny, CHUNK_CELL), ncells = ncx * ncy;
     MLC_REQUIRE(nchunks < (1L << 32), MLC_ERR_LIMIT, "more than 2^37 epochs in one sampling call");
-    char* ws = (char*)ws_get(ctx, WS_SAMPLE_ORDER, (size_t)nchunks * 12 + (size_t)ncells * 4 + 256);
-    int* first = (int*)ws;
+    const size_t gbytes = ((size_t)ntracks * sizeof(TrackGeom<T>) + 255) & ~(size_t)255;
+    char* ws = (char*)ws_get(ctx, WS_SAMPLE_ORDER, gbytes + (size_t)nchunks * 12 + (size_t)ncells * 4 + 256);
+    TrackGeom<T>* geom = (TrackGeom<T>*)ws;
+    int* first = (int*)(ws + gbytes);
     uint32_t* cell = (uint32_t*)(first + nchunks);
     uint32_t* order = cell + nchunks;
     uint32_t* count = order + nchunks;
@@ -387,11 +395,12 @@ static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps
     const int g = std::max(1, std::min(ctx->sm_count * 8, (int)((nchunks + 255) / 256)));
     {
       MLC_KSCOPE(ctx, "sample_cell_order");
-      k_il_chunk_tracks<<<std::max(1, std::min(ctx->sm_count * 8, ceil_div(ntracks, 256))), 256, 0, ctx->stream>>>(
-          off, ntracks, first);
-      k_il_chunk_cells<T><<<g, 256, 0, ctx->stream>>>((const T*)x0, (const T*)y0, (const T*)phi, (const T*)v, off,
-                                                       (const T*)t, first, ntracks, nchunks, Nx, Ny, ncx, ncy, cell,
-                                                       count);
+      const int gt = std::max(1, std::min(ctx->sm_count * 8, ceil_div(ntracks, 256)));
+      k_il_track_geom<T><<<gt, 256, 0, ctx->stream>>>((const T*)x0, (const T*)y0, (const T*)phi, (const T*)v, ntracks,
+                                                      geom);
+      k_il_chunk_tracks<<<gt, 256, 0, ctx->stream>>>(off, ntracks, first);
+      k_il_chunk_cells<T><<<g, 256, 0, ctx->stream>>>(geom, off, (const T*)t, first, ntracks, nchunks, Nx, Ny, ncx,
+                                                       ncy, cell, count);
       k_il_cell_scan<<<1, 1024, 0, ctx->stream>>>(count, ncells);
       k_il_cell_scatter<<<g, 256, 0, ctx->stream>>>(cell, nchunks, count, order);
     }
@@ -400,8 +409,7 @@ static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps
     MLC_REQUIRE(grid <= 0x7fffffffL, MLC_ERR_LIMIT, "too many epochs in one sampling call");
 #define MLC_CH_LAUNCH(NMV)                                                                                          \
   k_sample_chunks_il<T, NMV><<<(unsigned)grid, 256, 0, ctx->stream>>>(                                              \
-      (const T*)imap, Nx, Ny, ntracks, (const T*)x0, (const T*)y0, (const T*)phi, (const T*)v, off, (const T*)t,   \
-      first, order, nchunks, mag, (T*)out, E, nmaps, ebase)
+      (const T*)imap, Nx, Ny, ntracks, geom, off, (const T*)t, first, order, nchunks, mag, (T*)out, E, nmaps, ebase)
     MLC_KSCOPE(ctx, "sample_tracks_il");
     switch (stride) {
       case 1: MLC_CH_LAUNCH(1); break;
