@@ -321,12 +321,10 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
 // items, waits, and writes them in natural order: output r of item
 // it = 125 k1 + 25 a + 5 b + c is z[k1 + 8 (a + 5 (b + 5 (c + 5 r)))] = z[n0 + 1000 r].  512 threads, two
 // CTAs (32 warps) per SM, the same number of barriers as the three-level form.
-template <typename T, int JP, int ROWS = 1>
-__device__ __forceinline__ void c2r5_level(C2<T>* s0, const C2<T>* w) {
+template <typename T, int JP>
+__device__ __forceinline__ void c2r5_level(C2<T>* s, const C2<T>* w) {
   constexpr int SP = JP / 5, WS = 625 / JP, NB = 5000 / JP;
-  for (int it2 = threadIdx.x; it2 < 1000 * ROWS; it2 += blockDim.x) {
-    const int row = ROWS == 1 ? 0 : it2 / 1000, it = it2 - 1000 * row;  // rows ROWS of 5000 apart
-    C2<T>* s = s0 + 5000 * row;
+  for (int it = threadIdx.x; it < 1000; it += blockDim.x) {
     // Item (blk, m) reads and writes s[blk JP + m + r SP], r < 5.  With runs of SP >= 32 the
     // warp's 32 consecutive m are 32 consecutive elements; shorter runs (JP = 125, 25) would
     // put a warp over blocks JP apart in a few banks (a 5-way conflict at JP = 25), so there
@@ -352,17 +350,13 @@ __device__ __forceinline__ void c2r5_level(C2<T>* s0, const C2<T>* w) {
   __syncthreads();
 }
 
-template <typename T, int ROWS = 1>
-__device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a0, const C2<T>* __restrict__ a1,
-                                         const C2<T>* __restrict__ twx, C2<T>* s0) {
+template <typename T>
+__device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a, const C2<T>* __restrict__ twx, C2<T>* s) {
   constexpr int M = 5000, J = 625;
-  C2<T>* w = s0 + ROWS * M;  // W_625^e = W_Nx^(16 e), e < 625
+  C2<T>* w = s + M;  // W_625^e = W_Nx^(16 e), e < 625
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < J; e += nt) w[e] = ldc(twx + 16L * e);
-  for (int j2 = tid; j2 < J * ROWS; j2 += nt) {
-    const int row = ROWS == 1 ? 0 : j2 / J, j = j2 - J * row;
-    const C2<T>* a = row == 0 ? a0 : a1;
-    C2<T>* s = s0 + M * row;
+  for (int j = tid; j < J; j += nt) {
     C2<T> v[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
@@ -378,46 +372,38 @@ __device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a0, const C2<
     for (int n1 = 1; n1 < 8; n1++) s[n1 * J + j] = cmulc(v[n1], ldc(twx + 2L * j * n1));  // W_M^-(j n1)
   }
   __syncthreads();
-  c2r5_level<T, 625, ROWS>(s0, w);
-  c2r5_level<T, 125, ROWS>(s0, w);
-  c2r5_level<T, 25, ROWS>(s0, w);
+  c2r5_level<T, 625>(s, w);
+  c2r5_level<T, 125>(s, w);
+  c2r5_level<T, 25>(s, w);
   // blocks of 5: every item read (two per thread at most: blockDim >= 500), then written
   // in natural order.  Thread t takes the item whose outputs land at n0 = t (and t + nt),
   // n0 + 1000 r: consecutive threads write consecutive slots (taking items in their own
-  // order instead put a warp's writes 200 slots apart, all in one shared-memory bank).
-  // Row after row (two items of a row per thread at a time).
+  // order instead put a warp's writes 200 slots apart, all in one shared-memory bank)
+  C2<T> u[2][5];
 #pragma unroll
-  for (int row = 0; row < ROWS; row++) {
-    C2<T>* s = s0 + M * row;
-    C2<T> u[2][5];
+  for (int h = 0; h < 2; h++) {
+    const int n0 = tid + h * nt;
+    if (n0 < 1000) {
+      const int it = 125 * (n0 % 8) + 25 * ((n0 / 8) % 5) + 5 * ((n0 / 40) % 5) + n0 / 200;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int n0 = tid + h * nt;
-      if (n0 < 1000) {
-        const int it = 125 * (n0 % 8) + 25 * ((n0 / 8) % 5) + 5 * ((n0 / 40) % 5) + n0 / 200;
-#pragma unroll
-        for (int r = 0; r < 5; r++) u[h][r] = s[5 * it + r];
-        Dft<T, 5, true>::run(u[h]);
-      }
+      for (int r = 0; r < 5; r++) u[h][r] = s[5 * it + r];
+      Dft<T, 5, true>::run(u[h]);
     }
-    __syncthreads();
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int n0 = tid + h * nt;
-      if (n0 < 1000) {
-#pragma unroll
-        for (int r = 0; r < 5; r++) s[n0 + 1000 * r] = u[h][r];
-      }
-    }
-    __syncthreads();
   }
+  __syncthreads();
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int n0 = tid + h * nt;
+    if (n0 < 1000) {
+#pragma unroll
+      for (int r = 0; r < 5; r++) s[n0 + 1000 * r] = u[h][r];
+    }
+  }
+  __syncthreads();
 }
 
-// ROWS image rows per CTA (rows ROWS y .. ROWS y + ROWS - 1): with two, every barrier
-// interval holds twice the work and the radix-8 stage's 1250 items fill 512 threads better
-// (three rounds at 81 % instead of two at 61 %), at one CTA (160 KB) per SM instead of two.
-template <typename T, typename TO, int ROWS = 1>
-__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, ROWS == 1 ? 2 : 1)
+template <typename T, typename TO>
+__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
     k_rows_c2r5_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm, TO* __restrict__ out,
                    int S, const C2<T>* __restrict__ twx, unsigned planar) {
   constexpr int NX = 10000;
@@ -425,44 +411,39 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, ROWS == 1 ? 2 :
   cg::cluster_group cl = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C2<T>* s = reinterpret_cast<C2<T>*>(smem_raw);
+  const int row = blockIdx.y;
   const int k = (int)cl.block_rank(), quad = blockIdx.x >> 2, q = 4 * quad + k;
-  if (q < nm && ((planar >> q) & 1u)) {  // the direct form's real map: copy its rows
-    for (int rr = 0; rr < ROWS; rr++) {
-      const TO* src = reinterpret_cast<const TO*>(specs + (long)q * spec_stride) + (long)(blockIdx.y * ROWS + rr) * NX;
-      T* d = reinterpret_cast<T*>(s + 5000 * rr);
-      for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = T(src[n]);
-    }
+  if (q < nm && ((planar >> q) & 1u)) {  // the direct form's real map: copy its row
+    const TO* src = reinterpret_cast<const TO*>(specs + (long)q * spec_stride) + (long)row * NX;
+    T* d = reinterpret_cast<T*>(s);
+    for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = T(src[n]);
   } else if (q < nm) {
-    const C2<T>* a0 = specs + (long)q * spec_stride + (long)(blockIdx.y * ROWS) * pitch;
-    c2r5_row<T, ROWS>(a0, a0 + pitch, twx, s);
+    c2r5_row<T>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
   } else {
-    for (int n = threadIdx.x; n < ROWS * NX / 2; n += blockDim.x) s[n] = C2<T>{T(0), T(0)};
+    for (int n = threadIdx.x; n < NX / 2; n += blockDim.x) s[n] = C2<T>{T(0), T(0)};
   }
   cl.sync();  // every row of the cluster is in its CTA's shared memory
   const int W = S - 4 * quad < 4 ? S - 4 * quad : 4;
   constexpr int CH = NX / 4;
   const int x0 = k * CH, x1 = x0 + CH;
+  TO* dst = out + (long)row * NX * S + 4 * quad;
+  if (W == 4) {
+    const T* src[4];
 #pragma unroll
-  for (int rr = 0; rr < ROWS; rr++) {
-    TO* dst = out + (long)(blockIdx.y * ROWS + rr) * NX * S + 4 * quad;
-    if (W == 4) {
-      const T* src[4];
+    for (int r = 0; r < 4; r++) src[r] = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
+    for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
+      TO v[4];
 #pragma unroll
-      for (int r = 0; r < 4; r++) src[r] = reinterpret_cast<const T*>(cl.map_shared_rank(s + 5000 * rr, r));
-      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) {
-        TO v[4];
+      for (int r = 0; r < 4; r++) v[r] = out_cvt<TO>(src[r][x]);
+      float4* d = reinterpret_cast<float4*>(dst + (long)x * S);
+      const float4* wv = reinterpret_cast<const float4*>(v);
 #pragma unroll
-        for (int r = 0; r < 4; r++) v[r] = out_cvt<TO>(src[r][x]);
-        float4* d = reinterpret_cast<float4*>(dst + (long)x * S);
-        const float4* wv = reinterpret_cast<const float4*>(v);
-#pragma unroll
-        for (int i = 0; i < (int)(4 * sizeof(TO) / 16); i++) d[i] = wv[i];
-      }
-    } else {
-      for (int r = 0; r < W; r++) {
-        const T* sr = reinterpret_cast<const T*>(cl.map_shared_rank(s + 5000 * rr, r));
-        for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = out_cvt<TO>(sr[x]);
-      }
+      for (int i = 0; i < (int)(4 * sizeof(TO) / 16); i++) d[i] = wv[i];
+    }
+  } else {
+    for (int r = 0; r < W; r++) {
+      const T* sr = reinterpret_cast<const T*>(cl.map_shared_rank(s, r));
+      for (int x = x0 + threadIdx.x; x < x1; x += blockDim.x) dst[(long)x * S + r] = out_cvt<TO>(sr[x]);
     }
   }
   // no CTA leaves while the others still read its shared memory (relaxed: see k_rows_c2r3_il)
@@ -1141,12 +1122,11 @@ bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, lo
                          void* out, unsigned planar) {
   using K = void (*)(const C2<T>*, long, long, int, TO*, int, const C2<T>*, unsigned);
   K k = nullptr;
-  int J = 0, nthr = 256, rows = 1;
+  int J = 0, nthr = 256;
   switch (p.M) {
     case 5000:
       if constexpr (std::is_same<T, ff>::value) {
-        rows = c2r5_rows_choice(ctx, p);
-        k = rows == 2 ? k_rows_c2r5_il<T, TO, 2> : k_rows_c2r5_il<T, TO, 1>;
+        k = k_rows_c2r5_il<T, TO>;
         nthr = 512;
       } else {
         k = k_rows_c2r3_il<T, 8, 25, 25, TO>;
@@ -1159,13 +1139,13 @@ bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, lo
     default: return false;
   }
   if (!rows_c2r_interleave_supported(p)) return false;
-  const size_t smem = ((size_t)rows * p.M + J) * sizeof(C2<T>);
+  const size_t smem = ((size_t)p.M + J) * sizeof(C2<T>);
   set_max_smem((const void*)k, smem);
   const int quads = (nm + 3) / 4;
   {
     MLC_KSCOPE(ctx, "fft_rows_c2r_interleave");
-    k<<<dim3(4 * quads, p.Ny / rows), nthr, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm,
-                                                                  (TO*)out, S, (const C2<T>*)p.twx, planar);
+    k<<<dim3(4 * quads, p.Ny), nthr, smem, ctx->stream>>>((const C2<T>*)specs, spec_stride, p.Wp, nm, (TO*)out, S,
+                                                           (const C2<T>*)p.twx, planar);
   }
   MLC_CHECK_LAUNCH();
   return true;
