@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(Epi<EPIW>::threads, 1) k_pairdiff_tc(const __g
   uint32_t* tmem_slot = (uint32_t*)(bars + 16);
   volatile int* abort_s = (volatile int*)(tmem_slot + 1);
   uint32_t* hist_s = tmem_slot + 4;
-  // nbins counters, then the two out-of-range counters (below lo, at or above hi)
+  // counters: below lo, the nbins bins, at or above hi (flushed to the global layout: bins, below, above)
   float4* colv = (float4*)(hist_s + ((P.nbins + 2 + 3) & ~3));  // [EPIW][16] column constants
   const uint32_t hist_sa = tc::smem_u32(hist_s);
 
@@ -308,34 +308,43 @@ __global__ void __launch_bounds__(Epi<EPIW>::threads, 1) k_pairdiff_tc(const __g
             const float t2 = fmaf(-X1, s0 * 0x1p-8f, t1);
             const float w = fmaf(X3, 0x1p-8f, X2);
             float chi2 = t2 + fmaf(-w, s0 * 0x1p-16f, e + (aff.y + b.y));
-            // below that the float-float form: with this assembly almost no warp enters it (the
-            // earlier form, good to (|P|^2+|Q|^2)/16, sent some lane of most warps there)
-            if (chi2 < 0x1p-14f * ab)
-              chi2 = chi2_assemble(aff, make_float2(b.x, b.y), X0 * s0, X1 * (s0 * 0x1p-8f), X2 * (s0 * 0x1p-16f),
-                                   X3 * (s0 * 0x1p-24f), __uint_as_float(r4[c]) * (s0 * 0x1p-32f));
-            // below 1e-7 (|P|^2+|Q|^2) the float-float rounding (about 2^-40 of it) could exceed
-            // 1e-5 relative; those, the top-k candidates and (matrix mode) pairs within the
-            // quantisation-error bound go to the exact FP64 list (which also histograms them)
-            float bound = fmaxf(1e-7f * ab, P.thr);
+            // One test for the rare cases: lim is at least every bound below, so a value at or
+            // above it needs neither the float-float form nor the exact list.
+            float lim = fmaxf(0x1p-14f * ab, P.thr);
+            float qbound = 0.f;
             if constexpr (OUT) {
               const float q = pa + b.z * 0x1p-33f;
-              bound = fmaxf(bound, P.refine_f * q * q);
+              qbound = P.refine_f * q * q;
+              lim = fmaxf(lim, qbound);
             }
-            if (chi2 < bound) {
-              const unsigned k = atomicAdd(P.nref, 1u);
-              if (k < P.rcap) {
-                P.ri[k] = i;
-                P.rj[k] = j;
+            if (chi2 < lim) {
+              // below 2^-14 (|P|^2+|Q|^2) the float-float form: with this assembly almost no
+              // warp enters it (the earlier form, good to (|P|^2+|Q|^2)/16, sent some lane of
+              // most warps there)
+              if (chi2 < 0x1p-14f * ab)
+                chi2 = chi2_assemble(aff, make_float2(b.x, b.y), X0 * s0, X1 * (s0 * 0x1p-8f), X2 * (s0 * 0x1p-16f),
+                                     X3 * (s0 * 0x1p-24f), __uint_as_float(r4[c]) * (s0 * 0x1p-32f));
+              // below 1e-7 (|P|^2+|Q|^2) the float-float rounding (about 2^-40 of it) could
+              // exceed 1e-5 relative; those, the top-k candidates and (matrix mode) pairs within
+              // the quantisation-error bound go to the exact FP64 list (which also histograms
+              // them)
+              const float bound = fmaxf(fmaxf(1e-7f * ab, P.thr), qbound);
+              if (chi2 < bound) {
+                const unsigned k = atomicAdd(P.nref, 1u);
+                if (k < P.rcap) {
+                  P.ri[k] = i;
+                  P.rj[k] = j;
+                }
+                continue;
               }
-              continue;
             }
             if constexpr (OUT) P.out[(long)i * P.NB + j] = chi2;
             // chi2 >= 1e-7 (|P|^2+|Q|^2) > 0 here; a subnormal one (flat curves) falls out of range
             float lg;
             asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(lg) : "f"(chi2));
             const int bin = __float2int_rd(fmaf(lg, P.hscale, P.hoff));
-            const uint32_t slot = (unsigned)bin < (unsigned)P.nbins ? (uint32_t)bin
-                                  : (bin < 0 ? (uint32_t)P.nbins : (uint32_t)P.nbins + 1u);
+            // shared counters: [below lo, bins 0 .. nbins-1, at or above hi]
+            const uint32_t slot = (uint32_t)(min(max(bin, -1), P.nbins) + 1);
             asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(hist_sa + 4u * slot) : "memory");
           }
         }
@@ -347,8 +356,8 @@ __global__ void __launch_bounds__(Epi<EPIW>::threads, 1) k_pairdiff_tc(const __g
       epi_sync<EPIW>();
       for (int b = (int)threadIdx.x - 128; b < P.nbins + 2; b += EPI_WARPS * 32) {
         const uint32_t v = hist_s[b];
-        if (v) {
-          atomicAdd(P.hist + b, (unsigned long long)v);
+        if (v) {  // global layout: bins 0 .. nbins-1, then below, then above
+          atomicAdd(P.hist + (b == 0 ? P.nbins : (b <= P.nbins ? b - 1 : P.nbins + 1)), (unsigned long long)v);
           hist_s[b] = 0;
         }
       }
