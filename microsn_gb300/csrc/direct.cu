@@ -231,13 +231,6 @@ int conv_direct_choice(mlc_ctx* ctx, const FftPlan2D& p, const void* map, const 
   return best.first;
 }
 
-bool c2r5_split_choice(mlc_ctx* ctx, const FftPlan2D& p) {
-  char key[64];
-  std::snprintf(key, sizeof key, "c2r5 split %dx%d", p.Nx, p.Ny);
-  auto it = ctx->tune.find(key);
-  return it != ctx->tune.end() ? it->second != 0 : false;
-}
-
 bool p1_staged_choice(mlc_ctx* ctx, const FftPlan2D& p, const std::function<void(bool)>& run) {
   char key[96];
   const char* pn = p.prec == MLC_F64 ? "f64" : p.prec == MLC_F32 ? "f32" : p.prec == PREC_FF ? "f32x2" : "f32x2->f32";

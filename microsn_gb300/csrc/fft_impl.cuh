@@ -350,65 +350,26 @@ __device__ __forceinline__ void c2r5_level(C2<T>* s, const C2<T>* w) {
   __syncthreads();
 }
 
-// The c2r input of row element k: (X_k + conj X_{M-k}) + i (X_k - conj X_{M-k}) W^-k.
 template <typename T>
-__device__ __forceinline__ C2<T> c2r5_input(const C2<T>* __restrict__ a, const C2<T>* __restrict__ twx, int k) {
-  constexpr int M = 5000;
-  const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
-  const C2<T> e = cadd(xk, xm);
-  const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
-  return C2<T>{e.x - o.y, e.y + o.x};
-}
-
-// SPLIT: the radix-8 stage as its two halves, with a barrier between them -- the DFT-4s
-// of the even and the odd inputs (1250 items), stored as the registers hold them, then the
-// radix-2 combinations with their twiddles (2500 items) -- the same operations in the same
-// order as Dft<T, 8> on one thread, so the same values; 625 whole items on 512 threads
-// leave 399 threads idle through a second round, 1250 and 2500 items fill the rounds.
-template <typename T, bool SPLIT = false>
 __device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a, const C2<T>* __restrict__ twx, C2<T>* s) {
   constexpr int M = 5000, J = 625;
   C2<T>* w = s + M;  // W_625^e = W_Nx^(16 e), e < 625
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < J; e += nt) w[e] = ldc(twx + 16L * e);
-  if constexpr (SPLIT) {
-    // E = DFT4 of inputs q = 0, 2, 4, 6 into s[k J + j], O = DFT4 of q = 1, 3, 5, 7 into
-    // s[(4 + k) J + j], k < 4
-    for (int it = tid; it < 2 * J; it += nt) {
-      const int p = it / J, j = it - p * J;
-      C2<T> u[4];
+  for (int j = tid; j < J; j += nt) {
+    C2<T> v[8];
 #pragma unroll
-      for (int r = 0; r < 4; r++) u[r] = c2r5_input<T>(a, twx, J * (2 * r + p) + j);
-      Dft<T, 4, true>::run(u);
-#pragma unroll
-      for (int r = 0; r < 4; r++) s[(4 * p + r) * J + j] = u[r];
+    for (int q = 0; q < 8; q++) {
+      const int k = J * q + j;
+      const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
+      const C2<T> e = cadd(xk, xm);
+      const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
+      v[q] = C2<T>{e.x - o.y, e.y + o.x};
     }
-    __syncthreads();
-    // X[k] = E[k] + W8^k O[k], X[k + 4] = E[k] - W8^k O[k] (inverse W8 = (1 + i)/sqrt 2), then
-    // the stage twiddles W_M^-(j n1)
-    const T rt = (T)0.70710678118654752440084436210485;
-    for (int it = tid; it < 4 * J; it += nt) {
-      const int kq = it / J, j = it - kq * J;
-      const C2<T> e = s[kq * J + j], o = s[(4 + kq) * J + j];
-      C2<T> ot;
-      if (kq == 0) ot = o;
-      else if (kq == 1) ot = C2<T>{rt * (o.x - o.y), rt * (o.x + o.y)};
-      else if (kq == 2) ot = mul_mi<T, true>(o);
-      else ot = C2<T>{-rt * (o.x + o.y), rt * (o.x - o.y)};
-      const C2<T> lo = cadd(e, ot), hi = csub(e, ot);
-      s[kq * J + j] = kq == 0 ? lo : cmulc(lo, ldc(twx + 2L * j * kq));
-      s[(4 + kq) * J + j] = cmulc(hi, ldc(twx + 2L * j * (4 + kq)));
-    }
-  } else {
-    for (int j = tid; j < J; j += nt) {
-      C2<T> v[8];
+    Dft<T, 8, true>::run(v);
+    s[j] = v[0];
 #pragma unroll
-      for (int q = 0; q < 8; q++) v[q] = c2r5_input<T>(a, twx, J * q + j);
-      Dft<T, 8, true>::run(v);
-      s[j] = v[0];
-#pragma unroll
-      for (int n1 = 1; n1 < 8; n1++) s[n1 * J + j] = cmulc(v[n1], ldc(twx + 2L * j * n1));  // W_M^-(j n1)
-    }
+    for (int n1 = 1; n1 < 8; n1++) s[n1 * J + j] = cmulc(v[n1], ldc(twx + 2L * j * n1));  // W_M^-(j n1)
   }
   __syncthreads();
   c2r5_level<T, 625>(s, w);
@@ -441,7 +402,7 @@ __device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a, const C2<T
   __syncthreads();
 }
 
-template <typename T, typename TO, bool SPLIT = false>
+template <typename T, typename TO>
 __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
     k_rows_c2r5_il(const C2<T>* __restrict__ specs, long spec_stride, long pitch, int nm, TO* __restrict__ out,
                    int S, const C2<T>* __restrict__ twx, unsigned planar) {
@@ -457,7 +418,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
     T* d = reinterpret_cast<T*>(s);
     for (int n = threadIdx.x; n < NX; n += blockDim.x) d[n] = T(src[n]);
   } else if (q < nm) {
-    c2r5_row<T, SPLIT>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
+    c2r5_row<T>(specs + (long)q * spec_stride + (long)row * pitch, twx, s);
   } else {
     for (int n = threadIdx.x; n < NX / 2; n += blockDim.x) s[n] = C2<T>{T(0), T(0)};
   }
@@ -1165,7 +1126,7 @@ bool c2r_interleave_impl(mlc_ctx* ctx, const FftPlan2D& p, const void* specs, lo
   switch (p.M) {
     case 5000:
       if constexpr (std::is_same<T, ff>::value) {
-        k = c2r5_split_choice(ctx, p) ? k_rows_c2r5_il<T, TO, true> : k_rows_c2r5_il<T, TO, false>;
+        k = k_rows_c2r5_il<T, TO>;
         nthr = 512;
       } else {
         k = k_rows_c2r3_il<T, 8, 25, 25, TO>;

@@ -200,9 +200,6 @@ std::string autotune_report(mlc_ctx* ctx);
 // stages the map-spectrum tile in shared memory.  The autotuner times run(false) and
 // run(true) once per key; a pinned or earlier choice is reused.
 bool p1_staged_choice(mlc_ctx* ctx, const FftPlan2D& p, const std::function<void(bool)>& run);
-// The float-float 5000-point last pass with its radix-8 stage split in two halves: the
-// pinned "c2r5 split <Nx>x<Ny>" tune key, else the whole stage per item.
-bool c2r5_split_choice(mlc_ctx* ctx, const FftPlan2D& p);
 // Cached profile spectra: the profile's spectrum as the fused convolution's P1 holds it
 // before the product with the map spectrum (Ny x Wp complex of the plan's arithmetic, the
 // map spectrum's layout), and conv_fused_spectrum starting from it.  Supported where P1 has

@@ -153,28 +153,3 @@ def test_p1_staged_and_prefetched_forms_agree(lib_built, prec, key):
         m.close()
         c.close()
     assert torch.equal(out[0], out[1])
-
-
-def test_last_pass_split_radix8_equals_whole(lib_built):
-    """The float-float 5000-point last pass with its radix-8 stage split into the DFT-4 halves
-    and their radix-2 combinations (pinned) against the whole stage per item: the same
-    operations in the same order, so the same light curves bit for bit."""
-    import microsn_gb300 as mlc
-    N = 10000
-    mp = synth.lognormal_map(N, seed=19).astype(np.float32)
-    profs = [mlc.profile(s, r, 1.0, ref_compat=False) for s, r in (("uniform", 4.0), ("exponential", 9.0),
-                                                                    ("gaussian", 2.5))]
-    x0, y0, phi, v, off, t = synth.tracks(2000, N, 40.0, 8, epochs=(10, 60), v_range=(0.5, 3.0))
-    arrs = dict(zip(("x0", "y0", "phi", "v", "off", "t"), (x0, y0, phi, v, off, t)))
-    outs = []
-    for split in (0, 1):
-        c = mlc.Context(0)
-        c.tune_set("c2r5 split 10000x10000", split)
-        m = mlc.Map(c, mp, "f32")
-        m.set_fft("f32x2")
-        tr = {k: torch.as_tensor(np.ascontiguousarray(a, np.int64 if k == "off" else np.float32), device=DEV)
-              for k, a in arrs.items()}
-        outs.append(mlc.convolve_sample_tracks(c, m, profs, tr, mag=True).cpu())
-        m.close()
-        c.close()
-    assert torch.equal(outs[0], outs[1])
