@@ -101,7 +101,8 @@ int mlc_ctx_set_timing(mlc_ctx* ctx, int on);
  * profile size) of an FP32 fused convolution the first call times the FFT form against
  * the direct tiled form's tile shapes (mlc_convolve_direct) on the context's stream and
  * keeps the fastest; likewise the fused convolution's P1 variant per map size and
- * arithmetic, and the pair kernel's epilogue width per shape class.  Later calls reuse the
+ * arithmetic, the pair kernel's epilogue width per shape class and the track sampler's
+ * order (track or map cell) for large calls.  Later calls reuse the
  * choice.  Tuning synchronises the stream once
  * per key and is skipped while the stream is captured into a CUDA graph.  Off: the FFT
  * form everywhere (results then do not depend on timings).  The report lists every tuned
@@ -118,7 +119,10 @@ int mlc_ctx_autotune_report(mlc_ctx* ctx, char* buf, int cap);
  *     batched step's key, where the second convolution chain runs alongside (not timed:
  *     0 unless pinned);
  *   "pairdiff_tc K<64|128>[ matrix] bins<1024|4096> pairs~4^<k>": epilogue warps 12, 16
- *     or 24.
+ *     or 24;
+ *   "sample_tracks_il order <Nx>x<Ny> <f32|f64> x<stride> epochs~2^<k>": the track sampler
+ *     in track order (0) or in map-cell order (1); "sample_tracks_il cell-order" pins it for
+ *     every size.
  * Other values fall back to the default. */
 int mlc_ctx_tune_set(mlc_ctx* ctx, const char* key, int choice);
 

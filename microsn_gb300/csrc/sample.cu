@@ -3,6 +3,7 @@
 // magnitude conversion fused in; plus the offset-minimised chi2 against one observed
 // curve.
 #include <cmath>
+#include <cstdio>
 
 #include "bilinear.cuh"
 #include <algorithm>
@@ -374,19 +375,18 @@ __global__ void __launch_bounds__(256) k_sample_chunks_il(const T* __restrict__ 
 // (64-byte pixels, where track order already reads the map only about twice) run 8 % slower
 // -- their 7 GB of light curves are then written in scattered 128-byte pieces instead of
 // track after track.  A pinned "sample_tracks_il cell-order" tune key (0 or 1) decides
-// instead.
-static bool il_cell_order(mlc_ctx* ctx, long npix, int stride, size_t es, int64_t nep) {
-  auto it = ctx->tune.find("sample_tracks_il cell-order");
-  if (it != ctx->tune.end()) return it->second != 0;
+// instead; with the autotuner on, large calls (a map above L2 and at least 2^20 epochs)
+// time both orders once per size class and keep the faster.
+static bool il_cell_heuristic(long npix, int stride, size_t es, int64_t nep) {
   return stride * es <= 16 && (double)npix * stride * es > 256e6 &&
          nep >= 4 * npix / (CHUNK_CELL * CHUNK_CELL) * CHUNK_EPOCHS;
 }
 
 template <typename T>
-static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int ntracks,
-                           const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
-                           const void* t, int mag, void* out, long E, int64_t ebase, int64_t nep) {
-  if (nep > 0 && il_cell_order(ctx, (long)Nx * Ny, stride, sizeof(T), nep)) {
+static void sample_il_run(mlc_ctx* ctx, bool cell, const void* imap, int stride, int nmaps, int Nx, int Ny,
+                          int ntracks, const void* x0, const void* y0, const void* phi, const void* v,
+                          const int64_t* off, const void* t, int mag, void* out, long E, int64_t ebase, int64_t nep) {
+  if (nep > 0 && cell) {
     const long nchunks = (long)((nep + CHUNK_EPOCHS - 1) / CHUNK_EPOCHS);
     const int ncx = ceil_div(Nx, CHUNK_CELL), ncy = ceil_div(Ny, CHUNK_CELL), ncells = ncx * ncy;
     MLC_REQUIRE(nchunks < (1L << 32), MLC_ERR_LIMIT, "more than 2^37 epochs in one sampling call");
@@ -441,6 +441,64 @@ static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps
     default: MLC_IL_LAUNCH(16); break;
   }
 #undef MLC_IL_LAUNCH
+}
+
+template <typename T>
+static void sample_il_impl(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int ntracks,
+                           const void* x0, const void* y0, const void* phi, const void* v, const int64_t* off,
+                           const void* t, int mag, void* out, long E, int64_t ebase, int64_t nep) {
+  auto run = [&](bool cell) {
+    sample_il_run<T>(ctx, cell, imap, stride, nmaps, Nx, Ny, ntracks, x0, y0, phi, v, off, t, mag, out, E, ebase,
+                     nep);
+  };
+  const long npix = (long)Nx * Ny;
+  auto pin = ctx->tune.find("sample_tracks_il cell-order");
+  if (pin != ctx->tune.end()) return run(pin->second != 0);
+  bool cell = il_cell_heuristic(npix, stride, sizeof(T), nep);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  MLC_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
+  if (ctx->autotune && cs == cudaStreamCaptureStatusNone && (double)npix * stride * sizeof(T) > 256e6 &&
+      nep >= (1 << 20)) {
+    int lg = 0;
+    while ((int64_t)1 << (lg + 1) <= nep) lg++;
+    char key[96];
+    std::snprintf(key, sizeof key, "sample_tracks_il order %dx%d %s x%d epochs~2^%d", Nx, Ny,
+                  sizeof(T) == 8 ? "f64" : "f32", stride, lg);
+    auto it = ctx->tune.find(key);
+    if (it != ctx->tune.end()) return run(it->second != 0);
+    // both orders write the same values: time each once, keep the faster
+    const bool saved = ctx->timing;
+    ctx->timing = false;
+    float ms[2] = {0.f, 0.f};
+    cudaEvent_t a = nullptr, b = nullptr;
+    try {
+      MLC_CUDA(cudaEventCreate(&a));
+      MLC_CUDA(cudaEventCreate(&b));
+      for (int o = 0; o < 2; o++) {
+        MLC_CUDA(cudaEventRecord(a, ctx->stream));
+        run(o == 1);
+        MLC_CUDA(cudaEventRecord(b, ctx->stream));
+        MLC_CUDA(cudaEventSynchronize(b));
+        MLC_CUDA(cudaEventElapsedTime(&ms[o], a, b));
+      }
+    } catch (...) {
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+      ctx->timing = saved;
+      throw;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx->timing = saved;
+    cell = ms[1] < ms[0];
+    ctx->tune[key] = cell ? 1 : 0;
+    ctx->tune_name[key] = cell ? "cell-order" : "track-order";
+    char rec[80];
+    std::snprintf(rec, sizeof rec, "track-order=%.4f cell-order=%.4f", ms[0], ms[1]);
+    ctx->tune_log[key] = rec;
+    return;  // the outputs are written (by both runs)
+  }
+  run(cell);
 }
 
 void sample_tracks_il(mlc_ctx* ctx, const void* imap, int stride, int nmaps, int Nx, int Ny, int prec, int ntracks,
