@@ -118,22 +118,30 @@ __global__ void __launch_bounds__(256) k_pd_quantize(const double* __restrict__ 
   const int lane = threadIdx.x & 31;
   const long r = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (r >= Npad) return;
+  // The smallest e with rowmax 2^-e <= QMAX, from the bits of rowmax = (1 + f 2^-52) 2^E0
+  // (GB300's FP64 pipe is narrow; log2 and exp2 here had cost more than the rest of the
+  // kernel): QMAX = 8355711 lies in [2^22, 2^23), so e = E0 - 22 when (1 + f 2^-52) 2^22 <=
+  // QMAX, i.e. f <= (QMAX - 2^22) 2^30, else E0 - 21.  Subnormal or zero maxima keep PD_EMIN.
   int e = PD_EMIN;
   if (r < N && rowmax[r] > 0) {
-    e = (int)ceil(log2(rowmax[r] / (double)PD_QMAX));
-    if (rowmax[r] * exp2(-(double)e) > (double)PD_QMAX) e++;  // guard the rounding of log2
+    const long long b = __double_as_longlong(rowmax[r]);
+    const int E0 = (int)((b >> 52) & 0x7ff) - 1023;
+    const long long f = b & 0xFFFFFFFFFFFFFll;
+    if (E0 > -1023) e = E0 - 22 + (f > ((long long)(PD_QMAX - (1 << 22)) << 30) ? 1 : 0);
     if (e > PD_EMAX) atomicExch(err, 2);
     e = max(PD_EMIN, min(PD_EMAX, e));
   }
-  const double inv_delta = exp2(-(double)e);
+  const double inv_delta = __longlong_as_double((long long)(1023 - e) << 52);  // 2^-e exactly
   uint16_t* row = ops + r * (3L * Kp);
   long long acc = 0;
   for (int t = lane; t < Kp; t += 32) {
     int q = 0;
     if (r < N && t < T) {
-      const double x = rint(v[r * T + t] * inv_delta);
-      if (!(fabs(x) <= (double)PD_QMAX)) atomicExch(err, 1);
-      q = (int)fmax(fmin(x, (double)PD_QMAX), -(double)PD_QMAX);
+      // v 2^-e is exact; rounded to the nearest integer (ties to even, as rint), NaN and
+      // infinities convert out of range
+      const long long x = __double2ll_rn(v[r * T + t] * inv_delta);
+      if (!(x >= -PD_QMAX && x <= PD_QMAX)) atomicExch(err, 1);
+      q = (int)max((long long)-PD_QMAX, min((long long)PD_QMAX, x));
     }
     int s2 = ((q % 256) + 256 + 128) % 256 - 128;  // balanced digit
     int r1 = (q - s2) / 256;
@@ -148,7 +156,7 @@ __global__ void __launch_bounds__(256) k_pd_quantize(const double* __restrict__ 
   if (lane == 0) {
     norm2[r] = acc;
     // |P|^2 in natural units, alpha 2^(2e), as a float-float pair (exact scaling in FP64)
-    const double v2 = (double)acc * exp2(2.0 * e);
+    const double v2 = (double)acc * __longlong_as_double((long long)(1023 + 2 * e) << 52);  // 2^(2e)
     const float hi = (float)v2;
     norm2_ff[r] = make_float2(hi, (float)(v2 - (double)hi));
     exps[r] = e;
