@@ -150,13 +150,13 @@ __device__ __forceinline__ void load_pix(const T* __restrict__ p, T* v) {
 
 // One epoch of one track on an interleaved map: with the bilinear weights of its position
 // (TrackGeom::at), every map's value (or magnitude) into out[q * E + o].
-template <typename T, int NM, int CB = 16>
+template <typename T, int NM>
 __device__ __forceinline__ void sample_epoch(const T* __restrict__ imap, int Nx, const Bilin<T>& B, int mag,
                                              T* __restrict__ out, long E, int nm_out, int64_t o) {
-  // CB bytes of maps at a time (16: 4 FP32 / 2 FP64): the four corners of one chunk in
+  // 16 bytes of maps at a time (4 FP32 / 2 FP64): the four corners of one chunk in
   // registers, not all NM maps of all four corners (which needed 100 registers and left
   // 2 CTAs per SM, too few warps to hide the gather latency)
-  constexpr int CH = (NM * (int)sizeof(T) >= CB) ? CB / (int)sizeof(T) : NM;
+  constexpr int CH = (NM * (int)sizeof(T) >= 16) ? 16 / (int)sizeof(T) : NM;
   const T* pa = imap + ((long)B.iu * Nx + B.jl) * NM;
   const T* pb = imap + ((long)B.iu * Nx + B.jr) * NM;
   const T* pc = imap + ((long)B.il * Nx + B.jl) * NM;
@@ -190,7 +190,7 @@ __device__ __forceinline__ void sample_epoch(const T* __restrict__ imap, int Nx,
 
 // One warp per track, lanes over epochs; each epoch reads 4 corners x NM interleaved
 // values and writes nm_out light-curve values out[q*E + e].
-template <typename T, int NM, int CB = 16>
+template <typename T, int NM>
 __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ imap, int Nx, int Ny, int ntracks,
                                                           const T* __restrict__ x0, const T* __restrict__ y0,
                                                           const T* __restrict__ phi, const T* __restrict__ v,
@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(256) k_sample_tracks_il(const T* __restrict__ 
   const TrackGeom<T> g(x0[track], y0[track], phi[track], v[track]);
   const int64_t e0 = off[track], e1 = off[track + 1];
   for (int64_t e = e0 + lane; e < e1; e += 32)
-    sample_epoch<T, NM, CB>(imap, Nx, g.at(t[e], Nx, Ny), mag, out, E, nm_out, e - ebase);
+    sample_epoch<T, NM>(imap, Nx, g.at(t[e], Nx, Ny), mag, out, E, nm_out, e - ebase);
 }
 
 // FP32 with a contiguous output (width == S, off == 0, W in {4, 8, 16}), npix % 4 == 0 and
@@ -428,26 +428,17 @@ static void sample_il_run(mlc_ctx* ctx, bool cell, const void* imap, int stride,
     return;
   }
   const int grid = ceil_div(ntracks, 8);
-  // bytes of each corner per load round: 16, or 32 where pinned ("sample_tracks_il chunk")
-  auto cb = ctx->tune.find("sample_tracks_il chunk");
-  const bool wide = cb != ctx->tune.end() && cb->second == 32 && stride * (int)sizeof(T) >= 32;
-#define MLC_IL_LAUNCH(NMV, CBV)                                                                                 \
-  k_sample_tracks_il<T, NMV, CBV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, Nx, Ny, ntracks, (const T*)x0, \
-                                                                   (const T*)y0, (const T*)phi, (const T*)v, off, \
-                                                                   (const T*)t, mag, (T*)out, E, nmaps, ebase)
+#define MLC_IL_LAUNCH(NMV)                                                                                    \
+  k_sample_tracks_il<T, NMV><<<grid, 256, 0, ctx->stream>>>((const T*)imap, Nx, Ny, ntracks, (const T*)x0,  \
+                                                              (const T*)y0, (const T*)phi, (const T*)v, off, \
+                                                              (const T*)t, mag, (T*)out, E, nmaps, ebase)
   MLC_KSCOPE(ctx, "sample_tracks_il");
   switch (stride) {
-    case 1: MLC_IL_LAUNCH(1, 16); break;
-    case 2: MLC_IL_LAUNCH(2, 16); break;
-    case 4: MLC_IL_LAUNCH(4, 16); break;
-    case 8:
-      if (wide) MLC_IL_LAUNCH(8, 32);
-      else MLC_IL_LAUNCH(8, 16);
-      break;
-    default:
-      if (wide) MLC_IL_LAUNCH(16, 32);
-      else MLC_IL_LAUNCH(16, 16);
-      break;
+    case 1: MLC_IL_LAUNCH(1); break;
+    case 2: MLC_IL_LAUNCH(2); break;
+    case 4: MLC_IL_LAUNCH(4); break;
+    case 8: MLC_IL_LAUNCH(8); break;
+    default: MLC_IL_LAUNCH(16); break;
   }
 #undef MLC_IL_LAUNCH
 }
