@@ -1375,10 +1375,11 @@ def main():
     e2e_step()
     ctx.synchronize()
     esteps = args.steps
-    # three timed loops of K calls (the overlap of uploads, kernels and downloads on the host
-    # link varies from loop to loop); the median is reported, all three are listed
+    # five timed loops of K calls (the host link is shared with other jobs on the machine, so
+    # the overlap of uploads, kernels and downloads varies from loop to loop); the median is
+    # reported, all five are listed
     reps = []
-    for _ in range(3):
+    for _ in range(5):
         barrier()
         e0.record(stream)
         for _ in range(esteps):
@@ -1388,7 +1389,7 @@ def main():
         ctx.synchronize()
         barrier()
         reps.append(e0.elapsed_time(e1) / esteps)
-    e2e_ms = sorted(reps)[1]
+    e2e_ms = sorted(reps)[2]
     if world > 1:  # the slowest rank's time
         te = torch.tensor([e2e_ms], device=dev)
         torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)

@@ -545,6 +545,15 @@ int mlc_histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double l
 int mlc_histogram_f64_noalloc(mlc_ctx* ctx, long n, const double* v, int nbins, double lo, double hi, int logscale,
                               uint64_t* counts_host);
 
+/* Self-test of the bounded-wait error path of the tensor-core kernels (no reference
+ * counterpart).  One CTA allocates tensor memory as k_pairdiff_tc does, waits on an mbarrier
+ * that nothing arrives at and that no copy or MMA feeds, gives up after `polls` polls
+ * (1 .. 2^24), releases its tensor memory and returns.  report_host[3]: [0] 1 if the wait
+ * gave up, [1] polls used, [2] 1 if the tensor memory was released after it.  Returns
+ * MLC_ERR_TIMEOUT with the message of a timed-out wait (the expected outcome), after which
+ * the context stays usable; waits for its stream before it returns. */
+int mlc_selftest_wait_timeout(mlc_ctx* ctx, unsigned polls, unsigned* report_host);
+
 /* ======================================================================= host-side stages (C++, FP64) */
 
 /* setup_chi2_calculation (cpu_functions.cpp:80-144) with find_indices (:28-45), M = {MA, MB},

@@ -112,6 +112,7 @@ SIGNATURES = {
     "mlc_ctx_set_profile_cache": (i32, [vp, C.c_longlong]),
     "mlc_pair_chi2_sides": (i32, [vp, vp, vp, i32, f64, f64, vp, i32, vp, vp, vp, vp, vp]),
     "mlc_histogram_f64_noalloc": (i32, [vp, C.c_long, vp, i32, f64, f64, i32, vp]),
+    "mlc_selftest_wait_timeout": (i32, [vp, C.c_uint, vp]),
     "mlc_setup_chi2": (i32, [f64, f64, f64, f64, i32, vp, vp, vp, i32, vp, i32, P_i32, vp, vp, vp, vp, vp, vp,
                              P_f64]),
     "mlc_locations_grid": (i32, [i32, i32, i32, vp, vp]),

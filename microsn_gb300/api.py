@@ -720,6 +720,15 @@ def histogram_f64(ctx: Context, v: torch.Tensor, nbins: int, lo: float, hi: floa
     return out
 
 
+def selftest_wait_timeout(ctx: Context, polls: int = 4096):
+    """Runs the bounded-wait self-test (mlc_selftest_wait_timeout).  Returns (status, report):
+    status MLC_ERR_TIMEOUT (4) when the wait gave up, as it should; report = [gave up, polls
+    used, tensor memory released].  The context stays usable either way."""
+    rep = np.zeros(3, np.uint32)
+    st = ctx.L.mlc_selftest_wait_timeout(ctx.h, int(polls), _ptr(rep))
+    return st, rep
+
+
 def bin_edges(Nbins: int, mn: float, mx: float, log: bool = True) -> np.ndarray:
     out = np.zeros(Nbins)
     st = _lib.load().mlc_bin_edges(Nbins, mn, mx, int(log), _ptr(out))

@@ -741,6 +741,11 @@ int mlc_pair_side_destroy(mlc_pair_side* side) {
   return MLC_OK;
 }
 
+int mlc_selftest_wait_timeout(mlc_ctx* ctx, unsigned polls, unsigned* report_host) {
+  if (!ctx || !report_host) return fail(ctx, MLC_ERR_ARG, "null argument");
+  return guarded(ctx, [&] { selftest_wait_timeout(ctx, polls, report_host); });
+}
+
 int mlc_pair_chi2_sides(mlc_ctx* ctx, const mlc_pair_side* A, const mlc_pair_side* B, int nbins, double lo_log10,
                         double hi_log10, uint64_t* hist_host, int k, double* topk_val_host, int64_t* topk_i_host,
                         int64_t* topk_j_host, float* chi2_out, mlc_pair_stats* stats) {

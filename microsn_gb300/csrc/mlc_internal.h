@@ -199,6 +199,9 @@ std::string autotune_report(mlc_ctx* ctx);
 // The fused convolution's P1 variant for this map size and arithmetic: true for the one that
 // stages the map-spectrum tile in shared memory.  The autotuner times run(false) and
 // run(true) once per key; a pinned or earlier choice is reused.
+// Runs k_wait_selftest (pairtc.cu) with the given poll limit; report_host[3] as documented
+// at mlc_selftest_wait_timeout.  Throws MLC_ERR_TIMEOUT when the wait gave up.
+void selftest_wait_timeout(mlc_ctx* ctx, unsigned polls, unsigned* report_host);
 bool p1_staged_choice(mlc_ctx* ctx, const FftPlan2D& p, const std::function<void(bool)>& run);
 // Cached profile spectra: the profile's spectrum as the fused convolution's P1 holds it
 // before the product with the map spectrum (Ny x Wp complex of the plan's arithmetic, the

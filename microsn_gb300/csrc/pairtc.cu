@@ -876,4 +876,56 @@ void pairdiff_sides(mlc_ctx* ctx, const PdSide& A, const PdSide& B, int nbins, d
                 tj, out, res);
 }
 
+// Self-test of the bounded-wait unwinding the pair kernel relies on: one CTA allocates TMEM
+// like the pair kernel, waits on an mbarrier that nothing arrives at and that no copy or MMA
+// feeds (so nothing asynchronous is in flight when the wait gives up), records that it gave
+// up, releases its TMEM and records that too.  report[0]: the wait gave up; report[1]: polls
+// used; report[2]: TMEM released after it.
+__global__ void __launch_bounds__(64) k_wait_selftest(uint32_t limit, unsigned* report) {
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tslot;
+  const int warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_barrier_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&tslot, 32);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tslot;
+  uint32_t polls = 0;
+  bool done = false;
+  for (; polls < limit && !done; polls++) done = tc::mbar_try_wait(&bar, 0);
+  if (threadIdx.x == 0) {
+    report[0] = done ? 0u : 1u;
+    report[1] = polls;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(tmem, 32);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) report[2] = 1u;
+}
+
+void selftest_wait_timeout(mlc_ctx* ctx, unsigned polls, unsigned* report_host) {
+  MLC_REQUIRE(polls >= 1 && polls <= (1u << 24), MLC_ERR_ARG, "polls: 1 .. 2^24");
+  unsigned* rep = (unsigned*)ws_get(ctx, WS_SMALL, 4 * sizeof(unsigned));
+  MLC_CUDA(cudaMemsetAsync(rep, 0, 4 * sizeof(unsigned), ctx->stream));
+  {
+    MLC_KSCOPE(ctx, "wait_selftest");
+    k_wait_selftest<<<1, 64, 0, ctx->stream>>>(polls, rep);
+  }
+  MLC_CHECK_LAUNCH();
+  unsigned h[4];
+  MLC_CUDA(cudaMemcpyAsync(h, rep, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  MLC_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int i = 0; i < 3; i++) report_host[i] = h[i];
+  MLC_REQUIRE(h[2] == 1u, MLC_ERR_CUDA, "wait self-test: TMEM was not released");
+  MLC_REQUIRE(h[0] == 0u, MLC_ERR_TIMEOUT, "wait self-test: the bounded wait gave up after its poll limit");
+}
+
 }  // namespace mlc

@@ -142,5 +142,16 @@ __device__ __forceinline__ void tmem_ld(uint32_t taddr, uint32_t* r) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// Placed after tmem_wait_ld: the registers a tmem_ld wrote are read only after the wait (the
+// compiler sees them as written here).
+template <int N>
+__device__ __forceinline__ void reg_fence(uint32_t* r) {
+  static_assert(N == 4 || N == 8, "reg_fence: 4 or 8 registers");
+  if constexpr (N == 8)
+    asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]));
+  else
+    asm volatile("" : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]));
+}
+
 }  // namespace tc
 }  // namespace mlc
