@@ -65,22 +65,27 @@ struct Dft<T, 4, INV> {
   }
 };
 
+// The cosine part in Winograd's form: x0 + c1 sa + c2 sb and x0 + c2 sa + c1 sb are
+// u +/- m with u = x0 + (c1 + c2)/2 (sa + sb), m = (c1 - c2)/2 (sa - sb), where
+// (c1 + c2)/2 = -1/4 exactly (an exact scaling) and (c1 - c2)/2 = sqrt(5)/4: one general
+// product per component instead of four.
 template <typename T, bool INV>
 struct Dft<T, 5, INV> {
   static __device__ __forceinline__ void run(C2<T>* v) {
-    const T c1 = (T)0.30901699437494742410229341718282;   // cos(2 pi/5)
-    const T c2 = (T)-0.80901699437494742410229341718282;  // cos(4 pi/5)
+    const T b = (T)0.55901699437494742410229341718282;    // (cos(2 pi/5) - cos(4 pi/5)) / 2
     const T s1 = (T)0.95105651629515357211643933337938;   // sin(2 pi/5)
     const T s2 = (T)0.58778525229247312916870595463907;   // sin(4 pi/5)
     C2<T> x0 = v[0];
     C2<T> sa = cadd(v[1], v[4]), da = csub(v[1], v[4]);
     C2<T> sb = cadd(v[2], v[3]), db = csub(v[2], v[3]);
-    C2<T> p1 = C2<T>{x0.x + c1 * sa.x + c2 * sb.x, x0.y + c1 * sa.y + c2 * sb.y};
-    C2<T> p2 = C2<T>{x0.x + c2 * sa.x + c1 * sb.x, x0.y + c2 * sa.y + c1 * sb.y};
+    C2<T> t1 = cadd(sa, sb), t2 = csub(sa, sb);
+    C2<T> u = C2<T>{x0.x - scale2(t1.x, 0.25f), x0.y - scale2(t1.y, 0.25f)};
+    C2<T> m = C2<T>{b * t2.x, b * t2.y};
+    C2<T> p1 = cadd(u, m), p2 = csub(u, m);
     C2<T> q1 = C2<T>{s1 * da.x + s2 * db.x, s1 * da.y + s2 * db.y};
     C2<T> q2 = C2<T>{s2 * da.x - s1 * db.x, s2 * da.y - s1 * db.y};
     C2<T> iq1 = mul_mi<T, INV>(q1), iq2 = mul_mi<T, INV>(q2);
-    v[0] = cadd(x0, cadd(sa, sb));
+    v[0] = cadd(x0, t1);
     v[1] = cadd(p1, iq1);
     v[4] = csub(p1, iq1);
     v[2] = cadd(p2, iq2);

@@ -79,6 +79,13 @@ __device__ __forceinline__ ff operator*(ff a, ff b) {
   return ff(p, e);
 }
 __device__ __forceinline__ ff& operator+=(ff& a, ff b) { return a = a + b; }
+
+// x times a power of two s: exact (barring underflow), two FP32 products for float-float.
+template <typename T>
+__device__ __forceinline__ T scale2(T x, float s) {
+  return x * (T)s;
+}
+__device__ __forceinline__ ff scale2(ff x, float s) { return ff(__fmul_rn(x.hi, s), __fmul_rn(x.lo, s)); }
 __device__ __forceinline__ double ff_to_double(ff a) { return __dadd_rn((double)a.hi, (double)a.lo); }
 
 // a / b to float-float accuracy: the FP32 quotient of the normalised operands, then one
