@@ -367,9 +367,19 @@ __device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a, const C2<T
       v[q] = C2<T>{e.x - o.y, e.y + o.x};
     }
     Dft<T, 8, true>::run(v);
+    // W_M^-(j n1) = conj(W_M^j)^n1: one table load (the other powers read at strides of
+    // 2 n1 entries fetched a sector per lane), the powers by products at most three deep
+    C2<T> p[8];
+    p[1] = ldc(twx + 2L * j);
+    p[2] = cmul(p[1], p[1]);
+    p[3] = cmul(p[2], p[1]);
+    p[4] = cmul(p[2], p[2]);
+    p[5] = cmul(p[3], p[2]);
+    p[6] = cmul(p[3], p[3]);
+    p[7] = cmul(p[4], p[3]);
     s[j] = v[0];
 #pragma unroll
-    for (int n1 = 1; n1 < 8; n1++) s[n1 * J + j] = cmulc(v[n1], ldc(twx + 2L * j * n1));  // W_M^-(j n1)
+    for (int n1 = 1; n1 < 8; n1++) s[n1 * J + j] = cmulc(v[n1], p[n1]);
   }
   __syncthreads();
   c2r5_level<T, 625>(s, w);
