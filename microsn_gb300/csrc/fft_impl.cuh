@@ -609,10 +609,11 @@ __global__ void __launch_bounds__(256) k_conv_fused(const C2<T>* __restrict__ Fm
 // into L2 and read from there in stage 2: no global-load latency in stage 2, for
 // N2 CW sizeof(C2<T>) more shared memory per CTA (fewer resident CTAs).
 // MODE splits the pass around the profile's spectrum, for profiles that are convolved with
-// many maps: 1 stops after forward stage 2 and stores the profile's spectrum in the map
-// spectrum's layout into ks (as the registers hold it, so that mode 2 continues exactly as
-// mode 0 would); 2 starts from it (ks times the map spectrum, then the inverse stages) --
-// no profile sub-pass and no forward transform.  0 is the whole pass.
+// many maps: 1 stops after forward stage 2 and stores the profile's spectrum, already scaled
+// by 1/(Nx Ny), in the map spectrum's layout into ks (as the registers hold it, so that
+// mode 2 continues exactly as mode 0 would: every mode multiplies the map spectrum by the
+// scaled profile spectrum); 2 starts from it (ks times the map spectrum, then the inverse
+// stages) -- no profile sub-pass, no forward transform and no scaling.  0 is the whole pass.
 template <typename T, int CW, int L1, int L2, bool STAGE = false, int MODE = 0>
 __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) ? 6 : 0) k_conv_fused2(const C2<T>* __restrict__ Fmap, C2<T>* __restrict__ out,
                                                      long pitch, const C2<T>* __restrict__ Kx, int h, int Ny,
@@ -745,13 +746,13 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
     }
     if constexpr (MODE == 1) {  // the profile's spectrum, frequencies k1 + L1 k2 of row block kk
 #pragma unroll
-      for (int k2 = 0; k2 < L2; k2++) ks[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c] = u[k2];
+      for (int k2 = 0; k2 < L2; k2++) ks[((long)kk * N2 + g + L1 * k2) * pitch + col0 + c] = cscale(u[k2], scale);
     } else {
 #pragma unroll
       for (int k2 = 0; k2 < L2; k2++) {
         const long e = ((long)kk * N2 + g + L1 * k2) * pitch + col0 + c;
         const C2<T> f = STAGE ? fs[(g + L1 * k2) * CW + c] : Fmap[e];
-        u[k2] = cscale(cmul(f, MODE == 2 ? ks[e] : u[k2]), scale);
+        u[k2] = cmul(f, MODE == 2 ? ks[e] : cscale(u[k2], scale));
       }
       Dft<T, L2, true>::run(u);  // over k2 -> n2
       // the thread rewrites exactly the entries of y it read above: no other thread's data
@@ -1055,10 +1056,11 @@ void profile_spectrum_impl(mlc_ctx* ctx, const FftPlan2D& p, const double* prof,
   launch_rows_r2c<T>(ctx, p, ProfileRows<T>{prof, pN, h, p.Nx}, 2 * h, kx);
   const size_t smem = ((size_t)p.N2 * CW + p.N1 + 2 * (size_t)p.N2) * sizeof(C2<T>);
   set_max_smem((const void*)k, smem);
+  const T scale = (T)(1.0 / ((double)p.Nx * (double)p.Ny));  // stored with the spectrum
   {
     MLC_KSCOPE(ctx, "conv_profile_spectrum");
     k<<<dim3(ceil_div(p.Wc, CW), p.N1), nthr, smem, ctx->stream>>>(nullptr, nullptr, p.Wp, (const C2<T>*)kx, h,
-                                                                     p.Ny, p.N1, (const C2<T>*)p.twy, T(0),
+                                                                     p.Ny, p.N1, (const C2<T>*)p.twy, scale,
                                                                      (C2<T>*)ks);
   }
   MLC_CHECK_LAUNCH();
