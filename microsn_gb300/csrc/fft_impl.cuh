@@ -313,8 +313,9 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
 // The same last pass for float-float rows of M = 5000 = 8 x 5^4 points, with levels small
 // enough for 64 registers: a float-float DFT25 item of the three-level form holds 100
 // registers of data alone, which left two CTAs of 256 threads (16 warps) per SM, waiting
-// on its barriers.  Here level 1 is the three-level form's (DFT8 over stride 625 from global
-// memory, twiddle W_M^-(j n1)); then in-place decimation-in-frequency radix-5 levels on
+// on its barriers.  Here the c2r sequence b is formed first, both partners k and M - k of
+// one read of the row (into shared memory); level 1 is the three-level form's (DFT8 over
+// stride 625, twiddle W_M^-(j n1)), in place; then in-place decimation-in-frequency radix-5 levels on
 // blocks of 625, 125, 25 (item (block, m < J'/5): DFT5 over stride J'/5, twiddle
 // W_J'^-(m r), written back to the slots it read, so a thread takes its items one after
 // another with no barrier between them); the last radix-5 level on blocks of 5 reads its
@@ -356,30 +357,38 @@ __device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a, const C2<T
   C2<T>* w = s + M;  // W_625^e = W_Nx^(16 e), e < 625
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < J; e += nt) w[e] = ldc(twx + 16L * e);
+  // b[k] = e + i o with e = X[k] + conj X[M-k], o = (X[k] - conj X[M-k]) W^-k, and for the
+  // partner M - k: e' = conj e and, as W^-(M-k) = -conj W^-k, o' = conj o, so
+  // b[M-k] = (e.x + o.y, o.x - e.y).  One thread forms both from one read of each input.
+  for (int k = tid; k <= M / 2; k += nt) {
+    const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
+    const C2<T> e = cadd(xk, xm);
+    const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
+    s[k] = C2<T>{e.x - o.y, e.y + o.x};
+    if (k > 0 && k < M / 2) s[M - k] = C2<T>{e.x + o.y, o.x - e.y};
+  }
+  __syncthreads();
+  // item j reads b[J q + j] (q < 8) and writes its outputs to the same eight slots
   for (int j = tid; j < J; j += nt) {
     C2<T> v[8];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int k = J * q + j;
-      const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
-      const C2<T> e = cadd(xk, xm);
-      const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
-      v[q] = C2<T>{e.x - o.y, e.y + o.x};
-    }
+    for (int q = 0; q < 8; q++) v[q] = s[J * q + j];
     Dft<T, 8, true>::run(v);
     // W_M^-(j n1) = conj(W_M^j)^n1: one table load (the other powers read at strides of
-    // 2 n1 entries fetched a sector per lane), the powers by products at most three deep
-    C2<T> p[8];
-    p[1] = ldc(twx + 2L * j);
-    p[2] = cmul(p[1], p[1]);
-    p[3] = cmul(p[2], p[1]);
-    p[4] = cmul(p[2], p[2]);
-    p[5] = cmul(p[3], p[2]);
-    p[6] = cmul(p[3], p[3]);
-    p[7] = cmul(p[4], p[3]);
+    // 2 n1 entries fetched a sector per lane), the powers by products at most three deep,
+    // each used as soon as it is formed
     s[j] = v[0];
-#pragma unroll
-    for (int n1 = 1; n1 < 8; n1++) s[n1 * J + j] = cmulc(v[n1], p[n1]);
+    const C2<T> p1 = ldc(twx + 2L * j);
+    s[J + j] = cmulc(v[1], p1);
+    const C2<T> p2 = cmul(p1, p1);
+    s[2 * J + j] = cmulc(v[2], p2);
+    const C2<T> p3 = cmul(p2, p1);
+    s[3 * J + j] = cmulc(v[3], p3);
+    const C2<T> p4 = cmul(p2, p2);
+    s[4 * J + j] = cmulc(v[4], p4);
+    s[5 * J + j] = cmulc(v[5], cmul(p3, p2));
+    s[6 * J + j] = cmulc(v[6], cmul(p3, p3));
+    s[7 * J + j] = cmulc(v[7], cmul(p4, p3));
   }
   __syncthreads();
   c2r5_level<T, 625>(s, w);
