@@ -588,6 +588,16 @@ double mlc_trapezium(int N, const double* f1, const double* f2, const double* x)
  * the size only; otherwise it receives the Nx*Nx FP64 magnifications. */
 int mlc_read_gerlumph(const char* dir, int* Nx, double* width, double* meta6, double* out_host, long cap);
 
+/* Page-locked host memory for the host-buffer calls (MLC_IO_HOST), on 2 MB pages: anonymous
+ * memory advised for transparent huge pages (small pages where the host has none free) and
+ * registered with the CUDA driver for every context.  The host-to-GPU copies of such buffers
+ * keep their rate when the host memory is fragmented, where buffers pinned on small pages
+ * lose part of it.  bytes are rounded up to 2 MB; the memory is zero-filled.  Returns
+ * MLC_ERR_OOM when the host is out of memory, MLC_ERR_CUDA when the registration fails (no
+ * GPU).  mlc_host_free releases a buffer from mlc_host_alloc (NULL is ignored). */
+int mlc_host_alloc(size_t bytes, void** ptr);
+int mlc_host_free(void* ptr);
+
 /* ======================================================================= synthetic maps */
 
 /* Inverse ray shooting (no reference counterpart; produces the gerlumph ray counts the

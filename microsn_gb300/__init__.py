@@ -14,7 +14,7 @@ from .api import convolve_sample_tracks, map_binned_mpd, mpd_divide, mpd_normali
 from .api import flux_ratio_chi2, track_chi2_offset  # noqa: F401
 from .api import convolve_many, sample_expanding  # noqa: F401
 from .api import FIT_PARAMS, TrackChi2, fit_raster, radius_stack, track_chi2, track_fit  # noqa: F401
-from .api import selftest_wait_timeout  # noqa: F401
+from .api import host_empty, selftest_wait_timeout  # noqa: F401
 from ._lib import MlcError
 
 __all__ = [
@@ -24,5 +24,5 @@ __all__ = [
     "track_fit",
     "expanding_source", "histogram_f64", "locations_grid", "locations_random", "pair_bin_fused", "profile",
     "profile_raster", "read_gerlumph", "sample_tracks", "sample_tracks_interleaved", "interleave_maps", "setup_chi2_calculation", "setup_integral", "sort_f64_u32",
-    "trapezium", "selftest_wait_timeout",
+    "trapezium", "selftest_wait_timeout", "host_empty",
 ]

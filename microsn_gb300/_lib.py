@@ -120,6 +120,8 @@ SIGNATURES = {
     "mlc_bin_edges": (i32, [i32, f64, f64, i32, vp]),
     "mlc_trapezium": (f64, [i32, vp, vp, vp]),
     "mlc_read_gerlumph": (i32, [C.c_char_p, P_i32, P_f64, vp, vp, C.c_long]),
+    "mlc_host_alloc": (i32, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    "mlc_host_free": (i32, [vp]),
     "mlc_rayshoot": (i32, [vp, vp, i32, f64, f64, f64, f64, f64, C.c_long, C.c_long, f64, i32, vp]),
 }
 

@@ -720,6 +720,41 @@ def histogram_f64(ctx: Context, v: torch.Tensor, nbins: int, lo: float, hi: floa
     return out
 
 
+class _HostBuffer:
+    """One mlc_host_alloc buffer, released when the last array or tensor on it is gone."""
+
+    def __init__(self, nbytes: int):
+        self.L = _lib.load()
+        p = C.c_void_p()
+        st = self.L.mlc_host_alloc(nbytes, C.byref(p))
+        if st:
+            raise MlcError(st, "mlc_host_alloc failed (host memory or registration with the CUDA driver)")
+        self.ptr = p.value
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            self.L.mlc_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+
+_NP_OF = {torch.float32: np.float32, torch.float64: np.float64, torch.int64: np.int64, torch.int32: np.int32,
+          torch.uint8: np.uint8}
+
+
+def host_empty(shape, dtype=torch.float32) -> torch.Tensor:
+    """A zero-filled CPU tensor in page-locked host memory on 2 MB pages (mlc_host_alloc),
+    for the host-buffer form of the library calls: its copies to and from the GPU keep
+    their rate when the host's memory is fragmented."""
+    shape = tuple(shape) if isinstance(shape, (tuple, list)) else (int(shape),)
+    numel = int(np.prod(shape)) if shape else 1
+    nbytes = max(numel * torch.empty((), dtype=dtype).element_size(), 1)
+    owner = _HostBuffer(nbytes)
+    raw = (C.c_char * nbytes).from_address(owner.ptr)
+    raw._owner = owner
+    arr = np.frombuffer(raw, dtype=np.uint8).view(_NP_OF[dtype])[:numel].reshape(shape)
+    return torch.from_numpy(arr)
+
+
 def selftest_wait_timeout(ctx: Context, polls: int = 4096):
     """Runs the bounded-wait self-test (mlc_selftest_wait_timeout).  Returns (status, report):
     status MLC_ERR_TIMEOUT (4) when the wait gave up, as it should; report = [gave up, polls

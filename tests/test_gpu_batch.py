@@ -134,6 +134,39 @@ def test_host_io_async_back_to_back(bctx):
     m.close()
 
 
+def test_host_buffers_on_huge_pages(bctx):
+    """mlc_host_alloc buffers (2 MB pages, registered): page-locked, zero-filled, and the
+    asynchronous host-buffer step through them equals the device-buffer step."""
+    import microsn_gb300 as mlc
+    N = 240
+    mp = synth.lognormal_map(N, seed=45).astype(np.float32)
+    m = mlc.Map(bctx, mp, "f32")
+    profs = _profiles(5)
+    trh = _host_tracks(600, N, 46, np.float32)
+    trp = {}
+    for k, a in trh.items():
+        x = mlc.host_empty(a.shape, torch.from_numpy(a).dtype)
+        assert x.is_pinned() and not x.any()
+        x.copy_(torch.from_numpy(a))
+        trp[k] = x
+    pix = mlc.host_empty((N, N), torch.float32)
+    pix.copy_(torch.from_numpy(mp))
+    E = int(trh["off"][-1])
+    out = mlc.host_empty((len(profs), E), torch.float32)
+    mlc.convolve_sample_tracks(bctx, m, profs, trp, mag=True, pixels=pix, out=out, async_=True)
+    bctx.synchronize()
+    ref = mlc.convolve_sample_tracks(bctx, m, profs, _device(trh), mag=True,
+                                     pixels=torch.as_tensor(mp, device=DEV)).cpu()
+    assert torch.equal(out, ref)
+    m.close()
+    del trp, pix, out  # released through mlc_host_free
+    import ctypes
+    L = mlc._lib.load()
+    assert L.mlc_host_free(ctypes.c_void_p(None)) == 0
+    p = ctypes.c_void_p()
+    assert L.mlc_host_alloc(0, ctypes.byref(p)) == 1  # MLC_ERR_ARG
+
+
 def test_join_orders_copies_on_the_stream(bctx):
     import microsn_gb300 as mlc
     N = 200
