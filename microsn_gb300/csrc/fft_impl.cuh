@@ -780,7 +780,8 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
 #pragma unroll
     for (int n1 = 0; n1 < L1; n1++) {
       const int n = g + L2 * n1;
-      out[((long)kk * N2 + n) * pitch + col0 + c] = cfin(cmulc(v[n1], w2[n]));
+      // not renormalised: the P2 sub-pass that reads it renormalises what it stores
+      out[((long)kk * N2 + n) * pitch + col0 + c] = cmulc(v[n1], w2[n]);
     }
   }
 }

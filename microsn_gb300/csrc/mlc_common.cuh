@@ -99,7 +99,8 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
 }
 
 // Values stored between passes are renormalised (3 operations per value) so that the low
-// parts cannot keep growing from pass to pass; FP32 and FP64 values pass unchanged.
+// parts cannot keep growing from pass to pass, at least every second pass (the convolution's
+// P1 leaves that to the P2 sub-pass after it); FP32 and FP64 values pass unchanged.
 template <typename T>
 __device__ __forceinline__ T fin(T v) { return v; }
 __device__ __forceinline__ ff fin(ff v) { return ff_norm(v); }
