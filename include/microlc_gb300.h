@@ -537,8 +537,8 @@ int mlc_histogram_f64(mlc_ctx* ctx, long n, const double* v, int nbins, double l
  * library (96 KB on every device that loads it, held until the process exits), so no
  * cudaMalloc, cudaFree or allocating library routine is called.  nbins is limited to
  * 12000; larger requests return MLC_ERR_LIMIT.  The first call on a device resolves the
- * array's device address (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  Every call clears the counters it uses, but all calls
+ * array's device address (cudaGetSymbolAddress) with that device current.  Every call
+ * clears the counters it uses, but all calls
  * on a device share the one array: calls that overlap on the GPU (other streams, other
  * contexts, other host threads) race and must be serialised by the caller.  The call copies
  * the counts to counts_host and waits for its stream before it returns. */
