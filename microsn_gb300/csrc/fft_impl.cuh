@@ -360,13 +360,22 @@ __device__ __forceinline__ void c2r5_row(const C2<T>* __restrict__ a, const C2<T
   // b[k] = e + i o with e = X[k] + conj X[M-k], o = (X[k] - conj X[M-k]) W^-k, and for the
   // partner M - k: e' = conj e and, as W^-(M-k) = -conj W^-k, o' = conj o, so
   // b[M-k] = (e.x + o.y, o.x - e.y).  One thread forms both from one read of each input.
-  for (int k = tid; k <= M / 2; k += nt) {
-    const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k)));
+  // two partners' loads in flight per thread at a time (the row comes from DRAM)
+  auto form = [&](int k, C2<T> xk, C2<T> xm, C2<T> w) {
     const C2<T> e = cadd(xk, xm);
-    const C2<T> o = cmulc(csub(xk, xm), ldc(twx + k));  // (X - conj X') W^-k
+    const C2<T> o = cmulc(csub(xk, xm), w);  // (X - conj X') W^-k
     s[k] = C2<T>{e.x - o.y, e.y + o.x};
     if (k > 0 && k < M / 2) s[M - k] = C2<T>{e.x + o.y, o.x - e.y};
+  };
+  int k = tid;
+  for (; k + nt <= M / 2; k += 2 * nt) {
+    const int k2 = k + nt;
+    const C2<T> xk = ldc(a + k), xm = cconj(ldc(a + (M - k))), w = ldc(twx + k);
+    const C2<T> xk2 = ldc(a + k2), xm2 = cconj(ldc(a + (M - k2))), w2 = ldc(twx + k2);
+    form(k, xk, xm, w);
+    form(k2, xk2, xm2, w2);
   }
+  if (k <= M / 2) form(k, ldc(a + k), cconj(ldc(a + (M - k))), ldc(twx + k));
   __syncthreads();
   // item j reads b[J q + j] (q < 8) and writes its outputs to the same eight slots
   for (int j = tid; j < J; j += nt) {
