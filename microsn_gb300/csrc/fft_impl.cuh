@@ -322,7 +322,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(256)
 // items, waits, and writes them in natural order: output r of item
 // it = 125 k1 + 25 a + 5 b + c is z[k1 + 8 (a + 5 (b + 5 (c + 5 r)))] = z[n0 + 1000 r].  512 threads, two
 // CTAs (32 warps) per SM, the same number of barriers as the three-level form.
-template <typename T, int JP>
+template <typename T, int JP, bool INV = true>
 __device__ __forceinline__ void c2r5_level(C2<T>* s, const C2<T>* w) {
   constexpr int SP = JP / 5, WS = 625 / JP, NB = 5000 / JP;
   for (int it = threadIdx.x; it < 1000; it += blockDim.x) {
@@ -343,10 +343,10 @@ __device__ __forceinline__ void c2r5_level(C2<T>* s, const C2<T>* w) {
     C2<T> u[5];
 #pragma unroll
     for (int r = 0; r < 5; r++) u[r] = b[r * SP];
-    Dft<T, 5, true>::run(u);
+    Dft<T, 5, INV>::run(u);
     b[0] = u[0];
 #pragma unroll
-    for (int r = 1; r < 5; r++) b[r * SP] = cmulc(u[r], w[m * r * WS]);
+    for (int r = 1; r < 5; r++) b[r * SP] = INV ? cmulc(u[r], w[m * r * WS]) : cmul(u[r], w[m * r * WS]);
   }
   __syncthreads();
 }
@@ -476,6 +476,68 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
   }
   // no CTA leaves while the others still read its shared memory (relaxed: see k_rows_c2r3_il)
   asm volatile("barrier.cluster.arrive.relaxed.aligned;\n\tbarrier.cluster.wait.aligned;" ::: "memory");
+}
+
+// The forward counterpart of c2r5_row for float-float rows of M = 5000: level 1 (DFT8 over
+// stride 625 of the loader's pairs, twiddles W_M^(j k1) as products of the one loaded
+// W_M^j), the three radix-5 levels and the last one in natural order as in c2r5_row (forward
+// DFTs, unconjugated twiddles), then the split into Nx/2+1 spectrum values and the zero
+// padding up to Wp.  512 threads, two CTAs per SM, like the last pass.
+template <typename Loader>
+__global__ void __launch_bounds__(512, 2) k_rows_r2c5(Loader ld, C2<ff>* __restrict__ out, long pitch,
+                                                      const C2<ff>* __restrict__ twx) {
+  constexpr int M = 5000, J = 625;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C2<ff>* s = reinterpret_cast<C2<ff>*>(smem_raw);
+  C2<ff>* w = s + M;  // W_625^e = W_Nx^(16 e), e < 625
+  const int tid = threadIdx.x, nt = blockDim.x, row = blockIdx.x;
+  for (int e = tid; e < J; e += nt) w[e] = ldc(twx + 16L * e);
+  for (int j = tid; j < J; j += nt) {
+    C2<ff> v[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) v[q] = ld.pair(row, J * q + j);
+    Dft<ff, 8, false>::run(v);
+    s[j] = v[0];
+    const C2<ff> p1 = ldc(twx + 2L * j);
+    s[J + j] = cmul(v[1], p1);
+    const C2<ff> p2 = cmul(p1, p1);
+    s[2 * J + j] = cmul(v[2], p2);
+    const C2<ff> p3 = cmul(p2, p1);
+    s[3 * J + j] = cmul(v[3], p3);
+    const C2<ff> p4 = cmul(p2, p2);
+    s[4 * J + j] = cmul(v[4], p4);
+    s[5 * J + j] = cmul(v[5], cmul(p3, p2));
+    s[6 * J + j] = cmul(v[6], cmul(p3, p3));
+    s[7 * J + j] = cmul(v[7], cmul(p4, p3));
+  }
+  __syncthreads();
+  c2r5_level<ff, 625, false>(s, w);
+  c2r5_level<ff, 125, false>(s, w);
+  c2r5_level<ff, 25, false>(s, w);
+  C2<ff> u[2][5];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int n0 = tid + h * nt;
+    if (n0 < 1000) {
+      const int it = 125 * (n0 % 8) + 25 * ((n0 / 8) % 5) + 5 * ((n0 / 40) % 5) + n0 / 200;
+#pragma unroll
+      for (int r = 0; r < 5; r++) u[h][r] = s[5 * it + r];
+      Dft<ff, 5, false>::run(u[h]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int n0 = tid + h * nt;
+    if (n0 < 1000) {
+#pragma unroll
+      for (int r = 0; r < 5; r++) s[n0 + 1000 * r] = u[h][r];
+    }
+  }
+  __syncthreads();
+  C2<ff>* o = out + (long)row * pitch;
+  for (int k = tid; k <= M; k += nt) o[k] = cfin(r2c_split(s, M, twx, k));
+  for (int k = M + 1 + tid; k < pitch; k += nt) o[k] = C2<ff>{ff(0), ff(0)};
 }
 
 // ---------------------------------------------------------------- column kernels
@@ -832,9 +894,21 @@ static void launch_rows_r2c(mlc_ctx* ctx, const FftPlan2D& p, const Loader& ld, 
     using K3 = void (*)(Loader, C2<T>*, long, const C2<T>*);
     K3 k3 = nullptr;
     int J = 0;
-    // FP32 and FP64 only: the float-float forward pass runs once per map, and its register
-    // kernels would double the float-float units' compile time
-    if constexpr (!std::is_same<T, ff>::value) {
+    // float-float: the five-level kernel of 5000-point rows (the three-level ones would
+    // double the float-float units' compile time)
+    if constexpr (std::is_same<T, ff>::value) {
+      if (p.M == 5000) {
+        auto k5 = k_rows_r2c5<Loader>;
+        const size_t smem5 = (size_t)(5000 + 625) * sizeof(C2<ff>);
+        set_max_smem((const void*)k5, smem5);
+        {
+          MLC_KSCOPE(ctx, name);
+          k5<<<nrows, 512, smem5, ctx->stream>>>(ld, (C2<ff>*)out, p.Wp, (const C2<ff>*)p.twx);
+        }
+        MLC_CHECK_LAUNCH();
+        return;
+      }
+    } else {
       switch (p.M) {
         case 5000: k3 = k_rows_r2c3<T, 8, 25, 25, Loader>; J = 625; break;
         case 4096: k3 = k_rows_r2c3<T, 16, 16, 16, Loader>; J = 256; break;
