@@ -104,3 +104,17 @@ def test_errors_are_status_codes(lib_built):
         mlc.profile_raster(mlc.profile("gaussian", -1.0, 0.01))
     with pytest.raises(mlc.MlcError):
         mlc.bin_edges(0, 1, 2)
+
+
+def test_host_alloc_argument_errors(lib_built):
+    """mlc_host_alloc / mlc_host_free argument handling (no GPU needed): zero bytes and a null
+    out-pointer are refused, NULL frees as a no-op, an unknown pointer is refused."""
+    import ctypes
+    from microsn_gb300 import _lib
+    L = _lib.load()
+    p = ctypes.c_void_p()
+    assert L.mlc_host_alloc(0, ctypes.byref(p)) == 1 and not p.value  # MLC_ERR_ARG
+    assert L.mlc_host_alloc(4096, None) == 1
+    assert L.mlc_host_free(None) == 0
+    buf = ctypes.create_string_buffer(64)
+    assert L.mlc_host_free(ctypes.cast(buf, ctypes.c_void_p)) == 1  # not from mlc_host_alloc
