@@ -1319,8 +1319,8 @@ def main():
                 "share_of_step": per_step[dom] / total_k if total_k else None}
         if HEADLINE_FFT == "f32x2" and dom in ("fft_rows_c2r_interleave", "conv_fused_spectrum", "fft_col_A"):
             roof["note"] = ("float-float transform pass: its DRAM traffic equals the algorithmic bytes, and it is "
-                            "bound by the FP32 pipe that carries the float-float arithmetic and by its CTA barriers "
-                            "(ncu: profiles/step_ff_10000.md), not by HBM")
+                            "bound by the FP32 pipe that carries the float-float arithmetic (65-74 % FMA, ncu: "
+                            "profiles/step_ff_10000.md), not by HBM")
     kernels = {k: {"ms_per_step": v, "launches_per_step": kt[k][1] / ksteps,
                    "GB_per_s": (algorithmic_bytes(k, n, E, len(profs), es=spec_es) / (kt[k][0] / kt[k][1] / 1000.0) / 1e9)
                    if algorithmic_bytes(k, n, E, len(profs), es=spec_es) else None} for k, v in per_step.items()}
