@@ -87,33 +87,55 @@ def test_inverse_row_decomposition_matches_irfft(L1, L2, L3):
     np.testing.assert_allclose(row, Nx * x, rtol=0, atol=1e-9 * Nx * np.abs(x).sum())
 
 
-def radix5_levels(b, twx):
-    """c2r5_row (float-float rows of M = 5000 = 8 x 5^4): level 1 as in three_level
-    (inverse DFT8 over stride 625, twiddle W_M^-(j n1)), then in-place decimation-in-frequency
-    radix-5 levels on blocks of 625, 125, 25 (item (block, m): inverse DFT5 over stride J'/5,
-    twiddle W_J'^-(m r), written back to the slots it read) and blocks of 5, whose outputs go
-    to natural order: output r of item it = 125 k1 + 25 a + 5 b + c is z[n0 + 1000 r] with
-    n0 = k1 + 8 (a + 5 (b + 5 c))."""
+def radix5_levels(b, twx, inv=True):
+    """c2r5_row (float-float rows of M = 5000 = 8 x 5^4; inv=False: the forward mirror in
+    k_rows_r2c5): level 1 as in three_level (DFT8 over stride 625, twiddle W_M^(-/+)(j n1),
+    formed in the kernels as products of the one loaded power W_M^j, at most three deep),
+    then in-place decimation-in-frequency radix-5 levels on blocks of 625, 125, 25 (item
+    (block, m): DFT5 over stride J'/5, twiddle W_J'^(-/+)(m r), written back to the slots it
+    read) and blocks of 5, whose outputs go to natural order: output r of item
+    it = 125 k1 + 25 a + 5 b + c is z[n0 + 1000 r] with n0 = k1 + 8 (a + 5 (b + 5 c))."""
     M, J = 5000, 625
+    conj = np.conj if inv else (lambda v: v)
     s = np.empty(M, complex)
     for j in range(J):
-        v = _dft(b[J * np.arange(8) + j], True)
+        v = _dft(b[J * np.arange(8) + j], inv)
+        p1 = twx[2 * j]
+        p2 = p1 * p1
+        p3 = p2 * p1
+        p4 = p2 * p2
+        pw = [1.0, p1, p2, p3, p4, p3 * p2, p3 * p3, p4 * p3]
         for n1 in range(8):
-            s[n1 * J + j] = v[n1] * np.conj(twx[2 * j * n1])
+            s[n1 * J + j] = v[n1] * conj(pw[n1])
     w = twx[16 * np.arange(J)]  # W_625^e
     for Jp in (625, 125, 25):
         Sp, ws = Jp // 5, 625 // Jp
         for it in range(1000):
             blk, m = divmod(it, Sp)
             idx = blk * Jp + m + Sp * np.arange(5)
-            u = _dft(s[idx], True)
-            s[idx] = u * np.conj(w[m * np.arange(5) * ws])
+            u = _dft(s[idx], inv)
+            s[idx] = u * conj(w[m * np.arange(5) * ws])
     z = np.empty(M, complex)
     for it in range(1000):
-        u = _dft(s[5 * it + np.arange(5)], True)
+        u = _dft(s[5 * it + np.arange(5)], inv)
         k1, a5, b5, c5 = it // 125, (it // 25) % 5, (it // 5) % 5, it % 5
         z[k1 + 8 * (a5 + 5 * (b5 + 5 * c5)) + 1000 * np.arange(5)] = u
     return z
+
+
+def c2r_input_pairs(X, twx):
+    """c2r5_row's input: one read of X[k] and X[M-k] (k <= M/2) gives b[k] = e + i o and, for
+    the partner, b[M-k] = (e.x + o.y) + i (o.x - e.y), with e = X[k] + conj X[M-k] and
+    o = (X[k] - conj X[M-k]) W^-k."""
+    M = X.shape[0] - 1
+    b = np.empty(M, complex)
+    for k in range(M // 2 + 1):
+        e = X[k] + np.conj(X[M - k])
+        o = (X[k] - np.conj(X[M - k])) * np.conj(twx[k])
+        b[k] = complex(e.real - o.imag, e.imag + o.real)
+        if 0 < k < M // 2:
+            b[M - k] = complex(e.real + o.imag, o.real - e.imag)
+    return b
 
 
 def test_radix5_last_pass_decomposition_matches_irfft():
@@ -122,13 +144,50 @@ def test_radix5_last_pass_decomposition_matches_irfft():
     twx = np.exp(-2j * np.pi * np.arange(Nx) / Nx)
     x = np.random.default_rng(7).lognormal(0.0, 0.5, Nx)
     X = np.fft.rfft(x)
-    k = np.arange(M)
-    xk, xm = X[k], np.conj(X[M - k])
-    b = (xk + xm) + 1j * (xk - xm) * np.conj(twx[k])
-    z = radix5_levels(b, twx)
+    z = radix5_levels(c2r_input_pairs(X, twx), twx)
     row = np.empty(Nx)
     row[0::2], row[1::2] = z.real, z.imag
     np.testing.assert_allclose(row, Nx * x, rtol=0, atol=1e-9 * Nx * np.abs(x).sum())
+
+
+def test_c2r_input_pairs_equal_direct_form():
+    M = 5000
+    Nx = 2 * M
+    twx = np.exp(-2j * np.pi * np.arange(Nx) / Nx)
+    X = np.fft.rfft(np.random.default_rng(8).lognormal(0.0, 0.5, Nx))
+    k = np.arange(M)
+    xk, xm = X[k], np.conj(X[M - k])
+    direct = (xk + xm) + 1j * (xk - xm) * np.conj(twx[k])
+    np.testing.assert_allclose(c2r_input_pairs(X, twx), direct, rtol=0, atol=1e-9 * np.abs(X).max())
+
+
+def test_radix5_forward_rows_match_rfft():
+    """k_rows_r2c5: the forward five-level transform of the row's pairs, then the split."""
+    M = 5000
+    Nx = 2 * M
+    twx = np.exp(-2j * np.pi * np.arange(Nx) / Nx)
+    x = np.random.default_rng(9).lognormal(0.0, 0.5, Nx)
+    Z = radix5_levels(x[0::2] + 1j * x[1::2], twx, inv=False)
+    X = r2c_split(Z, twx)
+    np.testing.assert_allclose(X, np.fft.rfft(x), rtol=0, atol=1e-9 * np.abs(x).sum())
+
+
+def test_winograd_dft5_matches_fft():
+    """Dft<T, 5>: the cosine part as u +/- m, u = x0 - (sa + sb)/4, m = sqrt(5)/4 (sa - sb)."""
+    rng = np.random.default_rng(10)
+    for inv in (False, True):
+        x = rng.normal(size=5) + 1j * rng.normal(size=5)
+        s1, s2 = np.sin(2 * np.pi / 5), np.sin(4 * np.pi / 5)
+        b = (np.cos(2 * np.pi / 5) - np.cos(4 * np.pi / 5)) / 2
+        sa, da, sb, db = x[1] + x[4], x[1] - x[4], x[2] + x[3], x[2] - x[3]
+        t1, t2 = sa + sb, sa - sb
+        u = x[0] - t1 / 4
+        m = b * t2
+        p1, p2 = u + m, u - m
+        q1, q2 = s1 * da + s2 * db, s2 * da - s1 * db
+        iq1, iq2 = (1j * q1, 1j * q2) if inv else (-1j * q1, -1j * q2)
+        got = np.array([x[0] + t1, p1 + iq1, p2 + iq2, p2 - iq2, p1 - iq1])
+        np.testing.assert_allclose(got, _dft(x, inv), rtol=0, atol=1e-12)
 
 
 def test_prime_factor_dft10_matches_fft():
