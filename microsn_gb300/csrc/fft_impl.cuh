@@ -615,7 +615,9 @@ __global__ void __launch_bounds__(256) k_colpass2(C2<T>* __restrict__ buf, long 
       const int j = g + L1 * k2;
       C2<T> val = u[k2];
       if (post_tw) val = INV ? cmulc(val, pw[j]) : cmul(val, pw[j]);
-      buf[(base + (long)j * j_mul) * pitch + col0 + c] = cfin(val);
+      // inverse passes store float-float values as they are: the row pass that reads them
+      // (the last of the transform) rounds each pixel from both parts
+      buf[(base + (long)j * j_mul) * pitch + col0 + c] = INV ? val : cfin(val);
     }
   }
 }
@@ -851,7 +853,7 @@ __global__ void __launch_bounds__(256, (sizeof(T) == 4 && L1 <= 10 && L2 <= 10) 
 #pragma unroll
     for (int n1 = 0; n1 < L1; n1++) {
       const int n = g + L2 * n1;
-      // not renormalised: the P2 sub-pass that reads it renormalises what it stores
+      // not renormalised (see fin in mlc_common.cuh)
       out[((long)kk * N2 + n) * pitch + col0 + c] = cmulc(v[n1], w2[n]);
     }
   }

@@ -98,9 +98,10 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
   return ff_renorm(q1, __fdiv_rn(r.hi, b.hi));
 }
 
-// Values stored between passes are renormalised (3 operations per value) so that the low
-// parts cannot keep growing from pass to pass, at least every second pass (the convolution's
-// P1 leaves that to the P2 sub-pass after it); FP32 and FP64 values pass unchanged.
+// Values stored between the passes of a forward transform are renormalised (3 operations per
+// value) so that the low parts cannot keep growing from pass to pass; the inverse column
+// passes (P1, P2) store theirs as they are, since only the last row pass follows them and it
+// rounds every pixel from both parts.  FP32 and FP64 values pass unchanged.
 template <typename T>
 __device__ __forceinline__ T fin(T v) { return v; }
 __device__ __forceinline__ ff fin(ff v) { return ff_norm(v); }
