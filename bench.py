@@ -195,6 +195,18 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x: float, device) -> float:
+    """The slowest rank's x: an all-reduce MAX over the process group (NCCL on the GPUs,
+    gloo in the CPU tests); x itself in a single process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ----------------------------------------------------------------------------- roofline helpers
 
 def peaks():
@@ -830,11 +842,7 @@ def pair_workload(args, ctx, m, profs, n, dev, world, rank, stream):
         r = pstep()
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / psteps
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / psteps, dev)
     pairs = float(N) * N
     value = world * pairs / (ms / 1000.0)
     # per-kernel times of one step
@@ -1286,11 +1294,7 @@ def main():
     barrier()
     clk = clocks.stop()
     launches = ctx.launch_count() - l0
-    ms_total = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = max_over_ranks(e0.elapsed_time(e1), dev)
     ms_step = ms_total / args.steps
     lc_per_step = len(profs) * ntracks
     value = world * lc_per_step / (ms_step / 1000.0)
@@ -1390,11 +1394,7 @@ def main():
         ctx.synchronize()
         barrier()
         reps.append(e0.elapsed_time(e1) / esteps)
-    e2e_ms = sorted(reps)[2]
-    if world > 1:  # the slowest rank's time
-        te = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(te, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(te.item())
+    e2e_ms = max_over_ranks(sorted(reps)[2], dev)  # the slowest rank's time
     e2e_val = world * lc_per_step / (e2e_ms / 1000.0)
     # the host link itself: plain 1 GiB copies between pinned host memory and HBM on this machine
     # (the light curves' download bounds the e2e step); the host memory is shared with other
